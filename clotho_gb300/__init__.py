@@ -1,0 +1,275 @@
+"""clotho_gb300 -- GB300-native (sm_103a) engine for the per-generation hot
+path of putnampp/clotho.
+
+The compute lives in libclotho_gpu.so (C-ABI, include/clotho_gpu.h).  This
+module is the Python mirror of the reference's engine and stage policies
+(examples/QTLSim/engine_batched_task.hpp:70-373) over that ABI; the C++
+mirror is clotho_gb300/cpp/clotho_policies.hpp.  There is no CPU fallback:
+every call goes to the CUDA library and raises on any error.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .tape import GenTape, neutral_tape, load_tapes, save_tapes  # noqa: F401
+
+__all__ = ["Population", "GenTape", "neutral_tape", "ClothoError", "FITNESS", "build"]
+
+# fitness_toolkit registry keys (src/clotho/fitness/fitness_toolkit.cpp:50-78)
+FITNESS = {"constant": 0, "gaussian": 1, "quadratic": 2, "gaussian_vs": 3}
+FLAG_Q1 = 1
+
+DEVICE_ERRORS = {1: "allele capacity exceeded", 2: "fixed table capacity exceeded",
+                 4: "more than 128 device-drawn events in a gamete", 8: "tape parent index out of range",
+                 16: "tape mutation row out of range", 32: "mutation capacity exceeded",
+                 64: "all fitness values zero"}
+
+
+class ClothoError(RuntimeError):
+    pass
+
+
+def build(force: bool = False) -> str:
+    from . import builder
+    return builder.build(force=force)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None and a.size else None
+
+
+class Population:
+    """One resident population on the GPU: the Engine<...,batched_task> state
+    (two population_space_row bitsets, AlleleSpace, trait_space_vector, free
+    space, fixed tables, phenotypes and fitness)."""
+
+    def __init__(self, max_individuals: int, max_alleles: int, traits: int = 1, *, max_events: int | None = None,
+                 max_mutations: int | None = None, max_fixed: int | None = None, fitness: str = "constant",
+                 fit_param: float = 1.0, mu: float = 1e-4, rho: float = 1e-4, bias: float = 0.5,
+                 p_neutral: float = 0.5, eff_mean: float = 0.0, eff_sigma: float = 1.0, seed: int = 1,
+                 q1: bool = True):
+        self.L = capi.load()
+        S = 2 * max_individuals
+        if max_events is None:
+            max_events = int(S * rho + 10 * np.sqrt(S * rho + 1) + 64)
+        if max_mutations is None:
+            max_mutations = int(S * mu + 10 * np.sqrt(S * mu + 1) + 64)
+        if max_fixed is None:
+            max_fixed = max(1024, max_alleles)
+        self.T = int(traits)
+        self.desc = capi.Desc(max_individuals, max_alleles, traits, max_events, max_mutations, max_fixed,
+                              FITNESS[fitness], FLAG_Q1 if q1 else 0, fit_param, mu, rho, bias, p_neutral,
+                              eff_mean, eff_sigma, seed)
+        h = C.c_void_p()
+        rc = self.L.clotho_create(C.byref(self.desc), C.byref(h))
+        if rc != 0:
+            raise ClothoError(f"clotho_create failed ({rc})")
+        self.h = h
+
+    # ---- lifetime
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.clotho_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, rc: int, what: str):
+        if rc != 0:
+            msg = self.L.clotho_last_error(self.h)
+            raise ClothoError(f"{what}: rc={rc}: {msg.decode() if msg else ''}")
+
+    @property
+    def footprint(self) -> int:
+        return int(self.L.clotho_footprint(self.h))
+
+    def sync(self):
+        self._ck(self.L.clotho_sync(self.h), "sync")
+
+    # ---- set-up
+    def init(self, N0: int):
+        self._ck(self.L.clotho_init(self.h, N0), "init")
+
+    def seed_population(self, N: int, pos, eff, thr, seed: int):
+        pos = np.ascontiguousarray(pos, np.float64)
+        eff = np.ascontiguousarray(eff, np.float32)
+        thr = np.ascontiguousarray(thr, np.uint32)
+        self._ck(self.L.clotho_seed_population(self.h, N, len(pos), _ptr(pos), _ptr(eff), _ptr(thr), seed),
+                 "seed_population")
+
+    # ---- fused generation (Engine::simulate)
+    def simulate(self, tape):
+        t = tape if isinstance(tape, GenTape) else GenTape(tape.N, tape.M, tape.pairs, tape.swap, tape.ev_off,
+                                                            tape.ev_pos, tape.mut_seq, tape.mut_pos, tape.mut_eff)
+        t = t.contiguous()
+        s = capi.GenTape(t.N, t.M, _ptr(t.pairs), _ptr(t.swap), _ptr(t.ev_off), _ptr(t.ev_pos), _ptr(t.mut_seq),
+                         _ptr(t.mut_pos), _ptr(t.mut_eff))
+        self._keep = t  # arrays must outlive the copy (the call waits for it anyway)
+        self._ck(self.L.clotho_generation_tape(self.h, C.byref(s)), "generation_tape")
+
+    def simulate_philox(self, N: int):
+        self._ck(self.L.clotho_generation_philox(self.h, N), "generation_philox")
+
+    def run_philox(self, N: int, G: int):
+        self._ck(self.L.clotho_run_philox(self.h, N, G), "run_philox")
+
+    # ---- staged policies
+    def begin_generation(self, N: int, M: int):
+        self._ck(self.L.clotho_begin_generation(self.h, N, M), "begin_generation")
+
+    def free_space(self):
+        c = np.zeros(3, np.uint32)
+        self._ck(self.L.clotho_free_space(self.h, _ptr(c)), "free_space")
+        return int(c[0]), int(c[1]), int(c[2])
+
+    def set_pairs(self, pairs):
+        pairs = np.ascontiguousarray(pairs, np.uint32)
+        self._ck(self.L.clotho_set_pairs(self.h, _ptr(pairs)), "set_pairs")
+
+    def select(self, N: int):
+        out = np.zeros(2 * N, np.uint32)
+        self._ck(self.L.clotho_select(self.h, _ptr(out)), "select")
+        return out
+
+    def crossover(self, swap, ev_off, ev_pos):
+        swap = np.ascontiguousarray(swap, np.uint8)
+        ev_off = np.ascontiguousarray(ev_off, np.uint32)
+        ev_pos = np.ascontiguousarray(ev_pos, np.float64)
+        self._ck(self.L.clotho_crossover(self.h, _ptr(swap), _ptr(ev_off), _ptr(ev_pos)), "crossover")
+
+    def mutate(self, mut_seq, mut_pos, mut_eff):
+        mut_seq = np.ascontiguousarray(mut_seq, np.uint32)
+        mut_pos = np.ascontiguousarray(mut_pos, np.float64)
+        mut_eff = np.ascontiguousarray(mut_eff, np.float32)
+        self._ck(self.L.clotho_mutate(self.h, _ptr(mut_seq), _ptr(mut_pos), _ptr(mut_eff)), "mutate")
+
+    def phenotype(self):
+        self._ck(self.L.clotho_phenotype(self.h), "phenotype")
+
+    def evaluate_fitness(self):
+        self._ck(self.L.clotho_fitness(self.h), "fitness")
+
+    def end_generation(self):
+        self._ck(self.L.clotho_end_generation(self.h), "end_generation")
+
+    def simulate_staged(self, tape):
+        """Engine::simulate driven stage by stage through the policy entry points."""
+        t = tape
+        self.begin_generation(t.N, t.M)
+        self.free_space()
+        self.set_pairs(t.pairs)
+        self.crossover(t.swap, t.ev_off, t.ev_pos)
+        self.mutate(t.mut_seq, t.mut_pos, t.mut_eff)
+        self.phenotype()
+        self.evaluate_fitness()
+        self.end_generation()
+
+    # ---- read-back
+    def info(self) -> dict:
+        i = capi.Info()
+        self._ck(self.L.clotho_get_info(self.h, C.byref(i)), "get_info")
+        return {n: getattr(i, n) for n, _ in capi.Info._fields_}
+
+    def check(self):
+        err = self.info()["device_error"]
+        if err:
+            raise ClothoError("device error: " + ", ".join(m for b, m in DEVICE_ERRORS.items() if err & b))
+
+    def rows(self) -> np.ndarray:
+        i = self.info()
+        out = np.zeros((2 * i["N"], i["W"]), np.uint64)
+        self._ck(self.L.clotho_get_rows(self.h, _ptr(out), out.size), "get_rows")
+        return out
+
+    def alleles(self):
+        A = self.info()["A"]
+        pos = np.zeros(A, np.float64)
+        age = np.zeros(A, np.uint32)
+        eff = np.zeros(A * self.T, np.float32)
+        self._ck(self.L.clotho_get_alleles(self.h, _ptr(pos), _ptr(age), _ptr(eff)), "get_alleles")
+        return pos, age, eff.reshape(A, self.T)
+
+    def fixed(self):
+        F = self.info()["fixed_total"]
+        pos = np.zeros(F, np.float64)
+        age = np.zeros(F, np.uint32)
+        eff = np.zeros(F * self.T, np.float32)
+        self._ck(self.L.clotho_get_fixed(self.h, _ptr(pos), _ptr(age), _ptr(eff)), "get_fixed")
+        return pos, age, eff.reshape(F, self.T)
+
+    def free_list(self) -> np.ndarray:
+        n = self.info()["free_count"]
+        out = np.zeros(n, np.uint32)
+        self._ck(self.L.clotho_get_free(self.h, _ptr(out)), "get_free")
+        return out
+
+    def genome_traits(self) -> np.ndarray:
+        S = 2 * self.info()["N"]
+        out = np.zeros(S * self.T, np.float32)
+        self._ck(self.L.clotho_get_genome_traits(self.h, _ptr(out)), "get_genome_traits")
+        return out.reshape(S, self.T)
+
+    def phenotypes(self) -> np.ndarray:
+        N = self.info()["N"]
+        out = np.zeros(N * self.T, np.float32)
+        self._ck(self.L.clotho_get_phenotypes(self.h, _ptr(out)), "get_phenotypes")
+        return out.reshape(N, self.T)
+
+    def fitness(self) -> np.ndarray:
+        N = self.info()["N"]
+        out = np.zeros(N, np.float64)
+        self._ck(self.L.clotho_get_fitness(self.h, _ptr(out)), "get_fitness")
+        return out
+
+    def pairs(self) -> np.ndarray:
+        N = self.info()["N"]
+        out = np.zeros(2 * N, np.uint32)
+        self._ck(self.L.clotho_get_pairs(self.h, _ptr(out)), "get_pairs")
+        return out
+
+    def stats(self, sfs_len: int = 0):
+        st = capi.Stats()
+        sfs = np.zeros(sfs_len, np.uint32) if sfs_len else None
+        self._ck(self.L.clotho_stats_compute(self.h, C.byref(st), _ptr(sfs), sfs_len), "stats")
+        d = {"segregating": st.segregating, "fixed_now": st.fixed_now, "mean_fitness": st.mean_fitness,
+             "mean_phenotype": list(st.mean_phenotype)[: self.T], "heterozygosity": st.heterozygosity}
+        if sfs is not None:
+            d["sfs"] = sfs
+        return d
+
+    # ---- timing
+    def profile(self, enable: bool):
+        self._ck(self.L.clotho_profile(self.h, 1 if enable else 0), "profile")
+
+    def kernel_time(self):
+        ms = C.c_double()
+        n = C.c_uint32()
+        r = C.c_uint64()
+        w = C.c_uint64()
+        self._ck(self.L.clotho_kernel_time(self.h, C.byref(ms), C.byref(n), C.byref(r), C.byref(w)), "kernel_time")
+        return ms.value, n.value, r.value, w.value
+
+    def timer_begin(self):
+        self._ck(self.L.clotho_timer_begin(self.h), "timer_begin")
+
+    def timer_end(self) -> float:
+        ms = C.c_double()
+        self._ck(self.L.clotho_timer_end(self.h, C.byref(ms)), "timer_end")
+        return ms.value
+
+    @property
+    def launches(self) -> int:
+        return int(self.L.clotho_launch_count(self.h))

@@ -1,0 +1,910 @@
+// capi.cu -- host side of the C-ABI (include/clotho_gpu.h).
+//
+// A context owns a set of resident populations (one for the plain engine) and
+// two CUDA streams: a compute stream for every kernel and a copy stream for
+// tape uploads.  Tape buffers are double-buffered so the host->device copy of
+// generation g+1 overlaps the kernels of generation g.
+#include "engine.cuh"
+#include "../../include/clotho_gpu.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace clotho;
+
+namespace {
+
+struct PopHost {
+    clotho_desc desc{};
+    PopDev dev[3]{};          // tape set 0, tape set 1, device-drawn (Philox)
+    std::vector<void*> allocs;
+    size_t bytes = 0;
+    bool acc_valid = false;   // accF/accV hold AND/OR of the current child rows
+    bool ready = false;       // init/seed done
+    uint32_t hostN = 0;       // host view of N after the last completed call
+};
+
+struct Geometry {
+    uint32_t Ncap, Scap, Wcap, Aslots, Mcap, EVcap, FXcap, T;
+};
+
+Geometry geometry(const clotho_desc& d) {
+    Geometry g{};
+    g.Ncap = d.max_individuals ? d.max_individuals : 1;
+    g.Scap = 2 * g.Ncap;
+    uint32_t w = ref_width(d.max_alleles ? d.max_alleles : 1);
+    g.Wcap = (w + kWordAlign - 1) / kWordAlign * kWordAlign;
+    g.Aslots = g.Wcap * 64u;
+    g.Mcap = d.max_mutations ? d.max_mutations : 1;
+    g.EVcap = d.max_events ? d.max_events : 1;
+    g.FXcap = d.max_fixed ? d.max_fixed : 1;
+    g.T = d.traits;
+    return g;
+}
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Byte sizes of every device array of one population, in allocation order.
+std::vector<size_t> sizes_of(const Geometry& g) {
+    const size_t S = g.Scap, N = g.Ncap, W = g.Wcap, A = g.Aslots, T = g.T;
+    return {
+        S * W * 8, S * W * 8,            // rows[0], rows[1]
+        W * 8, W * 8, W * 8,             // fixmask, accF, accV
+        A * 4, A * 8, A * 4, A * T * 4,  // free_list, pos, age, eff
+        g.FXcap * 8ull, g.FXcap * 4ull, g.FXcap * T * 4ull,
+        S * 16, N * 16, N * 8, N * 8,    // zg, zi, fit, cdf
+        (N / 1024 + 8) * 8, (S / 1024 + 8) * 4,
+        (S + 1) * 4 * 2ull,              // row_cnt, row_off
+        S * 4, g.Mcap * 4ull, g.Mcap * 4ull,  // row_cur, row_mut, mut_slot
+        sizeof(DevStatus),
+        // two tape sets: pairs, swap, ev_off, ev_pos, mut_seq, mut_pos, mut_eff
+        S * 4, S, (S + 1) * 4, g.EVcap * 8ull, g.Mcap * 4ull, g.Mcap * 8ull, g.Mcap * T * 4ull,
+        S * 4, S, (S + 1) * 4, g.EVcap * 8ull, g.Mcap * 4ull, g.Mcap * 8ull, g.Mcap * T * 4ull,
+    };
+}
+
+}  // namespace
+
+struct clotho_ctx {
+    int device = 0;
+    int num_sms = 152;
+    cudaStream_t stream = nullptr, copy_stream = nullptr;
+    std::vector<PopHost*> pops;
+    PopDev* d_pops[3] = {nullptr, nullptr, nullptr};  // per set: npops contiguous PopDev
+    WorkCtl* d_ctl = nullptr;
+    uint32_t* d_hdr[3] = {nullptr, nullptr, nullptr}; // per set: [2*npops]
+    uint32_t* h_hdr = nullptr;                          // pinned staging [2*npops]
+    uint32_t set = 0;                                    // next tape set
+    cudaEvent_t copy_done[2]{}, kern_done[2]{};
+    std::string err;
+    bool profiling = false;
+    std::vector<cudaEvent_t> prof_ev;  // pairs around each k_generation launch
+    size_t prof_used = 0;
+    double prof_ms = 0.0;
+    uint32_t prof_launches = 0;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    uint64_t launches = 0;
+    cudaGraphExec_t graph = nullptr;
+    uint32_t graph_N = 0;
+    bool in_step = false;
+    uint32_t maxW = 0, maxS = 0, maxN = 0;
+};
+
+namespace {
+
+int fail(clotho_ctx* c, int code, const std::string& m) {
+    if (c) c->err = m;
+    return code;
+}
+
+#define CK(call)                                                                    \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess)                                                      \
+            return fail(ctx, CLOTHO_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+LaunchCfg cfg(clotho_ctx* ctx) { return LaunchCfg{ctx->stream, ctx->num_sms}; }
+
+int check_launch(clotho_ctx* ctx, const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ctx, CLOTHO_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return 0;
+}
+
+void free_pop(PopHost* p) {
+    for (void* a : p->allocs) cudaFree(a);
+    p->allocs.clear();
+    delete p;
+}
+
+int alloc_pop(clotho_ctx* ctx, const clotho_desc& d, PopHost** out) {
+    if (d.traits < 1 || d.traits > kMaxTraits) return fail(ctx, CLOTHO_E_ARG, "traits must be 1..4");
+    if (d.max_individuals == 0 || d.max_alleles == 0) return fail(ctx, CLOTHO_E_ARG, "zero capacity");
+    const Geometry g = geometry(d);
+    PopHost* p = new PopHost();
+    p->desc = d;
+    std::vector<size_t> sz = sizes_of(g);
+    std::vector<void*> ptr(sz.size(), nullptr);
+    for (size_t i = 0; i < sz.size(); ++i) {
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, align256(sz[i]));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            free_pop(p);
+            return fail(ctx, CLOTHO_E_NOMEM, "device allocation refused (" + std::to_string(align256(sz[i])) + " bytes)");
+        }
+        p->allocs.push_back(q);
+        p->bytes += align256(sz[i]);
+        ptr[i] = q;
+    }
+    // zero the tables (cheap) and the status
+    for (size_t i = 2; i < sz.size(); ++i) cudaMemsetAsync(ptr[i], 0, sz[i], ctx->stream);
+    PopDev b{};
+    size_t k = 0;
+    b.rows[0] = (uint64_t*)ptr[k++]; b.rows[1] = (uint64_t*)ptr[k++];
+    b.fixmask = (uint64_t*)ptr[k++]; b.accF = (uint64_t*)ptr[k++]; b.accV = (uint64_t*)ptr[k++];
+    b.free_list = (uint32_t*)ptr[k++]; b.pos = (double*)ptr[k++]; b.age = (uint32_t*)ptr[k++]; b.eff = (float*)ptr[k++];
+    b.fx_pos = (double*)ptr[k++]; b.fx_age = (uint32_t*)ptr[k++]; b.fx_eff = (float*)ptr[k++];
+    b.zg = (float*)ptr[k++]; b.zi = (float*)ptr[k++]; b.fit = (double*)ptr[k++]; b.cdf = (double*)ptr[k++];
+    b.scan_part = (double*)ptr[k++]; b.scan_upart = (uint32_t*)ptr[k++];
+    b.row_cnt = (uint32_t*)ptr[k++];
+    b.row_off = b.row_cnt + (g.Scap + 1);
+    b.row_cur = (uint32_t*)ptr[k++]; b.row_mut = (uint32_t*)ptr[k++]; b.mut_slot = (uint32_t*)ptr[k++];
+    b.st = (DevStatus*)ptr[k++];
+    b.Scap = g.Scap; b.Ncap = g.Ncap; b.Wcap = g.Wcap; b.Acap = g.Aslots; b.Mcap = g.Mcap;
+    b.EVcap = g.EVcap; b.FXcap = g.FXcap; b.T = g.T;
+    b.mu = d.mu; b.rho = d.rho; b.bias = d.bias; b.p_neutral = d.p_neutral;
+    b.eff_mean = d.eff_mean; b.eff_sigma = d.eff_sigma; b.fit_param = d.fit_param;
+    b.exp_neg_rho = std::exp(-d.rho);
+    b.exp_neg_mu = std::exp(-d.mu);
+    b.seed = d.seed; b.fitness = d.fitness; b.flags = d.flags;
+    for (int s = 0; s < 2; ++s) {
+        PopDev t = b;
+        t.mode = kModeTape;
+        t.pairs = (uint32_t*)ptr[k++]; t.swap = (uint8_t*)ptr[k++]; t.ev_off = (uint32_t*)ptr[k++];
+        t.ev_pos = (double*)ptr[k++]; t.mut_seq = (uint32_t*)ptr[k++]; t.mut_pos = (double*)ptr[k++];
+        t.mut_eff = (float*)ptr[k++];
+        p->dev[s] = t;
+    }
+    p->dev[2] = p->dev[0];
+    p->dev[2].mode = kModePhilox;
+    *out = p;
+    return 0;
+}
+
+// Rebuild the device PopDev arrays after the population set changed.
+int sync_pop_arrays(clotho_ctx* ctx) {
+    const uint32_t n = (uint32_t)ctx->pops.size();
+    if (n > kMaxPops) return fail(ctx, CLOTHO_E_CAPACITY, "more than 256 populations");
+    for (int s = 0; s < 3; ++s) {
+        if (ctx->d_pops[s]) cudaFree(ctx->d_pops[s]);
+        if (ctx->d_hdr[s]) cudaFree(ctx->d_hdr[s]);
+        ctx->d_pops[s] = nullptr;
+        ctx->d_hdr[s] = nullptr;
+        if (!n) continue;
+        CK(cudaMalloc(&ctx->d_pops[s], sizeof(PopDev) * n));
+        CK(cudaMalloc(&ctx->d_hdr[s], sizeof(uint32_t) * 2 * n));
+        std::vector<PopDev> h(n);
+        for (uint32_t i = 0; i < n; ++i) h[i] = ctx->pops[i]->dev[s];
+        CK(cudaMemcpyAsync(ctx->d_pops[s], h.data(), sizeof(PopDev) * n, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    if (ctx->h_hdr) cudaFreeHost(ctx->h_hdr);
+    ctx->h_hdr = nullptr;
+    if (n) CK(cudaMallocHost(&ctx->h_hdr, sizeof(uint32_t) * 2 * n));
+    ctx->maxW = ctx->maxS = ctx->maxN = 0;
+    for (PopHost* p : ctx->pops) {
+        ctx->maxW = std::max(ctx->maxW, p->dev[0].Wcap);
+        ctx->maxS = std::max(ctx->maxS, p->dev[0].Scap);
+        ctx->maxN = std::max(ctx->maxN, p->dev[0].Ncap);
+    }
+    if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+DevStatus read_status(clotho_ctx* ctx, PopHost* p, int* rc) {
+    DevStatus s{};
+    cudaError_t e = cudaMemcpyAsync(&s, p->dev[0].st, sizeof(DevStatus), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    *rc = (e == cudaSuccess) ? 0 : fail(ctx, CLOTHO_E_CUDA, std::string("status read: ") + cudaGetErrorString(e));
+    return s;
+}
+
+// ---- profiling around the generation kernel
+void prof_begin(clotho_ctx* ctx) {
+    if (!ctx->profiling) return;
+    if (ctx->prof_used + 2 > ctx->prof_ev.size()) {
+        for (int i = 0; i < 64; ++i) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            ctx->prof_ev.push_back(e);
+        }
+    }
+    cudaEventRecord(ctx->prof_ev[ctx->prof_used], ctx->stream);
+}
+void prof_end(clotho_ctx* ctx) {
+    if (!ctx->profiling) return;
+    cudaEventRecord(ctx->prof_ev[ctx->prof_used + 1], ctx->stream);
+    ctx->prof_used += 2;
+    ctx->prof_launches += 1;
+}
+int prof_collect(clotho_ctx* ctx) {
+    if (ctx->prof_used == 0) return 0;
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (size_t i = 0; i + 1 < ctx->prof_used; i += 2) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ctx->prof_ev[i], ctx->prof_ev[i + 1]));
+        ctx->prof_ms += ms;
+    }
+    ctx->prof_used = 0;
+    return 0;
+}
+
+void launch_gen(clotho_ctx* ctx, const PopDev* pops, uint32_t npops, uint32_t fuse) {
+    prof_begin(ctx);
+    launch_generation(cfg(ctx), pops, npops, ctx->d_ctl, ctx->maxW, fuse, ctx->profiling ? 1 : 0);
+    prof_end(ctx);
+    ctx->launches += 1;
+}
+
+template <class T>
+int h2d(clotho_ctx* ctx, T* dst, const T* src, size_t n, cudaStream_t s) {
+    if (n == 0) return 0;
+    if (!src) return fail(ctx, CLOTHO_E_ARG, "null host array");
+    CK(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, s));
+    return 0;
+}
+
+// Upload one generation's tape into tape set s of population p (copy stream).
+int upload_tape(clotho_ctx* ctx, PopHost* p, uint32_t s, const clotho_gen_tape* t) {
+    const PopDev& D = p->dev[s];
+    const uint32_t N = t->N, M = t->M, T = D.T;
+    if (N > D.Ncap) return fail(ctx, CLOTHO_E_CAPACITY, "tape N exceeds max_individuals");
+    if (M > D.Mcap) return fail(ctx, CLOTHO_E_CAPACITY, "tape M exceeds max_mutations");
+    if (!t->ev_off) return fail(ctx, CLOTHO_E_ARG, "tape ev_off is null");
+    const uint32_t ev_total = t->ev_off[2ull * N];
+    if (ev_total > D.EVcap) return fail(ctx, CLOTHO_E_CAPACITY, "tape events exceed max_events");
+    for (uint64_t g = 0; g < 2ull * N; ++g)
+        if (t->ev_off[g] > t->ev_off[g + 1]) return fail(ctx, CLOTHO_E_ARG, "tape ev_off not monotone");
+    cudaStream_t cs = ctx->copy_stream;
+    int rc;
+    if ((rc = h2d(ctx, D.pairs, t->pairs, 2ull * N, cs))) return rc;
+    if ((rc = h2d(ctx, D.swap, t->swap, 2ull * N, cs))) return rc;
+    if ((rc = h2d(ctx, D.ev_off, t->ev_off, 2ull * N + 1, cs))) return rc;
+    if ((rc = h2d(ctx, D.ev_pos, t->ev_pos, (size_t)ev_total, cs))) return rc;
+    if ((rc = h2d(ctx, D.mut_seq, t->mut_seq, (size_t)M, cs))) return rc;
+    if ((rc = h2d(ctx, D.mut_pos, t->mut_pos, (size_t)M, cs))) return rc;
+    if ((rc = h2d(ctx, D.mut_eff, t->mut_eff, (size_t)M * T, cs))) return rc;
+    return 0;
+}
+
+int require_ready(clotho_ctx* ctx) {
+    if (!ctx) return CLOTHO_E_ARG;
+    for (PopHost* p : ctx->pops)
+        if (!p->ready) return fail(ctx, CLOTHO_E_STATE, "population not initialised (clotho_init / clotho_seed_population)");
+    return 0;
+}
+
+// Make accF/accV of every population hold the AND/OR of its parent rows
+// (called right after k_begin when the previous step did not fuse them).
+void ensure_parent_acc(clotho_ctx* ctx, const PopDev* pops, uint32_t npops) {
+    bool need = false;
+    for (PopHost* p : ctx->pops) need |= !p->acc_valid;
+    if (need) {
+        launch_fs_reduce(cfg(ctx), pops, npops, ctx->maxW, 1u);
+        ctx->launches += 1;
+    }
+}
+
+// The fused step shared by tape and device-drawn modes, for every population.
+void enqueue_fused_step(clotho_ctx* ctx, uint32_t set, bool philox) {
+    const uint32_t n = (uint32_t)ctx->pops.size();
+    const PopDev* pops = ctx->d_pops[set];
+    LaunchCfg L = cfg(ctx);
+    launch_begin(L, pops, n, ctx->d_hdr[set], ctx->d_ctl);
+    ensure_parent_acc(ctx, pops, n);
+    if (philox) launch_mut_counts_philox(L, pops, n, ctx->maxS);
+    launch_fs_finalize(L, pops, n);
+    if (!philox) launch_mut_csr_tape(L, pops, n, ctx->maxS);
+    launch_mut_resolve(L, pops, n);
+    if (philox) launch_select_philox(L, pops, n);
+    launch_gen(ctx, pops, n, kFuseMut | kFusePheno | kFuseFs);
+    launch_individuals(L, pops, n);
+    launch_cdf(L, pops, n, ctx->maxN);
+    launch_end(L, pops, n);
+    ctx->launches += philox ? 14 : 15;
+    for (PopHost* p : ctx->pops) p->acc_valid = true;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+size_t clotho_footprint_for(const clotho_desc* d) {
+    if (!d) return 0;
+    size_t t = 0;
+    for (size_t s : sizes_of(geometry(*d))) t += align256(s);
+    return t;
+}
+
+int clotho_create(const clotho_desc* desc, clotho_ctx** out) {
+    if (!desc || !out) return CLOTHO_E_ARG;
+    *out = nullptr;
+    clotho_ctx* ctx = new clotho_ctx();
+    cudaError_t e = cudaGetDevice(&ctx->device);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return CLOTHO_E_CUDA;
+    }
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return CLOTHO_E_CUDA;
+    }
+    for (int i = 0; i < 2; ++i) {
+        cudaEventCreateWithFlags(&ctx->copy_done[i], cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&ctx->kern_done[i], cudaEventDisableTiming);
+        cudaEventRecord(ctx->kern_done[i], ctx->stream);
+    }
+    cudaEventCreate(&ctx->t0);
+    cudaEventCreate(&ctx->t1);
+    if (cudaMalloc(&ctx->d_ctl, sizeof(WorkCtl)) != cudaSuccess) {
+        clotho_destroy(ctx);
+        return CLOTHO_E_NOMEM;
+    }
+    cudaMemsetAsync(ctx->d_ctl, 0, sizeof(WorkCtl), ctx->stream);
+    PopHost* p = nullptr;
+    int rc = alloc_pop(ctx, *desc, &p);
+    if (rc) {
+        std::string m = ctx->err;
+        clotho_destroy(ctx);
+        fprintf(stderr, "clotho_create: %s\n", m.c_str());
+        return rc;
+    }
+    ctx->pops.push_back(p);
+    rc = sync_pop_arrays(ctx);
+    if (rc) {
+        clotho_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return 0;
+}
+
+int clotho_destroy(clotho_ctx* ctx) {
+    if (!ctx) return CLOTHO_E_ARG;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    for (PopHost* p : ctx->pops) free_pop(p);
+    ctx->pops.clear();
+    for (int s = 0; s < 3; ++s) {
+        if (ctx->d_pops[s]) cudaFree(ctx->d_pops[s]);
+        if (ctx->d_hdr[s]) cudaFree(ctx->d_hdr[s]);
+    }
+    if (ctx->h_hdr) cudaFreeHost(ctx->h_hdr);
+    if (ctx->d_ctl) cudaFree(ctx->d_ctl);
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
+    for (int i = 0; i < 2; ++i) {
+        if (ctx->copy_done[i]) cudaEventDestroy(ctx->copy_done[i]);
+        if (ctx->kern_done[i]) cudaEventDestroy(ctx->kern_done[i]);
+    }
+    if (ctx->t0) cudaEventDestroy(ctx->t0);
+    if (ctx->t1) cudaEventDestroy(ctx->t1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    delete ctx;
+    return 0;
+}
+
+const char* clotho_last_error(const clotho_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+size_t clotho_footprint(const clotho_ctx* ctx) {
+    size_t t = 0;
+    if (ctx)
+        for (PopHost* p : ctx->pops) t += p->bytes;
+    return t;
+}
+
+int clotho_sync(clotho_ctx* ctx) {
+    if (!ctx) return CLOTHO_E_ARG;
+    CK(cudaStreamSynchronize(ctx->copy_stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+uint64_t clotho_launch_count(const clotho_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int clotho_init(clotho_ctx* ctx, uint32_t N0) {
+    if (!ctx) return CLOTHO_E_ARG;
+    PopHost* p = ctx->pops[0];
+    const PopDev& D = p->dev[0];
+    if (N0 > D.Ncap) return fail(ctx, CLOTHO_E_CAPACITY, "N0 exceeds max_individuals");
+    CK(cudaStreamSynchronize(ctx->stream));
+    DevStatus s{};
+    s.gen = 1;
+    s.cur = 0;
+    s.N = N0;
+    s.fit_const = 1;
+    s.fit_total = (double)N0;
+    s.all_neutral = 1;
+    CK(cudaMemcpyAsync(D.st, &s, sizeof(s), cudaMemcpyHostToDevice, ctx->stream));
+    std::vector<double> ones(N0, 1.0);
+    if (N0) CK(cudaMemcpyAsync(D.fit, ones.data(), N0 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(D.pos, 0, (size_t)D.Acap * 8, ctx->stream));
+    CK(cudaMemsetAsync(D.eff, 0, (size_t)D.Acap * D.T * 4, ctx->stream));
+    CK(cudaMemsetAsync(D.age, 0, (size_t)D.Acap * 4, ctx->stream));
+    CK(cudaMemsetAsync(D.accF, 0xff, (size_t)D.Wcap * 8, ctx->stream));
+    CK(cudaMemsetAsync(D.accV, 0, (size_t)D.Wcap * 8, ctx->stream));
+    CK(cudaMemsetAsync(D.row_cnt, 0, ((size_t)D.Scap + 1) * 4, ctx->stream));
+    CK(cudaMemsetAsync(D.row_cur, 0, (size_t)D.Scap * 4, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    p->acc_valid = true;  // A == 0: the first analysis is skipped (free_space_mt...:46)
+    p->ready = true;
+    p->hostN = N0;
+    return 0;
+}
+
+int clotho_seed_population(clotho_ctx* ctx, uint32_t N, uint32_t A, const double* pos, const float* eff,
+                           const uint32_t* thr, uint64_t seed) {
+    if (!ctx || (A && (!pos || !eff || !thr))) return CLOTHO_E_ARG;
+    PopHost* p = ctx->pops[0];
+    const PopDev& D = p->dev[0];
+    if (A > D.Acap || ref_width(A) > D.Wcap) return fail(ctx, CLOTHO_E_CAPACITY, "A exceeds max_alleles");
+    int rc = clotho_init(ctx, N);
+    if (rc) return rc;
+    const uint32_t T = D.T;
+    int32_t nz = 0;
+    for (size_t i = 0; i < (size_t)A * T; ++i) nz += (eff[i] != 0.0f);
+    DevStatus s{};
+    s.gen = 1;
+    s.cur = 0;
+    s.N = N;
+    s.A = A;
+    s.W = ref_width(A);
+    s.nz_eff = nz;
+    s.fit_const = 1;
+    s.fit_total = (double)N;
+    CK(cudaMemcpyAsync(D.st, &s, sizeof(s), cudaMemcpyHostToDevice, ctx->stream));
+    uint32_t* d_thr = nullptr;
+    CK(cudaMalloc(&d_thr, std::max<size_t>(4, (size_t)A * 4)));
+    if (A) {
+        CK(cudaMemcpyAsync(D.pos, pos, (size_t)A * 8, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(D.eff, eff, (size_t)A * T * 4, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(d_thr, thr, (size_t)A * 4, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    LaunchCfg L = cfg(ctx);
+    launch_seed_rows(L, ctx->d_pops[0], 0, d_thr, seed, A);
+    launch_fs_reduce(L, ctx->d_pops[0], 1, ctx->maxW, 0u);
+    launch_phenotype(L, ctx->d_pops[0], 1);
+    launch_individuals(L, ctx->d_pops[0], 1);
+    launch_cdf(L, ctx->d_pops[0], 1, ctx->maxN);
+    ctx->launches += 10;
+    if ((rc = check_launch(ctx, "seed"))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(d_thr);
+    p->acc_valid = true;
+    return 0;
+}
+
+int clotho_generation_tape(clotho_ctx* ctx, const clotho_gen_tape* tape) {
+    int rc = require_ready(ctx);
+    if (rc) return rc;
+    if (!tape || ctx->pops.size() != 1) return fail(ctx, CLOTHO_E_ARG, "bad tape");
+    if (ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "a staged generation is in progress");
+    const uint32_t s = ctx->set;
+    // the tape set s was last read by the kernels of two steps ago
+    CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->kern_done[s], 0));
+    if ((rc = upload_tape(ctx, ctx->pops[0], s, tape))) return rc;
+    ctx->h_hdr[0] = tape->N;
+    ctx->h_hdr[1] = tape->M;
+    CK(cudaMemcpyAsync(ctx->d_hdr[s], ctx->h_hdr, 8, cudaMemcpyHostToDevice, ctx->copy_stream));
+    CK(cudaEventRecord(ctx->copy_done[s], ctx->copy_stream));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->copy_done[s], 0));
+    enqueue_fused_step(ctx, s, false);
+    if ((rc = check_launch(ctx, "generation_tape"))) return rc;
+    CK(cudaEventRecord(ctx->kern_done[s], ctx->stream));
+    // the caller's host arrays are free once the copies are done
+    CK(cudaEventSynchronize(ctx->copy_done[s]));
+    ctx->set ^= 1u;
+    ctx->pops[0]->hostN = tape->N;
+    return 0;
+}
+
+int clotho_generation_philox(clotho_ctx* ctx, uint32_t N) {
+    int rc = require_ready(ctx);
+    if (rc) return rc;
+    if (ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "a staged generation is in progress");
+    for (size_t i = 0; i < ctx->pops.size(); ++i) {
+        if (N > ctx->pops[i]->dev[2].Ncap) return fail(ctx, CLOTHO_E_CAPACITY, "N exceeds max_individuals");
+        ctx->h_hdr[2 * i] = N;
+        ctx->h_hdr[2 * i + 1] = 0;
+    }
+    CK(cudaMemcpyAsync(ctx->d_hdr[2], ctx->h_hdr, 8 * ctx->pops.size(), cudaMemcpyHostToDevice, ctx->stream));
+    enqueue_fused_step(ctx, 2, true);
+    if ((rc = check_launch(ctx, "generation_philox"))) return rc;
+    for (PopHost* p : ctx->pops) p->hostN = N;
+    return 0;
+}
+
+int clotho_run_philox(clotho_ctx* ctx, uint32_t N, uint32_t G) {
+    int rc = require_ready(ctx);
+    if (rc) return rc;
+    if (ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "a staged generation is in progress");
+    if (G == 0) return 0;
+    // the first generation runs eagerly (it may need the parent reduction)
+    if ((rc = clotho_generation_philox(ctx, N))) return rc;
+    if (G == 1) return 0;
+    if (ctx->profiling) {  // per-launch events are taken from eager launches
+        for (uint32_t g = 1; g < G; ++g)
+            if ((rc = clotho_generation_philox(ctx, N))) return rc;
+        return 0;
+    }
+    if (!ctx->graph || ctx->graph_N != N) {
+        if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+        cudaGraph_t gr;
+        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_fused_step(ctx, 2, true);
+        CK(cudaStreamEndCapture(ctx->stream, &gr));
+        CK(cudaGraphInstantiate(&ctx->graph, gr, 0));
+        cudaGraphDestroy(gr);
+        ctx->graph_N = N;
+    }
+    for (uint32_t g = 1; g < G; ++g) {
+        CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+        ctx->launches += 14;
+    }
+    return 0;
+}
+
+// ---- staged entry points -------------------------------------------------
+int clotho_begin_generation(clotho_ctx* ctx, uint32_t N, uint32_t M) {
+    int rc = require_ready(ctx);
+    if (rc) return rc;
+    if (ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "generation already begun");
+    PopHost* p = ctx->pops[0];
+    if (N > p->dev[0].Ncap) return fail(ctx, CLOTHO_E_CAPACITY, "N exceeds max_individuals");
+    if (M > p->dev[0].Mcap) return fail(ctx, CLOTHO_E_CAPACITY, "M exceeds max_mutations");
+    CK(cudaStreamSynchronize(ctx->copy_stream));
+    ctx->h_hdr[0] = N;
+    ctx->h_hdr[1] = M;
+    CK(cudaMemcpyAsync(ctx->d_hdr[0], ctx->h_hdr, 8, cudaMemcpyHostToDevice, ctx->stream));
+    launch_begin(cfg(ctx), ctx->d_pops[0], 1, ctx->d_hdr[0], ctx->d_ctl);
+    ctx->launches += 1;
+    ctx->in_step = true;
+    p->hostN = N;
+    return check_launch(ctx, "begin");
+}
+
+int clotho_free_space(clotho_ctx* ctx, uint32_t* counts) {
+    if (!ctx || !ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "clotho_begin_generation first");
+    PopHost* p = ctx->pops[0];
+    if (!p->acc_valid) {
+        launch_fs_reduce(cfg(ctx), ctx->d_pops[0], 1, ctx->maxW, 1u);
+        ctx->launches += 1;
+    }
+    launch_fs_finalize(cfg(ctx), ctx->d_pops[0], 1);
+    ctx->launches += 1;
+    p->acc_valid = false;  // reset for the child; the staged crossover does not refill it
+    int rc = check_launch(ctx, "free_space");
+    if (rc) return rc;
+    if (counts) {
+        DevStatus s = read_status(ctx, p, &rc);
+        if (rc) return rc;
+        counts[0] = s.fixed_cnt;
+        counts[1] = s.lost_cnt;
+        counts[2] = s.free_cnt;
+    }
+    return 0;
+}
+
+int clotho_set_pairs(clotho_ctx* ctx, const uint32_t* pairs) {
+    if (!ctx || !ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "clotho_begin_generation first");
+    PopHost* p = ctx->pops[0];
+    int rc = h2d(ctx, p->dev[0].pairs, pairs, 2ull * p->hostN, ctx->stream);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int clotho_select(clotho_ctx* ctx, uint32_t* pairs_out) {
+    if (!ctx || !ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "clotho_begin_generation first");
+    PopHost* p = ctx->pops[0];
+    // device draws write the pairs of the Philox set, which shares buffers with set 0
+    launch_select_philox(cfg(ctx), ctx->d_pops[2], 1);
+    ctx->launches += 1;
+    int rc = check_launch(ctx, "select");
+    if (rc) return rc;
+    if (pairs_out) {
+        CK(cudaMemcpyAsync(pairs_out, p->dev[2].pairs, 2ull * p->hostN * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return 0;
+}
+
+int clotho_crossover(clotho_ctx* ctx, const uint8_t* swap, const uint32_t* ev_off, const double* ev_pos) {
+    if (!ctx || !ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "clotho_begin_generation first");
+    PopHost* p = ctx->pops[0];
+    const PopDev& D = p->dev[0];
+    const uint32_t N = p->hostN;
+    if (!ev_off) return fail(ctx, CLOTHO_E_ARG, "ev_off is null");
+    const uint32_t ev_total = ev_off[2ull * N];
+    if (ev_total > D.EVcap) return fail(ctx, CLOTHO_E_CAPACITY, "events exceed max_events");
+    int rc;
+    if ((rc = h2d(ctx, D.swap, swap, 2ull * N, ctx->stream))) return rc;
+    if ((rc = h2d(ctx, D.ev_off, ev_off, 2ull * N + 1, ctx->stream))) return rc;
+    if ((rc = h2d(ctx, D.ev_pos, ev_pos, (size_t)ev_total, ctx->stream))) return rc;
+    // item prefix is already set by begin
+    launch_gen(ctx, ctx->d_pops[0], 1, 0u);
+    if ((rc = check_launch(ctx, "crossover"))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int clotho_mutate(clotho_ctx* ctx, const uint32_t* mut_seq, const double* mut_pos, const float* mut_eff) {
+    if (!ctx || !ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "clotho_begin_generation first");
+    PopHost* p = ctx->pops[0];
+    const PopDev& D = p->dev[0];
+    int rc;
+    DevStatus s = read_status(ctx, p, &rc);
+    if (rc) return rc;
+    const uint32_t M = s.M;
+    if ((rc = h2d(ctx, D.mut_seq, mut_seq, (size_t)M, ctx->stream))) return rc;
+    if ((rc = h2d(ctx, D.mut_pos, mut_pos, (size_t)M, ctx->stream))) return rc;
+    if ((rc = h2d(ctx, D.mut_eff, mut_eff, (size_t)M * D.T, ctx->stream))) return rc;
+    launch_mut_resolve(cfg(ctx), ctx->d_pops[0], 1);
+    launch_mut_scatter(cfg(ctx), ctx->d_pops[0], 1);
+    ctx->launches += 2;
+    if ((rc = check_launch(ctx, "mutate"))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int clotho_phenotype(clotho_ctx* ctx) {
+    if (!ctx) return CLOTHO_E_ARG;
+    launch_phenotype(cfg(ctx), ctx->d_pops[0], 1);
+    ctx->launches += 1;
+    return check_launch(ctx, "phenotype");
+}
+
+int clotho_fitness(clotho_ctx* ctx) {
+    if (!ctx) return CLOTHO_E_ARG;
+    launch_individuals(cfg(ctx), ctx->d_pops[0], 1);
+    launch_cdf(cfg(ctx), ctx->d_pops[0], 1, ctx->maxN);
+    ctx->launches += 4;
+    return check_launch(ctx, "fitness");
+}
+
+int clotho_end_generation(clotho_ctx* ctx) {
+    if (!ctx || !ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "no generation in progress");
+    launch_end(cfg(ctx), ctx->d_pops[0], 1);
+    ctx->launches += 1;
+    ctx->in_step = false;
+    int rc = check_launch(ctx, "end");
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+// ---- read-back -------------------------------------------------------------
+int clotho_get_info(clotho_ctx* ctx, clotho_info* out) {
+    if (!ctx || !out) return CLOTHO_E_ARG;
+    CK(cudaStreamSynchronize(ctx->copy_stream));
+    int rc;
+    DevStatus s = read_status(ctx, ctx->pops[0], &rc);
+    if (rc) return rc;
+    out->generation = s.gen;
+    out->N = s.N;
+    out->A = s.A;
+    out->W = s.W;
+    out->fixed_count = s.fixed_cnt;
+    out->lost_count = s.lost_cnt;
+    out->free_count = s.free_cnt;
+    out->variable_count = (s.pA > s.free_cnt ? s.pA - s.free_cnt : 0);
+    out->fixed_total = s.fixed_total;
+    out->last_M = s.last_M;
+    out->all_neutral = s.all_neutral;
+    out->device_error = s.err;
+    out->mean_fitness = s.N ? s.fit_total / (double)s.N : 0.0;
+    return 0;
+}
+
+int clotho_get_rows(clotho_ctx* ctx, uint64_t* dst, size_t dst_words) {
+    if (!ctx) return CLOTHO_E_ARG;
+    int rc;
+    PopHost* p = ctx->pops[0];
+    DevStatus s = read_status(ctx, p, &rc);
+    if (rc) return rc;
+    const size_t S = 2ull * s.N, W = s.W;
+    if (S * W == 0) return 0;
+    if (!dst || dst_words < S * W) return fail(ctx, CLOTHO_E_ARG, "destination too small");
+    CK(cudaMemcpy2DAsync(dst, W * 8, p->dev[0].rows[s.cur], (size_t)p->dev[0].Wcap * 8, W * 8, S,
+                         cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int clotho_get_alleles(clotho_ctx* ctx, double* pos, uint32_t* age, float* eff) {
+    if (!ctx) return CLOTHO_E_ARG;
+    int rc;
+    PopHost* p = ctx->pops[0];
+    DevStatus s = read_status(ctx, p, &rc);
+    if (rc) return rc;
+    const PopDev& D = p->dev[0];
+    if (pos && s.A) CK(cudaMemcpyAsync(pos, D.pos, (size_t)s.A * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (age && s.A) CK(cudaMemcpyAsync(age, D.age, (size_t)s.A * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (eff && s.A) CK(cudaMemcpyAsync(eff, D.eff, (size_t)s.A * D.T * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int clotho_get_fixed(clotho_ctx* ctx, double* pos, uint32_t* age, float* eff) {
+    if (!ctx) return CLOTHO_E_ARG;
+    int rc;
+    PopHost* p = ctx->pops[0];
+    DevStatus s = read_status(ctx, p, &rc);
+    if (rc) return rc;
+    const PopDev& D = p->dev[0];
+    const size_t F = s.fixed_total;
+    if (pos && F) CK(cudaMemcpyAsync(pos, D.fx_pos, F * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (age && F) CK(cudaMemcpyAsync(age, D.fx_age, F * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (eff && F) CK(cudaMemcpyAsync(eff, D.fx_eff, F * D.T * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int clotho_get_free(clotho_ctx* ctx, uint32_t* dst) {
+    if (!ctx) return CLOTHO_E_ARG;
+    int rc;
+    PopHost* p = ctx->pops[0];
+    DevStatus s = read_status(ctx, p, &rc);
+    if (rc) return rc;
+    if (s.free_cnt && !dst) return fail(ctx, CLOTHO_E_ARG, "null destination");
+    if (s.free_cnt)
+        CK(cudaMemcpyAsync(dst, p->dev[0].free_list, (size_t)s.free_cnt * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+static int get_float4(clotho_ctx* ctx, const float* src, size_t n, float* dst) {
+    const uint32_t T = ctx->pops[0]->dev[0].T;
+    std::vector<float> tmp(n * 4);
+    if (n) CK(cudaMemcpyAsync(tmp.data(), src, n * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (size_t i = 0; i < n; ++i)
+        for (uint32_t t = 0; t < T; ++t) dst[i * T + t] = tmp[i * 4 + t];
+    return 0;
+}
+
+int clotho_get_genome_traits(clotho_ctx* ctx, float* dst) {
+    if (!ctx) return CLOTHO_E_ARG;
+    int rc;
+    DevStatus s = read_status(ctx, ctx->pops[0], &rc);
+    if (rc) return rc;
+    return get_float4(ctx, ctx->pops[0]->dev[0].zg, 2ull * s.N, dst);
+}
+
+int clotho_get_phenotypes(clotho_ctx* ctx, float* dst) {
+    if (!ctx) return CLOTHO_E_ARG;
+    int rc;
+    DevStatus s = read_status(ctx, ctx->pops[0], &rc);
+    if (rc) return rc;
+    return get_float4(ctx, ctx->pops[0]->dev[0].zi, s.N, dst);
+}
+
+int clotho_get_fitness(clotho_ctx* ctx, double* dst) {
+    if (!ctx) return CLOTHO_E_ARG;
+    int rc;
+    DevStatus s = read_status(ctx, ctx->pops[0], &rc);
+    if (rc) return rc;
+    if (s.N) CK(cudaMemcpyAsync(dst, ctx->pops[0]->dev[0].fit, (size_t)s.N * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int clotho_get_pairs(clotho_ctx* ctx, uint32_t* dst) {
+    if (!ctx) return CLOTHO_E_ARG;
+    int rc;
+    DevStatus s = read_status(ctx, ctx->pops[0], &rc);
+    if (rc) return rc;
+    // the last tape step used set (set ^ 1); device draws use set 0's buffer
+    const PopDev& D = ctx->pops[0]->dev[ctx->set ^ 1u];
+    if (s.N) CK(cudaMemcpyAsync(dst, D.pairs, 2ull * s.N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int clotho_stats_compute(clotho_ctx* ctx, clotho_stats* out, uint32_t* sfs, uint32_t sfs_len) {
+    if (!ctx || !out) return CLOTHO_E_ARG;
+    int rc;
+    PopHost* p = ctx->pops[0];
+    DevStatus s = read_status(ctx, p, &rc);
+    if (rc) return rc;
+    const PopDev& D = p->dev[0];
+    const uint32_t A = s.A, S = 2 * s.N;
+    std::vector<uint32_t> counts(std::max<size_t>(1, (size_t)s.W * 64), 0);
+    uint32_t* d_counts = nullptr;
+    CK(cudaMalloc(&d_counts, counts.size() * 4));
+    CK(cudaMemsetAsync(d_counts, 0, counts.size() * 4, ctx->stream));
+    if (S && s.W) launch_stats(cfg(ctx), ctx->d_pops[0], 0, d_counts, s.W);
+    CK(cudaMemcpyAsync(counts.data(), d_counts, counts.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<float> zi((size_t)s.N * 4);
+    if (s.N) CK(cudaMemcpyAsync(zi.data(), D.zi, (size_t)s.N * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(d_counts);
+    ctx->launches += 1;
+    *out = clotho_stats{};
+    if (sfs)
+        for (uint32_t k = 0; k < sfs_len; ++k) sfs[k] = 0;
+    double het = 0.0;
+    for (uint32_t a = 0; a < A; ++a) {
+        const uint32_t c = counts[a];
+        if (c > 0 && c < S) out->segregating += 1;
+        if (S && c == S) out->fixed_now += 1;
+        if (S) {
+            const double f = (double)c / (double)S;
+            het += 2.0 * f * (1.0 - f);
+        }
+        if (sfs && sfs_len) sfs[c < sfs_len ? c : sfs_len - 1] += 1;
+    }
+    out->heterozygosity = het;
+    out->mean_fitness = s.N ? s.fit_total / (double)s.N : 0.0;
+    for (uint32_t t = 0; t < 4; ++t) {
+        double m = 0.0;
+        for (uint32_t i = 0; i < s.N; ++i) m += zi[(size_t)i * 4 + t];
+        out->mean_phenotype[t] = s.N ? m / s.N : 0.0;
+    }
+    return 0;
+}
+
+// ---- timing --------------------------------------------------------------
+int clotho_profile(clotho_ctx* ctx, int enable) {
+    if (!ctx) return CLOTHO_E_ARG;
+    int rc = prof_collect(ctx);
+    if (rc) return rc;
+    ctx->profiling = enable != 0;
+    ctx->prof_ms = 0.0;
+    ctx->prof_launches = 0;
+    if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+    CK(cudaMemsetAsync(&ctx->d_ctl->rows_done, 0, 16, ctx->stream));
+    return 0;
+}
+
+int clotho_kernel_time(clotho_ctx* ctx, double* total_ms, uint32_t* launches, uint64_t* rows, uint64_t* words) {
+    if (!ctx) return CLOTHO_E_ARG;
+    int rc = prof_collect(ctx);
+    if (rc) return rc;
+    uint64_t rw[2] = {0, 0};
+    CK(cudaMemcpyAsync(rw, &ctx->d_ctl->rows_done, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (total_ms) *total_ms = ctx->prof_ms;
+    if (launches) *launches = ctx->prof_launches;
+    if (rows) *rows = rw[0];
+    if (words) *words = rw[1];
+    return 0;
+}
+
+int clotho_timer_begin(clotho_ctx* ctx) {
+    if (!ctx) return CLOTHO_E_ARG;
+    CK(cudaEventRecord(ctx->t0, ctx->stream));
+    return 0;
+}
+
+int clotho_timer_end(clotho_ctx* ctx, double* ms) {
+    if (!ctx) return CLOTHO_E_ARG;
+    CK(cudaEventRecord(ctx->t1, ctx->stream));
+    CK(cudaEventSynchronize(ctx->t1));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, ctx->t0, ctx->t1));
+    if (ms) *ms = f;
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,193 @@
+// engine.cuh -- device data layout and shared device helpers of the GB300
+// engine for Clotho's per-generation hot path.
+//
+// One PopDev describes one resident population.  Every kernel takes an array
+// of PopDev and walks all of them, so the plain engine is a batch of one and
+// the batched/served forms reuse the same launches.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace clotho {
+
+constexpr uint32_t kMaxTraits = 4;
+constexpr uint32_t kGenThreads = 256;      // 8 warps per CTA in the generation kernel
+constexpr uint32_t kRowsPerItem = 64;      // child rows per scheduling item
+constexpr uint32_t kMaxEvReg = 16;         // events held in registers
+constexpr uint32_t kMaxEvDevice = 128;     // device-drawn events per gamete
+constexpr uint32_t kMaxMutReg = 32;        // mutations per row held in registers
+constexpr uint32_t kWordAlign = 64;        // row stride granularity (words)
+
+// sticky device error bits (CLOTHO_DEVERR_* in clotho_gpu.h)
+constexpr uint32_t kErrAlleles = 1u, kErrFixed = 2u, kErrEvents = 4u, kErrParent = 8u,
+                   kErrSeq = 16u, kErrMut = 32u, kErrFitness = 64u;
+
+enum Mode : uint32_t { kModeTape = 0, kModePhilox = 1 };
+
+// Philox counter streams
+enum Stream : uint32_t {
+    kStreamGamete = 1, kStreamSelect = 2, kStreamMutCount = 3, kStreamMutAllele = 4
+};
+
+struct DevStatus {
+    uint32_t gen;          // generation number of the step in progress / next step
+    uint32_t cur;          // rows buffer holding the current child
+    uint32_t N, A, W;      // current child: individuals, alleles, reference width
+    uint32_t pN, pA, pW;   // parent of the step in progress
+    uint32_t M;            // mutations of the step in progress
+    uint32_t fixed_cnt, lost_cnt, free_cnt;
+    uint32_t fixed_total;
+    int32_t  nz_eff;       // nonzero effect entries in eff[0, A*T)
+    uint32_t fs_valid;     // accF/accV hold AND/OR over the current child rows
+    uint32_t err;
+    uint32_t fit_const;    // every fitness value equal (selection is uniform)
+    uint32_t all_neutral;  // phenotype took the constant path
+    uint32_t last_M;
+    uint32_t pad0;
+    double   fit_total;    // sum of fitness of the current population
+};
+
+struct PopDev {
+    uint64_t* rows[2];     // [Scap * Wcap] each
+    uint64_t* fixmask;     // [Wcap] fixed columns of the parent
+    uint64_t* accF;        // [Wcap] AND over current child rows
+    uint64_t* accV;        // [Wcap] OR over current child rows
+    uint32_t* free_list;   // [Acap]
+    double*   pos;         // [Acap] allele positions (non-negative: ordered as u64)
+    uint32_t* age;         // [Acap]
+    float*    eff;         // [Acap * T]
+    double*   fx_pos;      // [FXcap]
+    uint32_t* fx_age;      // [FXcap]
+    float*    fx_eff;      // [FXcap * T]
+    float*    zg;          // [Scap * 4] per-genome trait sums
+    float*    zi;          // [Ncap * 4] per-individual phenotypes
+    double*   fit;         // [Ncap]
+    double*   cdf;         // [Ncap]
+    double*   scan_part;   // [Ncap / 1024 + 2]
+    uint32_t* scan_upart;  // [Scap / 1024 + 2]
+    uint32_t* pairs;       // [2 * Ncap]
+    uint8_t*  swap;        // [Scap]
+    uint32_t* ev_off;      // [Scap + 1]
+    double*   ev_pos;      // [EVcap]
+    uint32_t* mut_seq;     // [Mcap]
+    double*   mut_pos;     // [Mcap]
+    float*    mut_eff;     // [Mcap * T]
+    uint32_t* mut_slot;    // [Mcap]
+    uint32_t* row_cnt;     // [Scap + 1] per-row mutation counts (zero between steps)
+    uint32_t* row_off;     // [Scap + 1] exclusive prefix of row_cnt
+    uint32_t* row_cur;     // [Scap] scatter cursors (zero between steps)
+    uint32_t* row_mut;     // [Mcap] mutation indices grouped by row
+    DevStatus* st;
+    uint32_t Scap, Ncap, Wcap, Acap, Mcap, EVcap, FXcap, T;
+    double mu, rho, bias, p_neutral, eff_mean, eff_sigma, fit_param;
+    double exp_neg_rho, exp_neg_mu;   // Poisson inversion seeds, computed on the host
+    uint64_t seed;
+    int32_t fitness;
+    uint32_t flags;
+    uint32_t mode;
+    uint32_t pad1;
+};
+
+// Work control shared by the persistent kernels of one step.
+struct WorkCtl {
+    uint32_t gen_counter;           // dynamic item counter of k_generation
+    uint32_t gen_items;             // total items
+    uint32_t item_base[257];        // item prefix per population (<= 256 pops)
+    uint64_t rows_done;             // profiling: rows processed
+    uint64_t words_done;            // profiling: words written
+};
+
+constexpr uint32_t kMaxPops = 256;
+
+// ---------------------------------------------------------------------------
+// small helpers
+
+__host__ __device__ inline uint32_t ref_width(uint32_t A) {
+    // population_space_row::setMaxAlleles (population_space_row_block.hpp:94-101)
+    return ((A + 511u) / 512u) * 8u;
+}
+
+__device__ inline uint64_t dkey(double d) { return (uint64_t)__double_as_longlong(d); }
+
+// seed rule shared with the oracle (orc_seed_hash)
+__host__ __device__ inline uint32_t seed_hash(uint64_t seed, uint32_t row, uint32_t slot) {
+    uint64_t x = seed + 0x9E3779B97F4A7C15ull * ((((uint64_t)row) << 32) + (uint64_t)slot + 1ull);
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    x ^= x >> 31;
+    return (uint32_t)(x >> 32);
+}
+
+// Philox-4x32-10 counter-based generator, written from the published
+// description (Salmon, Moraes, Dror, Shaw: "Parallel random numbers: as easy
+// as 1, 2, 3", SC'11): multipliers 0xD2511F53/0xCD9E8D57, Weyl key increments
+// 0x9E3779B9/0xBB67AE85, ten rounds.
+struct U4 { uint32_t x, y, z, w; };
+
+__device__ inline U4 philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint64_t key) {
+    uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    return U4{c0, c1, c2, c3};
+}
+
+// [0,1) double from 53 random bits
+__device__ inline double u01(uint32_t hi, uint32_t lo) {
+    uint64_t v = ((((uint64_t)hi) << 32) | lo) >> 11;
+    return (double)v * 0x1.0p-53;
+}
+
+// Poisson draw by sequential inversion of the CDF; e = exp(-lambda) from the
+// host.  Used only for small means (per-gamete events, per-row mutations).
+__device__ inline uint32_t poisson_inv(double u, double lambda, double e) {
+    double p = e, F = e;
+    uint32_t k = 0;
+    while (u > F && k < 4096u) {
+        ++k;
+        p *= lambda / (double)k;
+        F += p;
+    }
+    return k;
+}
+
+__device__ inline uint32_t lane_id() { return threadIdx.x & 31u; }
+
+}  // namespace clotho
+
+// ---------------------------------------------------------------------------
+// Host-side launch wrappers (defined in the kernel translation units).
+namespace clotho {
+struct LaunchCfg {
+    cudaStream_t stream;
+    int num_sms;
+};
+// which: 0 = current child rows, 1 = parent rows of the step in progress
+void launch_fs_reduce(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxW, uint32_t which);
+void launch_fs_finalize(const LaunchCfg&, const PopDev* pops, uint32_t npops);
+void launch_begin(const LaunchCfg&, const PopDev* pops, uint32_t npops, const uint32_t* hdr,
+                  WorkCtl* ctl);
+void launch_mut_csr_tape(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
+void launch_mut_counts_philox(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
+void launch_mut_resolve(const LaunchCfg&, const PopDev* pops, uint32_t npops);
+void launch_select_philox(const LaunchCfg&, const PopDev* pops, uint32_t npops);
+void launch_generation(const LaunchCfg&, const PopDev* pops, uint32_t npops, WorkCtl* ctl,
+                       uint32_t maxW, uint32_t fuse, int profile);
+void launch_mut_scatter(const LaunchCfg&, const PopDev* pops, uint32_t npops);
+void launch_phenotype(const LaunchCfg&, const PopDev* pops, uint32_t npops);
+void launch_individuals(const LaunchCfg&, const PopDev* pops, uint32_t npops);
+void launch_cdf(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxN);
+void launch_end(const LaunchCfg&, const PopDev* pops, uint32_t npops);
+void launch_seed_rows(const LaunchCfg&, const PopDev* pops, uint32_t npops, const uint32_t* thr,
+                      uint64_t seed, uint32_t A);
+void launch_stats(const LaunchCfg&, const PopDev* pops, uint32_t p, uint32_t* counts, uint32_t A);
+
+// fuse flags of k_generation
+constexpr uint32_t kFuseMut = 1u, kFusePheno = 2u, kFuseFs = 4u;
+}  // namespace clotho

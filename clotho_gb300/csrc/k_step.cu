@@ -1,0 +1,525 @@
+// k_step.cu -- the small per-generation kernels around the generation pass:
+// step begin/end, mutation bookkeeping (slot resolution, per-row CSR), device
+// draws (Philox), fitness-proportional parent sampling (FP64 prefix sum),
+// per-individual phenotype + fitness, seeding and column statistics.
+//
+// All kernels walk every population of the batch; sizes are read from the
+// device status words so a step needs no host synchronisation and can be
+// captured in a CUDA graph.
+#include "engine.cuh"
+
+namespace clotho {
+
+namespace {
+constexpr uint32_t kScanChunk = 4096;  // elements per scan chunk (1024 threads x 4)
+
+__device__ inline uint32_t warp_incl_u32(uint32_t x) {
+    const uint32_t lane = threadIdx.x & 31u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    return x;
+}
+__device__ inline double warp_incl_f64(double x) {
+    const uint32_t lane = threadIdx.x & 31u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        double y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    return x;
+}
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Step begin: the child becomes the parent (engine_batched_task.hpp:164), the
+// offspring count comes from the tape header / growth rule, and the item
+// prefix of the generation kernel is rebuilt.
+__global__ void k_begin(const PopDev* __restrict__ pops, uint32_t npops, const uint32_t* __restrict__ hdr,
+                        WorkCtl* ctl) {
+    const uint32_t p = threadIdx.x;
+    __shared__ uint32_t s_items[kMaxPops];
+    if (p < npops) {
+        const PopDev& P = pops[p];
+        DevStatus* st = P.st;
+        uint32_t N = hdr[2 * p], M = hdr[2 * p + 1];
+        if (N > P.Ncap) { st->err |= kErrAlleles; N = P.Ncap; }
+        if (M > P.Mcap) { st->err |= kErrMut; M = P.Mcap; }
+        st->pN = st->N;
+        st->pA = st->A;
+        st->pW = st->W;
+        st->N = N;
+        st->M = M;
+        st->cur ^= 1u;
+        s_items[p] = (2u * N + kRowsPerItem - 1u) / kRowsPerItem;
+    }
+    __syncthreads();
+    if (p == 0) {
+        uint32_t acc = 0;
+        for (uint32_t q = 0; q < npops; ++q) {
+            ctl->item_base[q] = acc;
+            acc += s_items[q];
+        }
+        ctl->item_base[npops] = acc;
+        ctl->gen_items = acc;
+        ctl->gen_counter = 0;
+    }
+}
+
+void launch_begin(const LaunchCfg& L, const PopDev* pops, uint32_t npops, const uint32_t* hdr, WorkCtl* ctl) {
+    k_begin<<<1, kMaxPops, 0, L.stream>>>(pops, npops, hdr, ctl);
+}
+
+__global__ void k_end(const PopDev* __restrict__ pops, uint32_t npops) {
+    const uint32_t p = threadIdx.x;
+    if (p < npops) {
+        DevStatus* st = pops[p].st;
+        st->last_M = st->M;
+        st->gen += 1u;  // ++m_generation (engine_batched_task.hpp:222)
+    }
+}
+void launch_end(const LaunchCfg& L, const PopDev* pops, uint32_t npops) {
+    k_end<<<1, kMaxPops, 0, L.stream>>>(pops, npops);
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive u32 scan of row_cnt[0..S] into row_off[0..S], chunked, per
+// population.  Also zeroes row_cnt and row_cur for the next step.  When
+// set_M is set, row_off[S] (the total) becomes the step's mutation count.
+__global__ void __launch_bounds__(1024) k_uscan_a(const PopDev* __restrict__ pops, uint32_t npops) {
+    __shared__ uint32_t s_w[32];
+    for (uint32_t p = 0; p < npops; ++p) {
+        const PopDev& P = pops[p];
+        const uint32_t L = 2u * P.st->N + 1u;
+        const uint32_t nch = (L + kScanChunk - 1) / kScanChunk;
+        for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x) {
+            const uint32_t b = c * kScanChunk + threadIdx.x * 4u;
+            uint32_t s = 0;
+            for (uint32_t k = 0; k < 4; ++k) s += (b + k < L) ? P.row_cnt[b + k] : 0u;
+            s = warp_incl_u32(s);
+            if ((threadIdx.x & 31u) == 31u) s_w[threadIdx.x >> 5] = s;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                uint32_t t = 0;
+                for (int i = 0; i < 32; ++i) t += s_w[i];
+                P.scan_upart[c] = t;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void k_uscan_b(const PopDev* __restrict__ pops, uint32_t npops) {
+    const uint32_t p = blockIdx.x;
+    if (p >= npops || threadIdx.x != 0) return;
+    const PopDev& P = pops[p];
+    const uint32_t L = 2u * P.st->N + 1u;
+    const uint32_t nch = (L + kScanChunk - 1) / kScanChunk;
+    uint32_t acc = 0;
+    for (uint32_t c = 0; c < nch; ++c) {
+        uint32_t t = P.scan_upart[c];
+        P.scan_upart[c] = acc;
+        acc += t;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_uscan_c(const PopDev* __restrict__ pops, uint32_t npops, int set_M) {
+    __shared__ uint32_t s_w[32];
+    for (uint32_t p = 0; p < npops; ++p) {
+        const PopDev& P = pops[p];
+        const uint32_t S = 2u * P.st->N, L = S + 1u;
+        const uint32_t nch = (L + kScanChunk - 1) / kScanChunk;
+        for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x) {
+            const uint32_t b = c * kScanChunk + threadIdx.x * 4u;
+            uint32_t v[4], s = 0;
+            for (uint32_t k = 0; k < 4; ++k) {
+                v[k] = (b + k < L) ? P.row_cnt[b + k] : 0u;
+                s += v[k];
+            }
+            const uint32_t incl = warp_incl_u32(s);
+            if ((threadIdx.x & 31u) == 31u) s_w[threadIdx.x >> 5] = incl;
+            __syncthreads();
+            uint32_t woff = 0;
+            for (uint32_t i = 0; i < (threadIdx.x >> 5); ++i) woff += s_w[i];
+            uint32_t run = P.scan_upart[c] + woff + incl - s;
+            for (uint32_t k = 0; k < 4; ++k) {
+                if (b + k < L) {
+                    P.row_off[b + k] = run;
+                    P.row_cnt[b + k] = 0u;
+                    if (b + k < S) P.row_cur[b + k] = 0u;
+                    if (set_M && b + k == S) {
+                        DevStatus* st = P.st;
+                        if (run > P.Mcap) { st->err |= kErrMut; run = P.Mcap; }
+                        st->M = run;
+                    }
+                }
+                run += v[k];
+            }
+            __syncthreads();
+        }
+    }
+}
+
+static void launch_uscan(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS, int set_M) {
+    const uint32_t nch = (maxS + 1 + kScanChunk - 1) / kScanChunk;
+    const uint32_t g = max(1u, min(nch, (uint32_t)L.num_sms * 2u));
+    k_uscan_a<<<g, 1024, 0, L.stream>>>(pops, npops);
+    k_uscan_b<<<npops, 32, 0, L.stream>>>(pops, npops);
+    k_uscan_c<<<g, 1024, 0, L.stream>>>(pops, npops, set_M);
+}
+
+// ---------------------------------------------------------------------------
+// Tape mutations grouped by target row (device counting sort; the in-row order
+// does not affect any result).
+__global__ void k_csr_count(const PopDev* __restrict__ pops, uint32_t npops) {
+    for (uint32_t p = 0; p < npops; ++p) {
+        const PopDev& P = pops[p];
+        DevStatus* st = P.st;
+        const uint32_t M = st->M, S = 2u * st->N;
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+            const uint32_t s = P.mut_seq[i];
+            if (s >= S) { atomicOr(&st->err, kErrSeq); continue; }
+            atomicAdd(&P.row_cnt[s], 1u);
+        }
+    }
+}
+__global__ void k_csr_scatter(const PopDev* __restrict__ pops, uint32_t npops) {
+    for (uint32_t p = 0; p < npops; ++p) {
+        const PopDev& P = pops[p];
+        const uint32_t M = P.st->M, S = 2u * P.st->N;
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+            const uint32_t s = P.mut_seq[i];
+            if (s >= S) continue;
+            const uint32_t k = atomicAdd(&P.row_cur[s], 1u);
+            P.row_mut[P.row_off[s] + k] = i;
+        }
+    }
+}
+void launch_mut_csr_tape(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
+    const int g = L.num_sms * 2;
+    k_csr_count<<<g, 256, 0, L.stream>>>(pops, npops);
+    launch_uscan(L, pops, npops, maxS, 0);
+    k_csr_scatter<<<g, 256, 0, L.stream>>>(pops, npops);
+}
+
+// Device-drawn mutation counts: Poisson(mu) per offspring row.  The sum over
+// rows is Poisson(2N mu) and, given the total, the rows are uniform -- the
+// same law as M ~ Poisson(mu * 2N) with uniform target rows
+// (mutation_allocator.hpp:41-47, batch_mutation_task_population_space_row.hpp:77).
+__global__ void k_philox_rowcnt(const PopDev* __restrict__ pops, uint32_t npops) {
+    for (uint32_t p = 0; p < npops; ++p) {
+        const PopDev& P = pops[p];
+        if (P.mode != kModePhilox) continue;
+        const DevStatus* st = P.st;
+        const uint32_t S = 2u * st->N, gen = st->gen;
+        for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < S; r += gridDim.x * blockDim.x) {
+            const U4 x = philox4x32(r, 0u, gen, kStreamMutCount, P.seed);
+            P.row_cnt[r] = poisson_inv(u01(x.x, x.y), P.mu, P.exp_neg_mu);
+        }
+    }
+}
+void launch_mut_counts_philox(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
+    k_philox_rowcnt<<<L.num_sms * 4, 256, 0, L.stream>>>(pops, npops);
+    launch_uscan(L, pops, npops, maxS, 1);
+}
+
+// ---------------------------------------------------------------------------
+// Mutation i takes free_indices[i]; beyond the free list new slots are
+// appended at the parent allele count (batch_mutation_mt.hpp:69-80).  Writes
+// the allele table (AlleleGenerator, allele_generator_vector.hpp:76-83) and
+// the trait table (TraitSpaceGenerator2, trait_space_generator.hpp:118-129).
+__global__ void k_mut_resolve(const PopDev* __restrict__ pops, uint32_t npops) {
+    for (uint32_t p = 0; p < npops; ++p) {
+        const PopDev& P = pops[p];
+        DevStatus* st = P.st;
+        const uint32_t M = st->M, fr = st->free_cnt, pA = st->pA, gen = st->gen, T = P.T;
+        const uint32_t Alim = st->A;
+        int nz_delta = 0;
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+            const uint32_t slot = (i < fr) ? P.free_list[i] : pA + (i - fr);
+            if (slot >= Alim) { atomicOr(&st->err, kErrAlleles); P.mut_slot[i] = 0xffffffffu; continue; }
+            P.mut_slot[i] = slot;
+            double pos;
+            float e[kMaxTraits];
+            if (P.mode == kModePhilox) {
+                const U4 x = philox4x32(i, 0u, gen, kStreamMutAllele, P.seed);
+                pos = u01(x.x, x.y);
+                for (uint32_t t = 0; t < T; ++t) {
+                    const U4 a = philox4x32(i, 1u + t, gen, kStreamMutAllele, P.seed);
+                    float w = 0.0f;
+                    if (!(u01(a.x, a.y) < P.p_neutral)) {
+                        // Box-Muller on two fresh uniforms, first in (0,1]
+                        const double u1 = 1.0 - u01(a.z, a.w);
+                        const U4 b = philox4x32(i, 1u + kMaxTraits + t, gen, kStreamMutAllele, P.seed);
+                        const double u2 = u01(b.x, b.y);
+                        const double n = sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+                        w = (float)(P.eff_mean + P.eff_sigma * n);
+                    }
+                    e[t] = w;
+                }
+            } else {
+                pos = P.mut_pos[i];
+                for (uint32_t t = 0; t < T; ++t) e[t] = P.mut_eff[(size_t)i * T + t];
+            }
+            P.pos[slot] = pos;
+            P.age[slot] = gen;
+            for (uint32_t t = 0; t < T; ++t) {
+                const float old = P.eff[(size_t)slot * T + t];
+                nz_delta += (e[t] != 0.0f) - (old != 0.0f);
+                P.eff[(size_t)slot * T + t] = e[t];
+            }
+        }
+        if (nz_delta) atomicAdd(&st->nz_eff, nz_delta);
+    }
+}
+void launch_mut_resolve(const LaunchCfg& L, const PopDev* pops, uint32_t npops) {
+    k_mut_resolve<<<L.num_sms * 2, 256, 0, L.stream>>>(pops, npops);
+}
+
+// Standalone mutation scatter (staged API): child->mutate(seq, slot) is a
+// single-bit XOR (population_space_row_block.hpp:111-125).
+__global__ void k_mut_scatter(const PopDev* __restrict__ pops, uint32_t npops) {
+    for (uint32_t p = 0; p < npops; ++p) {
+        const PopDev& P = pops[p];
+        const DevStatus* st = P.st;
+        const uint32_t M = st->M, S = 2u * st->N;
+        uint64_t* rows = P.rows[st->cur];
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+            const uint32_t slot = P.mut_slot[i], s = P.mut_seq[i];
+            if (slot == 0xffffffffu || s >= S) continue;
+            atomicXor((unsigned long long*)&rows[(size_t)s * P.Wcap + (slot >> 6)], 1ull << (slot & 63u));
+        }
+    }
+}
+void launch_mut_scatter(const LaunchCfg& L, const PopDev* pops, uint32_t npops) {
+    k_mut_scatter<<<L.num_sms * 2, 256, 0, L.stream>>>(pops, npops);
+}
+
+// ---------------------------------------------------------------------------
+// Parent sampling on the device (SelectionGenerator::update,
+// general_fitness_selection_generator.hpp:45-69): uniform when every fitness
+// is equal, else the FP64 inclusive prefix sum and an upper_bound per draw.
+__global__ void k_select_philox(const PopDev* __restrict__ pops, uint32_t npops) {
+    for (uint32_t p = 0; p < npops; ++p) {
+        const PopDev& P = pops[p];
+        const DevStatus* st = P.st;
+        const uint32_t N = st->N, Np = st->pN, gen = st->gen;
+        const bool uni = st->fit_const != 0u || !(st->fit_total > 0.0);
+        const double total = st->fit_total;
+        for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
+            const U4 x = philox4x32(k, 0u, gen, kStreamSelect, P.seed);
+            const double u[2] = {u01(x.x, x.y), u01(x.z, x.w)};
+            for (int h = 0; h < 2; ++h) {
+                uint32_t id;
+                if (Np == 0) id = 0;
+                else if (uni) {
+                    id = (uint32_t)(u[h] * (double)Np);
+                    if (id >= Np) id = Np - 1u;
+                } else {
+                    const double target = u[h] * total;
+                    uint32_t lo = 0, hi = Np;  // first i with cdf[i] > target
+                    while (lo < hi) {
+                        const uint32_t mid = (lo + hi) >> 1;
+                        if (P.cdf[mid] > target) hi = mid; else lo = mid + 1u;
+                    }
+                    id = lo >= Np ? Np - 1u : lo;
+                }
+                P.pairs[2u * k + h] = id;
+            }
+        }
+    }
+}
+void launch_select_philox(const LaunchCfg& L, const PopDev* pops, uint32_t npops) {
+    k_select_philox<<<L.num_sms * 2, 256, 0, L.stream>>>(pops, npops);
+}
+
+// ---------------------------------------------------------------------------
+// Individual phenotype = genome 0 + genome 1 (individual_reducer_task_population_space_row.hpp:51-79),
+// or the constant 1.0 when every trait weight is zero (engine_batched_task.hpp:207-211);
+// then the fitness metric (GeneralFitness::operator(), general_fitness.hpp:101-119).
+__global__ void k_individuals(const PopDev* __restrict__ pops, uint32_t npops) {
+    for (uint32_t p = 0; p < npops; ++p) {
+        const PopDev& P = pops[p];
+        DevStatus* st = P.st;
+        const uint32_t N = st->N, T = P.T;
+        const bool neutral = st->nz_eff == 0;
+        if (blockIdx.x == 0 && threadIdx.x == 0) st->all_neutral = neutral ? 1u : 0u;
+        const double sig = sqrt(4.0 * (double)N * P.mu);  // normal/quadratic generators
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+            float4 z;
+            if (neutral) {
+                z = make_float4(1.f, 1.f, 1.f, 1.f);
+            } else {
+                const float4 a = reinterpret_cast<const float4*>(P.zg)[2u * i];
+                const float4 b = reinterpret_cast<const float4*>(P.zg)[2u * i + 1u];
+                z = make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+            }
+            if (T < 4) z.w = 0.f;
+            if (T < 3) z.z = 0.f;
+            if (T < 2) z.y = 0.f;
+            reinterpret_cast<float4*>(P.zi)[i] = z;
+            double f = 1.0;
+            const double z0 = (double)z.x;
+            switch (P.fitness) {
+                case 1: {  // gaussian (normal_fitness_metric.cpp:25-31)
+                    const double coeff = (1.0 / sig) * 0.398942280401432677939946059934;
+                    f = coeff * exp(-(z0 * z0) / (2.0 * sig * sig));
+                } break;
+                case 2: {  // quadratic (quadratic_fitness_metric.cpp:23-28)
+                    const double s = P.fit_param * sig;
+                    double r = z0 / s;
+                    r *= r;
+                    f = (r >= 1.0) ? 0.0 : 1.0 - r;
+                } break;
+                case 3: {  // gaussian_vs
+                    const double ss = (double)z.x * z.x + (double)z.y * z.y + (double)z.z * z.z + (double)z.w * z.w;
+                    f = exp(-ss / (2.0 * P.fit_param));
+                } break;
+                default: f = 1.0;
+            }
+            P.fit[i] = f;
+        }
+    }
+}
+void launch_individuals(const LaunchCfg& L, const PopDev* pops, uint32_t npops) {
+    k_individuals<<<L.num_sms * 2, 256, 0, L.stream>>>(pops, npops);
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic FP64 inclusive prefix sum of fitness (three phases with a
+// fixed association order), plus the total and the all-equal check.
+__global__ void __launch_bounds__(1024) k_fscan_a(const PopDev* __restrict__ pops, uint32_t npops) {
+    __shared__ double s_w[32];
+    for (uint32_t p = 0; p < npops; ++p) {
+        const PopDev& P = pops[p];
+        DevStatus* st = P.st;
+        const uint32_t N = st->N;
+        const uint32_t nch = (N + kScanChunk - 1) / kScanChunk;
+        if (blockIdx.x == 0 && threadIdx.x == 0) st->fit_const = 1u;
+        for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x) {
+            const uint32_t b = c * kScanChunk + threadIdx.x * 4u;
+            double s = 0.0;
+            for (uint32_t k = 0; k < 4; ++k) s += (b + k < N) ? P.fit[b + k] : 0.0;
+            s = warp_incl_f64(s);
+            if ((threadIdx.x & 31u) == 31u) s_w[threadIdx.x >> 5] = s;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double t = 0.0;
+                for (int i = 0; i < 32; ++i) t += s_w[i];
+                P.scan_part[c] = t;
+            }
+            __syncthreads();
+        }
+    }
+}
+__global__ void k_fscan_b(const PopDev* __restrict__ pops, uint32_t npops) {
+    const uint32_t p = blockIdx.x;
+    if (p >= npops || threadIdx.x != 0) return;
+    const PopDev& P = pops[p];
+    DevStatus* st = P.st;
+    const uint32_t N = st->N;
+    const uint32_t nch = (N + kScanChunk - 1) / kScanChunk;
+    double acc = 0.0;
+    for (uint32_t c = 0; c < nch; ++c) {
+        const double t = P.scan_part[c];
+        P.scan_part[c] = acc;
+        acc += t;
+    }
+    st->fit_total = acc;
+    if (!(acc > 0.0) && N > 0) st->err |= kErrFitness;
+}
+__global__ void __launch_bounds__(1024) k_fscan_c(const PopDev* __restrict__ pops, uint32_t npops) {
+    __shared__ double s_w[32];
+    for (uint32_t p = 0; p < npops; ++p) {
+        const PopDev& P = pops[p];
+        DevStatus* st = P.st;
+        const uint32_t N = st->N;
+        const uint32_t nch = (N + kScanChunk - 1) / kScanChunk;
+        const double f0 = N ? P.fit[0] : 0.0;
+        for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x) {
+            const uint32_t b = c * kScanChunk + threadIdx.x * 4u;
+            double v[4], s = 0.0;
+            bool same = true;
+            for (uint32_t k = 0; k < 4; ++k) {
+                v[k] = (b + k < N) ? P.fit[b + k] : 0.0;
+                if (b + k < N && v[k] != f0) same = false;
+                s += v[k];
+            }
+            const double incl = warp_incl_f64(s);
+            if ((threadIdx.x & 31u) == 31u) s_w[threadIdx.x >> 5] = incl;
+            if (!__all_sync(0xffffffffu, same) && (threadIdx.x & 31u) == 0u) atomicAnd(&st->fit_const, 0u);
+            __syncthreads();
+            double woff = 0.0;
+            for (uint32_t i = 0; i < (threadIdx.x >> 5); ++i) woff += s_w[i];
+            // exclusive prefix inside the warp = inclusive value of the previous lane
+            const double prev = __shfl_up_sync(0xffffffffu, incl, 1);
+            const double excl_w = (threadIdx.x & 31u) ? prev : 0.0;
+            double r = P.scan_part[c] + (woff + excl_w);
+            for (uint32_t k = 0; k < 4; ++k) {
+                r += v[k];
+                if (b + k < N) P.cdf[b + k] = r;
+            }
+            __syncthreads();
+        }
+    }
+}
+void launch_cdf(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxN) {
+    const uint32_t nch = (maxN + kScanChunk - 1) / kScanChunk;
+    const uint32_t g = max(1u, min(nch, (uint32_t)L.num_sms * 2u));
+    k_fscan_a<<<g, 1024, 0, L.stream>>>(pops, npops);
+    k_fscan_b<<<npops, 32, 0, L.stream>>>(pops, npops);
+    k_fscan_c<<<g, 1024, 0, L.stream>>>(pops, npops);
+}
+
+// ---------------------------------------------------------------------------
+// Pre-seeded rows: bit (row, slot) iff seed_hash(seed,row,slot) < thr[slot].
+__global__ void k_seed_rows(const PopDev* __restrict__ pops, uint32_t p, const uint32_t* __restrict__ thr,
+                            uint64_t seed, uint32_t A) {
+    const PopDev& P = pops[p];
+    const DevStatus* st = P.st;
+    const uint32_t S = 2u * st->N, W = st->W;
+    uint64_t* rows = P.rows[st->cur];
+    const size_t total = (size_t)S * W;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t r = (uint32_t)(i / W), w = (uint32_t)(i % W);
+        uint64_t x = 0;
+        for (uint32_t j = 0; j < 64; ++j) {
+            const uint32_t a = w * 64u + j;
+            if (a < A && seed_hash(seed, r, a) < thr[a]) x |= 1ull << j;
+        }
+        rows[(size_t)r * P.Wcap + w] = x;
+    }
+}
+void launch_seed_rows(const LaunchCfg& L, const PopDev* pops, uint32_t p, const uint32_t* thr, uint64_t seed,
+                      uint32_t A) {
+    k_seed_rows<<<L.num_sms * 8, 256, 0, L.stream>>>(pops, p, thr, seed, A);
+}
+
+// ---------------------------------------------------------------------------
+// Column counts of the current child (count_alleles,
+// cuda/analysis/allele_frequency_kernels.hpp:20-73; column margins of
+// population_space_row_frequency_evaluator.hpp:37-62).
+__global__ void k_col_counts(const PopDev* __restrict__ pops, uint32_t p, uint32_t* __restrict__ counts, uint32_t A) {
+    const PopDev& P = pops[p];
+    const DevStatus* st = P.st;
+    const uint32_t S = 2u * st->N, W = st->W;
+    const uint64_t* rows = P.rows[st->cur];
+    // block (x: word, y: row group); thread = one bit of the word
+    const uint32_t w = blockIdx.x;
+    if (w >= W) return;
+    const uint32_t groups = gridDim.y, per = (S + groups - 1) / groups;
+    const uint32_t r0 = blockIdx.y * per, r1 = min(S, r0 + per);
+    const uint32_t j = threadIdx.x;  // 64 threads
+    uint32_t c = 0;
+    for (uint32_t r = r0; r < r1; ++r) c += (uint32_t)((rows[(size_t)r * P.Wcap + w] >> j) & 1ull);
+    const uint32_t a = w * 64u + j;
+    if (a < A && c) atomicAdd(&counts[a], c);
+}
+void launch_stats(const LaunchCfg& L, const PopDev* pops, uint32_t p, uint32_t* counts, uint32_t W) {
+    dim3 grid(max(1u, W), 64);
+    k_col_counts<<<grid, 64, 0, L.stream>>>(pops, p, counts, W * 64u);
+}
+
+}  // namespace clotho

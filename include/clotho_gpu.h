@@ -1,0 +1,225 @@
+/*
+ * clotho_gpu.h -- C-ABI of the GB300 (sm_103a) engine for the per-generation
+ * hot path of a putnampp/clotho forward-time simulation.
+ *
+ * The reference plugs its stages into Engine<RNG,Real,Block,Size,batched_task>
+ * through member typedefs (examples/QTLSim/engine_batched_task.hpp:84-103);
+ * each entry point below names the reference member it replaces.  Paths are
+ * relative to the putnampp/clotho source tree.
+ *
+ * Conventions
+ *  - Every call returns an int status: 0 on success, a negative CLOTHO_E_*
+ *    code on failure; clotho_last_error() gives the message.  No exception
+ *    crosses the ABI.
+ *  - A context owns one population (parent + child bitset spaces, allele and
+ *    trait tables, free-space lists) in device memory, and one CUDA stream.
+ *    Buffers are sized once at creation from clotho_desc capacities.
+ *  - Host pointers passed in are read before the call returns (host->device
+ *    copies complete before return); device work may still be in flight until
+ *    clotho_sync() or a call that returns host data.
+ *  - Bitset layout is the reference's population_space_row: row i is haploid
+ *    genome i, individual j owns rows 2j and 2j+1; allele slot a is bit a%64 of
+ *    word a/64; a row of A alleles has ceil(A/512)*8 words
+ *    (population_space_row_block.hpp:94-101).
+ *  - One context per host thread at a time.
+ */
+#ifndef CLOTHO_GPU_H_
+#define CLOTHO_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CLOTHO_ABI_VERSION 1
+
+typedef struct clotho_ctx clotho_ctx;
+
+/* status codes */
+#define CLOTHO_OK              0
+#define CLOTHO_E_ARG          -1   /* bad argument                            */
+#define CLOTHO_E_CUDA         -2   /* CUDA runtime error                      */
+#define CLOTHO_E_CAPACITY     -3   /* a size exceeds the context capacity     */
+#define CLOTHO_E_STATE        -4   /* call out of order                        */
+#define CLOTHO_E_DEVICE       -5   /* device-side check failed (see message)  */
+#define CLOTHO_E_NOMEM        -6   /* device allocation refused               */
+
+/* fitness metrics (fitness_toolkit registry, src/clotho/fitness/fitness_toolkit.cpp:50-78) */
+#define CLOTHO_FIT_CONSTANT    0   /* 1.0                                      */
+#define CLOTHO_FIT_GAUSSIAN    1   /* normal_fitness_metric.cpp:25-31, sigma = sqrt(4 N mu)
+                                      (normal_fitness_generator.cpp:36-52), trait 0 */
+#define CLOTHO_FIT_QUADRATIC   2   /* quadratic_fitness_metric.cpp:23-28,
+                                      s = scale*sqrt(4 N mu), trait 0        */
+#define CLOTHO_FIT_GAUSSIAN_VS 3   /* exp(-|z|^2 / (2 Vs)) over all traits     */
+
+/* flags */
+#define CLOTHO_FLAG_Q1         1u  /* reference behaviour: the second gamete of a
+                                      mate pair never recombines
+                                      (batch_crossover_taskwe_population_space_row.hpp:133-138) */
+
+typedef struct clotho_desc {
+    uint32_t max_individuals; /* N capacity; rows = 2N                        */
+    uint32_t max_alleles;     /* allele slot capacity (A)                      */
+    uint32_t traits;          /* T, 1..4 (traits.N)                            */
+    uint32_t max_events;      /* crossover events per generation (tape mode)  */
+    uint32_t max_mutations;   /* new mutations per generation                  */
+    uint32_t max_fixed;       /* fixed-allele table capacity                   */
+    int32_t  fitness;         /* CLOTHO_FIT_*                                  */
+    uint32_t flags;           /* CLOTHO_FLAG_*                                 */
+    double   fit_param;       /* quadratic: fitness.params.scale; gaussian_vs: Vs */
+    double   mu;              /* mutation.mu per sequence                       */
+    double   rho;             /* recombination.rho per gamete                   */
+    double   bias;            /* recombination.sequence_bias.p                  */
+    double   p_neutral;       /* neutral.p                                      */
+    double   eff_mean;        /* traits.mean                                    */
+    double   eff_sigma;       /* traits.sigma                                   */
+    uint64_t seed;            /* Philox-4x32-10 key for device-drawn generations */
+} clotho_desc;
+
+/* One generation of the event tape, in the reference's draw order
+ * (engine_batched_task.hpp:175-202).  These are the draws the reference's
+ * policies make with Boost.Random; given the same tape the engine produces
+ * the reference's genomes bit for bit. */
+typedef struct clotho_gen_tape {
+    uint32_t N;               /* offspring individuals                          */
+    uint32_t M;               /* new mutations (mutation_allocator.hpp:41-47)   */
+    const uint32_t *pairs;    /* [2N] (id0,id1) parent individuals per offspring
+                                 (general_fitness_selection_generator.hpp:104-113) */
+    const uint8_t  *swap;     /* [2N] strand-swap bit per gamete (batch_crossover_mtwe.hpp:135-145) */
+    const uint32_t *ev_off;   /* [2N+1] event lookup (batch_crossover_mtwe.hpp:117-133) */
+    const double   *ev_pos;   /* [ev_off[2N]] breakpoint positions, any order   */
+    const uint32_t *mut_seq;  /* [M] target offspring row (batch_mutation_task_population_space_row.hpp:77-81) */
+    const double   *mut_pos;  /* [M] allele position in [0,1) (allele_generator_vector.hpp:76-83) */
+    const float    *mut_eff;  /* [M*T] allele effects (trait_space_generator.hpp:118-129) */
+} clotho_gen_tape;
+
+typedef struct clotho_info {
+    uint32_t generation;      /* number of the next generation (age of its mutations) */
+    uint32_t N;               /* individuals of the current (child) population  */
+    uint32_t A;               /* allele slots (getMaxAlleles)                   */
+    uint32_t W;               /* row width in 64-bit words (getMaxBlocks)       */
+    uint32_t fixed_count;     /* last free-space analysis (free_space_details.hpp:193-277) */
+    uint32_t lost_count;
+    uint32_t free_count;
+    uint32_t variable_count;
+    uint32_t fixed_total;     /* alleles in the fixed table                     */
+    uint32_t last_M;          /* mutations of the last generation               */
+    uint32_t all_neutral;     /* phenotype was the constant 1.0 path            */
+    uint32_t device_error;    /* sticky CLOTHO_DEVERR_* bits                    */
+    double   mean_fitness;    /* of the current population                     */
+} clotho_info;
+
+/* device error bits reported in clotho_info.device_error */
+#define CLOTHO_DEVERR_ALLELES  1u   /* allele capacity exceeded               */
+#define CLOTHO_DEVERR_FIXED    2u   /* fixed table capacity exceeded          */
+#define CLOTHO_DEVERR_EVENTS   4u   /* more than 128 device-drawn events per gamete */
+#define CLOTHO_DEVERR_PARENT   8u   /* tape parent index out of range         */
+#define CLOTHO_DEVERR_SEQ     16u   /* tape mutation row out of range         */
+#define CLOTHO_DEVERR_MUT     32u   /* mutation capacity exceeded             */
+#define CLOTHO_DEVERR_FITNESS 64u   /* all fitness zero: uniform selection used */
+
+/* ---- lifetime ---------------------------------------------------------- */
+int  clotho_create(const clotho_desc *desc, clotho_ctx **out);
+int  clotho_destroy(clotho_ctx *ctx);
+const char *clotho_last_error(const clotho_ctx *ctx);
+/* Device bytes held by the context. */
+size_t clotho_footprint(const clotho_ctx *ctx);
+/* Bytes a context with this descriptor would allocate (admission control). */
+size_t clotho_footprint_for(const clotho_desc *desc);
+int  clotho_sync(clotho_ctx *ctx);
+
+/* ---- population set-up ------------------------------------------------- */
+/* Engine::init(0) (engine_batched_task.hpp:143-161): N0 individuals, no alleles. */
+int  clotho_init(clotho_ctx *ctx, uint32_t N0);
+/* Pre-seeded start: A slots with positions pos[A] and effects eff[A*T]; bit
+ * (row, slot) is set iff the seed hash of (seed,row,slot) < thr[slot]
+ * (splitmix64 finaliser of seed + 0x9E3779B97F4A7C15*((row<<32)+slot+1),
+ * upper 32 bits).  Ages are 0.  Phenotypes and fitness are evaluated. */
+int  clotho_seed_population(clotho_ctx *ctx, uint32_t N, uint32_t A, const double *pos,
+                            const float *eff, const uint32_t *thr, uint64_t seed);
+
+/* ---- fused generation (the hot path) ------------------------------------ */
+/* Engine::simulate() (engine_batched_task.hpp:163-223) with the tape standing
+ * in for the RNG draws: free space + fixed removal (FreeSpaceAnalyzerMT,
+ * updateFixedAlleles :303-345), crossover (BatchCrossoverMTWE), mutation
+ * (BatchMutationMT), phenotype (BatchPhenotypeMT) and fitness (GeneralFitness),
+ * with no host synchronisation. */
+int  clotho_generation_tape(clotho_ctx *ctx, const clotho_gen_tape *tape);
+/* The same step with every draw made on the device (Philox-4x32-10 keyed by
+ * (seed, generation, stream, index)); parents are sampled by an FP64 inclusive
+ * prefix sum of fitness.  N = offspring individuals. */
+int  clotho_generation_philox(clotho_ctx *ctx, uint32_t N);
+/* G device-drawn generations replayed from one captured CUDA graph. */
+int  clotho_run_philox(clotho_ctx *ctx, uint32_t N, uint32_t G);
+
+/* ---- staged entry points (one per reference policy) --------------------- */
+/* Start a generation: swap parent/child (engine_batched_task.hpp:164). */
+int  clotho_begin_generation(clotho_ctx *ctx, uint32_t N, uint32_t M);
+/* FreeSpaceAnalyzerMT::operator() (free_space_mt_population_space_row_interlaced.hpp:41-89)
+ * + analyze_free_indices (free_space_details.hpp:299-357) + fixed removal
+ * (engine_batched_task.hpp:303-345) + child_max_alleles (:287-301).
+ * counts[3] = {fixed, lost, free} (may be NULL). */
+int  clotho_free_space(clotho_ctx *ctx, uint32_t *counts);
+/* SelectionGenerator::update from tape pairs (general_fitness_selection_generator.hpp:45-69). */
+int  clotho_set_pairs(clotho_ctx *ctx, const uint32_t *pairs);
+/* SelectionGenerator::update on the device: FP64 prefix sum of the parent
+ * fitness and one uniform per draw (2N draws); pairs_out may be NULL. */
+int  clotho_select(clotho_ctx *ctx, uint32_t *pairs_out);
+/* BatchCrossoverMTWE::operator() (batch_crossover_mtwe.hpp:51-113). */
+int  clotho_crossover(clotho_ctx *ctx, const uint8_t *swap, const uint32_t *ev_off,
+                      const double *ev_pos);
+/* BatchMutationMT::operator() (batch_mutation_mt.hpp:67-81). */
+int  clotho_mutate(clotho_ctx *ctx, const uint32_t *mut_seq, const double *mut_pos,
+                   const float *mut_eff);
+/* BatchPhenotypeMT::operator() (batch_phenotype_mt_population_space_row.hpp:62-72). */
+int  clotho_phenotype(clotho_ctx *ctx);
+/* GeneralFitness::operator() (general_fitness.hpp:101-119). */
+int  clotho_fitness(clotho_ctx *ctx);
+/* Finish the generation (++m_generation, engine_batched_task.hpp:222). */
+int  clotho_end_generation(clotho_ctx *ctx);
+
+/* ---- read-back (synchronising) ------------------------------------------ */
+int  clotho_get_info(clotho_ctx *ctx, clotho_info *out);
+/* Current child rows, 2N x W words (reference width). */
+int  clotho_get_rows(clotho_ctx *ctx, uint64_t *dst, size_t dst_words);
+/* Allele table [A]: positions, ages, effects [A*T] (FP32). */
+int  clotho_get_alleles(clotho_ctx *ctx, double *pos, uint32_t *age, float *eff);
+/* Fixed-allele table [fixed_total]. */
+int  clotho_get_fixed(clotho_ctx *ctx, double *pos, uint32_t *age, float *eff);
+/* Free list of the last analysis [free_count]: fixed ascending, then lost ascending. */
+int  clotho_get_free(clotho_ctx *ctx, uint32_t *dst);
+int  clotho_get_genome_traits(clotho_ctx *ctx, float *dst);   /* [2N*T] */
+int  clotho_get_phenotypes(clotho_ctx *ctx, float *dst);      /* [N*T]  */
+int  clotho_get_fitness(clotho_ctx *ctx, double *dst);        /* [N]    */
+int  clotho_get_pairs(clotho_ctx *ctx, uint32_t *dst);        /* [2N] of the last generation */
+
+/* ---- statistics (allele_frequency, population_space_row_frequency_evaluator.hpp:37-62) */
+typedef struct clotho_stats {
+    uint32_t segregating;     /* slots with 0 < count < 2N                      */
+    uint32_t fixed_now;       /* slots with count == 2N                         */
+    double   mean_fitness;
+    double   mean_phenotype[4];
+    double   heterozygosity;  /* mean over slots of 2p(1-p) (sum over slots)    */
+} clotho_stats;
+/* sfs may be NULL; else sfs[k] for k in [0, sfs_len) counts slots carried by
+ * exactly k rows (k = 2N folded into the last bin when sfs_len <= 2N). */
+int  clotho_stats_compute(clotho_ctx *ctx, clotho_stats *out, uint32_t *sfs, uint32_t sfs_len);
+
+/* ---- timing ------------------------------------------------------------- */
+/* CUDA events on the context stream around the fused generation kernel.
+ * After enabling, clotho_kernel_time returns total ms and launch count of the
+ * dominant kernel since the last reset. */
+int  clotho_profile(clotho_ctx *ctx, int enable);
+int  clotho_kernel_time(clotho_ctx *ctx, double *total_ms, uint32_t *launches,
+                        uint64_t *rows_processed, uint64_t *words_processed);
+int  clotho_timer_begin(clotho_ctx *ctx);
+int  clotho_timer_end(clotho_ctx *ctx, double *ms);
+/* Count of kernels this context launched since creation. */
+uint64_t clotho_launch_count(const clotho_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CLOTHO_GPU_H_ */

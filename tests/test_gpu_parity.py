@@ -1,0 +1,245 @@
+"""GPU parity against the CPU oracle through the C-ABI.
+
+The oracle (oracle/clotho_oracle.cpp, the restatement of QTLSimMT's
+Engine::simulate) draws each generation in the reference's order and records
+the tape; libclotho_gpu.so replays the same tape.  Bar:
+  * bit-exact for integer/bit work: every offspring row, allele count and row
+    width, the free list (fixed ascending then lost ascending), counts, the
+    allele table (positions, ages), the fixed-allele table;
+  * phenotypes: the GPU sums FP32 effects in FP32; the FP64 oracle sums the same
+    (FP32-valued) effects in FP64.  The tolerance written here is the a-priori
+    bound of a sequential FP32 sum of n terms plus one final add:
+    |z_gpu - z_fp64| <= (n + 1) * 2^-24 * sum|w_i|  over the n set bits of the
+    individual (both genomes);
+  * fitness: equal to the metric applied to the GPU phenotype in FP64
+    (rtol 1e-12), and within the propagated phenotype bound of the oracle.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from tests.conftest import gpu_available
+
+pytestmark = pytest.mark.gpu
+
+if not gpu_available():  # collected on CPU machines, skipped there
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+import clotho_gb300 as cg  # noqa: E402
+
+FITS = {"constant": oracle.FIT_CONSTANT, "gaussian": oracle.FIT_GAUSSIAN, "quadratic": oracle.FIT_QUADRATIC,
+        "gaussian_vs": oracle.FIT_GAUSSIAN_VS}
+
+
+def make_pair(N, A_cap, T=1, fitness="constant", fit_param=1.0, mu=0.05, rho=0.5, bias=0.5, p_neutral=1.0,
+              q1=True, seed=11, threads=2):
+    orc = oracle.Oracle(T=T, fitness=FITS[fitness], fit_param=fit_param, mu=mu, rho=rho, bias=bias,
+                        p_neutral=p_neutral, q1=q1, threads=threads, seed=seed)
+    gpu = cg.Population(N, A_cap, T, fitness=fitness, fit_param=fit_param, mu=mu, rho=rho, bias=bias,
+                        p_neutral=p_neutral, q1=q1, seed=seed, max_events=int(4 * N * rho + 4096),
+                        max_mutations=int(4 * N * mu + 4096), max_fixed=1 << 16)
+    return orc, gpu
+
+
+def pheno_bound(rows, eff):
+    """(n+1) 2^-24 sum|w| per individual from the rows and the FP32 effects."""
+    S, W = rows.shape
+    A = eff.shape[0]
+    bits = np.unpackbits(rows.view(np.uint8).reshape(S, W * 8), axis=1, bitorder="little")[:, :A].astype(np.float64)
+    absw = np.abs(eff.astype(np.float64))
+    s = bits @ absw                       # [S, T]
+    n = bits.sum(axis=1)                  # [S]
+    s_ind = s[0::2] + s[1::2]
+    n_ind = (n[0::2] + n[1::2])[:, None]
+    return (n_ind + 1.0) * 2.0 ** -24 * s_ind + 1e-30
+
+
+def fitness_of(z, kind, fit_param, N, mu):
+    z = z.astype(np.float64)
+    if kind == "constant":
+        return np.ones(len(z))
+    if kind == "gaussian":
+        sig = np.sqrt(4.0 * N * mu)
+        return (1.0 / sig) * 0.398942280401432677939946059934 * np.exp(-(z[:, 0] ** 2) / (2 * sig * sig))
+    if kind == "quadratic":
+        s = fit_param * np.sqrt(4.0 * N * mu)
+        r = (z[:, 0] / s) ** 2
+        return np.where(r >= 1.0, 0.0, 1.0 - r)
+    if kind == "gaussian_vs":
+        return np.exp(-(z ** 2).sum(axis=1) / (2 * fit_param))
+    raise ValueError(kind)
+
+
+def compare_state(orc, gpu, g, check_pheno=True, kind="constant", fit_param=1.0, mu=0.0):
+    oi, gi = orc.info(), gpu.info()
+    assert gi["device_error"] == 0, f"gen {g}: device error {gi['device_error']}"
+    for k in ("N", "A", "fixed_count", "lost_count", "free_count", "fixed_total", "generation"):
+        assert oi[k] == gi[k], f"gen {g}: {k} oracle={oi[k]} gpu={gi[k]}"
+    assert oi["B"] == gi["W"], f"gen {g}: width oracle={oi['B']} gpu={gi['W']}"
+    ro, rg = orc.rows(), gpu.rows()
+    assert ro.shape == rg.shape
+    if not np.array_equal(ro, rg):
+        bad = np.argwhere(ro != rg)
+        r, w = bad[0]
+        raise AssertionError(f"gen {g}: {len(bad)} words differ; first row {r} word {w}: "
+                             f"oracle {int(ro[r, w]):#x} gpu {int(rg[r, w]):#x}")
+    assert np.array_equal(orc.free_list(), gpu.free_list()), f"gen {g}: free list differs"
+    po, ao, eo = orc.alleles()
+    pg, ag, eg = gpu.alleles()
+    assert np.array_equal(po, pg) and np.array_equal(ao, ag), f"gen {g}: allele table differs"
+    assert np.array_equal(eo, eg.astype(np.float64)), f"gen {g}: trait table differs"
+    fpo, fao, feo = orc.fixed()
+    fpg, fag, feg = gpu.fixed()
+    assert np.array_equal(fpo, fpg) and np.array_equal(fao, fag) and np.array_equal(feo, feg.astype(np.float64))
+    if check_pheno:
+        zo, zg = orc.phenotypes(), gpu.phenotypes().astype(np.float64)
+        if oi["all_neutral"]:
+            assert np.all(zg == 1.0)
+        else:
+            bound = pheno_bound(rg, eg)
+            err = np.abs(zo - zg)
+            assert np.all(err <= bound), f"gen {g}: phenotype error {err.max()} > bound"
+        fg = gpu.fitness()
+        np.testing.assert_allclose(fg, fitness_of(gpu.phenotypes(), kind, fit_param, gi["N"], mu), rtol=1e-12,
+                                   atol=1e-300)
+
+
+def run_parity(G, N, A_cap, **kw):
+    orc, gpu = make_pair(N, A_cap, **kw)
+    orc.init(N)
+    gpu.init(N)
+    for g in range(G):
+        tape = orc.step_record(N)
+        gpu.simulate(tape)
+        compare_state(orc, gpu, g, kind=kw.get("fitness", "constant"), fit_param=kw.get("fit_param", 1.0),
+                      mu=kw.get("mu", 0.05))
+    return orc, gpu
+
+
+def test_neutral_wright_fisher_bit_exact():
+    # C1-shaped (neutral, uniform parents), small N so the oracle is instant
+    orc, gpu = run_parity(40, 300, 8192, mu=0.2, rho=0.3, p_neutral=1.0)
+    assert orc.info()["A"] > 64
+
+
+def test_qtl_selection_bit_exact_and_phenotype_bound():
+    # C2-shaped: single trait, N(0,1) effects, exp(-z^2/2), fitness-proportional parents
+    run_parity(30, 250, 8192, T=1, fitness="gaussian_vs", fit_param=1.0, mu=0.2, rho=1.0, p_neutral=0.0)
+
+
+def test_four_traits_reference_gaussian_q1_off():
+    run_parity(20, 200, 8192, T=4, fitness="gaussian", mu=0.3, rho=3.0, p_neutral=0.3, q1=False)
+
+
+def test_quadratic_three_traits():
+    run_parity(15, 150, 4096, T=3, fitness="quadratic", fit_param=3.0, mu=0.2, rho=2.0, p_neutral=0.5)
+
+
+def test_many_events_beyond_register_set():
+    # rho large enough that many gametes carry more than 16 breakpoints
+    run_parity(8, 100, 4096, mu=0.3, rho=24.0, p_neutral=1.0, q1=False)
+
+
+def test_staged_policies_equal_fused():
+    orc, gpu = make_pair(180, 4096, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.2, rho=1.5, p_neutral=0.4)
+    gpu2 = cg.Population(180, 4096, 2, fitness="gaussian_vs", fit_param=4.0, mu=0.2, rho=1.5, p_neutral=0.4,
+                         max_events=8192, max_mutations=8192, max_fixed=1 << 16)
+    orc.init(180)
+    gpu.init(180)
+    gpu2.init(180)
+    for g in range(12):
+        tape = orc.step_record(180)
+        gpu.simulate(tape)
+        gpu2.simulate_staged(tape)
+        compare_state(orc, gpu2, g, kind="gaussian_vs", fit_param=4.0)
+        assert np.array_equal(gpu.rows(), gpu2.rows())
+        assert np.array_equal(gpu.phenotypes(), gpu2.phenotypes())
+
+
+def test_seeded_population_parity():
+    rng = np.random.default_rng(5)
+    N, A, T = 200, 1500, 2
+    pos = rng.random(A)
+    eff = rng.standard_normal(A * T).astype(np.float32) * 0.1
+    thr = (rng.random(A) * 2 ** 32 * 0.3).astype(np.uint32)
+    orc, gpu = make_pair(N, 4096, T=T, fitness="gaussian_vs", fit_param=50.0, mu=0.1, rho=2.0, p_neutral=0.2)
+    orc.seed_population(N, pos, eff, thr, 99)
+    gpu.seed_population(N, pos, eff, thr, 99)
+    compare_state(orc, gpu, -1, kind="gaussian_vs", fit_param=50.0)
+    for g in range(10):
+        gpu.simulate(orc.step_record(N))
+        compare_state(orc, gpu, g, kind="gaussian_vs", fit_param=50.0)
+
+
+def test_edge_tie_breakpoint_equals_position():
+    # A breakpoint exactly at an allele's position counts as <= (upper_bound,
+    # classifiers/region_classifier.hpp:73): that allele comes from the bottom strand.
+    N = 4
+    orc, gpu = make_pair(N, 1024, mu=0.0, rho=0.0)
+    orc.init(N)
+    gpu.init(N)
+    # generation 1: give every row 3 alleles through mutations, positions 0.25/0.5/0.75
+    S = 2 * N
+    seq = np.array([0, 1, 1, 2, 3, 4, 5, 6, 7], np.uint32)
+    pos = np.array([0.25, 0.5, 0.75, 0.25, 0.5, 0.75, 0.5, 0.25, 0.75])
+    t1 = oracle.Tape(N, len(seq), np.arange(S, dtype=np.uint32) // 2 % N, np.zeros(S, np.uint8),
+                     np.zeros(S + 1, np.uint32), np.zeros(0), seq, pos, np.zeros(len(seq), np.float32))
+    orc.step_tape(t1)
+    gpu.simulate(t1)
+    compare_state(orc, gpu, 0)
+    # generation 2: one breakpoint exactly at 0.5 on every even gamete, swaps alternate
+    ev_off = np.zeros(S + 1, np.uint32)
+    ev_off[1:] = np.cumsum(np.array([1, 0] * N, np.uint32))
+    ev_pos = np.full(N, 0.5)
+    pairs = np.array([0, 1, 2, 3, 1, 0, 3, 2], np.uint32)
+    t2 = oracle.Tape(N, 0, pairs, np.array([0, 1] * N, np.uint8), ev_off, ev_pos, np.zeros(0, np.uint32),
+                     np.zeros(0), np.zeros(0, np.float32))
+    orc.step_tape(t2)
+    gpu.simulate(t2)
+    compare_state(orc, gpu, 1)
+
+
+def test_edge_append_path_and_fixed_clearing():
+    # M > free forces appended slots; a mutation carried by every row becomes
+    # fixed, is cleared and recorded, and its slot is reused first.
+    N = 3
+    S = 2 * N
+    orc, gpu = make_pair(N, 2048, mu=0.0, rho=0.0)
+    orc.init(N)
+    gpu.init(N)
+    seq = np.arange(S, dtype=np.uint32)
+    t1 = oracle.Tape(N, S, np.zeros(S, np.uint32), np.zeros(S, np.uint8), np.zeros(S + 1, np.uint32), np.zeros(0),
+                     seq, np.linspace(0.1, 0.9, S), np.arange(S, dtype=np.float32))
+    orc.step_tape(t1)
+    gpu.simulate(t1)
+    compare_state(orc, gpu, 0)
+    # every gamete copies row 0 of parent 0 (slot 0 then present in all rows -> fixed next time)
+    t2 = oracle.Tape(N, 700, np.zeros(S, np.uint32), np.zeros(S, np.uint8), np.zeros(S + 1, np.uint32),
+                     np.zeros(0), np.arange(700, dtype=np.uint32) % S, np.linspace(0.01, 0.99, 700),
+                     np.ones(700, np.float32))
+    orc.step_tape(t2)
+    gpu.simulate(t2)
+    compare_state(orc, gpu, 1)
+    t3 = oracle.Tape(N, 5, np.array([0, 1, 2, 0, 1, 2], np.uint32), np.array([0, 1, 0, 1, 0, 1], np.uint8),
+                     np.zeros(S + 1, np.uint32), np.zeros(0), np.array([0, 1, 2, 3, 4], np.uint32),
+                     np.array([0.3, 0.31, 0.32, 0.33, 0.34]), np.ones(5, np.float32))
+    orc.step_tape(t3)
+    gpu.simulate(t3)
+    compare_state(orc, gpu, 2)
+    assert orc.info()["fixed_total"] >= 1
+
+
+def test_philox_mode_runs_and_is_deterministic():
+    kw = dict(fitness="gaussian_vs", fit_param=2.0, mu=0.1, rho=1.0, p_neutral=0.5, seed=2024,
+              max_events=1 << 16, max_mutations=1 << 14, max_fixed=1 << 16)
+    a = cg.Population(2000, 1 << 14, 2, **kw)
+    b = cg.Population(2000, 1 << 14, 2, **kw)
+    a.init(2000)
+    b.init(2000)
+    a.run_philox(2000, 30)
+    for _ in range(30):
+        b.simulate_philox(2000)
+    a.check()
+    assert np.array_equal(a.rows(), b.rows())
+    assert np.array_equal(a.phenotypes(), b.phenotypes())
+    assert a.info()["A"] > 100
