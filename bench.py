@@ -1,0 +1,352 @@
+#!/usr/bin/env python3
+"""bench.py -- sequence-generations/s of Clotho's per-generation hot path on GB300.
+
+Workload: N=1e6 diploid (2e6 rows), 4 traits, 65,536 allele slots (W<=1,024
+words per row), rho=5, mu=1e-3 per sequence, pre-seeded neutral 1/i load,
+device Philox draws, reference `gaussian` fitness (sigma = sqrt(4 N mu)),
+fitness-proportional parents from an FP64 prefix sum.  One step = one
+generation (free space, selection, crossover, mutation, phenotype, fitness).
+
+  value    device-resident throughput, K generations replayed from one CUDA graph.
+  e2e      the same metric through the C-ABI tape call with host buffers: every
+           step copies that generation's tape from pinned host memory and reads
+           the step's status (mean fitness) back.
+  roofline the fused generation kernel: algorithmic bytes 16*W_live*S per launch
+           (each child row written once, each selected parent row read once)
+           over its CUDA-event duration, against MEASURED_PEAKS.json hbm_gbs.
+  cpu_baseline  the CPU oracle (restatement of the reference's path) on the
+           host cores, on a bounded sample of the same workload.
+
+--impl reference times that CPU restatement alone (the reference itself needs
+Boost, which is absent).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "sequence-generations/s at N=1e6 (HBM % peak)"
+UNIT = "seq-gen/s"
+FALLBACK_HBM_GBS = 6800.0
+CPU_SAMPLE_N = 20_000
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--n", type=int, default=None, help="override N (small runs / profiling)")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--profile-gens", type=int, default=4)
+    p.add_argument("--kernel-only", action="store_true", help="seed + eager generations only (ncu runs)")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-reduce over replicas (gloo; the data path has no collective)."""
+
+    def __init__(self, world):
+        self.world = world
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic():
+    path = os.path.join(ROOT, "profiles", "generation_kernel_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_population(cg, w, N, extra_fixed=1 << 20):
+    return cg.Population(N, w.max_alleles, w.T, fitness=w.fitness, fit_param=w.fit_param, mu=w.mu, rho=w.rho,
+                         bias=w.bias, p_neutral=w.p_neutral, seed=20261203, max_fixed=extra_fixed,
+                         max_events=int(2 * N * w.rho * 1.05 + 4096), max_mutations=int(2 * N * w.mu * 1.5 + 4096))
+
+
+def pinned_tape(cg, tape):
+    """Copy a GenTape into one page-locked block; returns (tape view, keepalive)."""
+    import numpy as np
+    L = cg.capi.load()
+    t = tape.contiguous()
+    arrs = [t.pairs, t.swap, t.ev_off, t.ev_pos, t.mut_seq, t.mut_pos, t.mut_eff]
+    offs, total = [], 0
+    for a in arrs:
+        total = (total + 63) & ~63
+        offs.append(total)
+        total += a.nbytes
+    ptr = C.c_void_p()
+    if L.clotho_host_alloc(max(total, 64), C.byref(ptr)) != 0:
+        raise RuntimeError("clotho_host_alloc failed")
+    buf = (C.c_char * max(total, 64)).from_address(ptr.value)
+    views = []
+    for a, o in zip(arrs, offs):
+        v = np.frombuffer(buf, dtype=a.dtype, count=a.size, offset=o)
+        v[...] = a
+        views.append(v)
+    out = cg.GenTape(t.N, t.M, *views)
+    return out, ptr
+
+
+def run_cpu_oracle(w, N, steps, warmup, threads):
+    """The CPU restatement on the host cores: bounded sample of the workload
+    (N individuals, same allele load and per-row width)."""
+    import oracle
+    from clotho_gb300.workloads import seeded_start
+    fit = {"constant": oracle.FIT_CONSTANT, "gaussian": oracle.FIT_GAUSSIAN, "quadratic": oracle.FIT_QUADRATIC,
+           "gaussian_vs": oracle.FIT_GAUSSIAN_VS}[w.fitness]
+    orc = oracle.Oracle(T=w.T, fitness=fit, fit_param=w.fit_param, mu=w.mu, rho=w.rho, bias=w.bias,
+                        p_neutral=w.p_neutral, q1=True, threads=threads, seed=7)
+    pos, eff, thr = seeded_start(w, N=N)
+    orc.seed_population(N, pos, eff, thr, 99)
+    for _ in range(warmup):
+        orc.step_record(N)
+    t0 = time.perf_counter()
+    stages = {}
+    for _ in range(steps):
+        orc.step_record(N)
+        for k, v in orc.times().items():
+            stages[k] = stages.get(k, 0.0) + v
+    dt = time.perf_counter() - t0
+    info = orc.info()
+    orc.close()
+    return 2.0 * N * steps / dt, dt, info, stages
+
+
+def reference_arm(args, rank):
+    from clotho_gb300.workloads import LARGE_N
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    N = CPU_SAMPLE_N
+    v, dt, info, stages = run_cpu_oracle(LARGE_N, N, args.steps, args.warmup, threads)
+    sample = (f"CPU restatement of the reference path (oracle/clotho_oracle.cpp), N={N} individuals "
+              f"({2 * N} rows) with the same pre-seeded allele load (A={info['A']}, W={info['B']} words/row), "
+              f"{args.steps} generations after {args.warmup} warm-up")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": LARGE_N.name, "N_sample": N, "T": LARGE_N.T, "rho": LARGE_N.rho,
+                       "mu": LARGE_N.mu, "threads": threads},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                             "stage_seconds": stages},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        reference_arm(args, rank)
+        return
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = Dist(world)
+
+    import numpy as np
+    import clotho_gb300 as cg
+    from clotho_gb300.workloads import LARGE_N, seeded_start
+
+    w = LARGE_N
+    N = args.n or w.N
+    pop = make_population(cg, w, N)
+    pos, eff, thr = seeded_start(w, N=N)
+    pop.seed_population(N, pos, eff, thr, 99)
+
+    if args.kernel_only:
+        for _ in range(args.warmup + args.steps):
+            pop.simulate_philox(N)
+        pop.sync()
+        pop.check()
+        print(json.dumps({"kernel_only": True, "N": N, "info": pop.info()}))
+        return
+
+    for _ in range(args.warmup):
+        pop.simulate_philox(N)
+    pop.sync()
+    pop.check()
+
+    # ---- timed region: K device-resident generations (graph replay)
+    clocks = ClockSampler(0 if world == 1 else local)
+    clocks.start()
+    dist.barrier()
+    pop.sync()
+    l0 = pop.launches
+    pop.timer_begin()
+    pop.run_philox(N, args.steps)
+    ms = pop.timer_end()
+    pop.sync()
+    dist.barrier()
+    launches = pop.launches - l0
+    ms = dist.max(ms)
+    clk = clocks.stop()
+    info = pop.info()
+    pop.check()
+    value = 2.0 * N * args.steps * world / (ms / 1e3)
+
+    # ---- dominant kernel: CUDA events around each fused generation launch
+    pop.profile(True)
+    for _ in range(args.profile_gens):
+        pop.simulate_philox(N)
+    kms, nl, rows_done, words_done = pop.kernel_time()
+    pop.profile(False)
+    avg_ms = kms / max(nl, 1)
+    bytes_per_launch = 16.0 * words_done / max(nl, 1)       # 16 B per (row, live word)
+    w_live = words_done / max(rows_done, 1)
+    achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = ncu_traffic()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": (traffic or {}).get("bytes_per_launch") if traffic else None,
+                "peak_kind": f"of {peak_kind}", "kernel": "k_generation", "kernel_ms": avg_ms,
+                "algorithmic_bytes_per_launch": bytes_per_launch, "W_live": w_live,
+                "step_share": (avg_ms * args.steps) / ms if ms else None}
+
+    # ---- end to end through the C-ABI tape call with host buffers
+    e2e = None
+    if not args.no_e2e:
+        rng = np.random.default_rng(1)
+        tapes, keep = [], []
+        for _ in range(2):
+            t = cg.neutral_tape(rng, N, w.mu, w.rho, w.bias, w.T, p_neutral=w.p_neutral)
+            pt, ptr = pinned_tape(cg, t)
+            tapes.append(pt)
+            keep.append(ptr)
+        h2d = tapes[0].nbytes + 8
+        pop.simulate(tapes[0])
+        pop.info()
+        dist.barrier()
+        pop.sync()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            pop.simulate(tapes[k % 2])
+            pop.info()  # device->host read of the step's status (mean fitness)
+        dt = time.perf_counter() - t0
+        dist.barrier()
+        dt = dist.max(dt)
+        pop.check()
+        e2e = {"value": 2.0 * N * args.steps * world / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": 80, "ms_per_step": 1e3 * dt / args.steps,
+               "note": "tape call per generation (uniform-parent tape), wall clock around H2D + kernels + D2H"}
+        for ptr in keep:
+            cg.capi.load().clotho_host_free(ptr)
+
+    # ---- CPU baseline (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, dt, oinfo, stages = run_cpu_oracle(w, CPU_SAMPLE_N, 2, 0, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": (f"oracle/clotho_oracle.cpp on {threads} host threads, N={CPU_SAMPLE_N} individuals, same "
+                          f"allele load (A={oinfo['A']}, W={oinfo['B']}), 2 generations, {dt:.1f} s"),
+               "stage_seconds": stages}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+                "config": {"workload": w.name, "N": N, "T": w.T, "A": info["A"], "W_live": info["W"],
+                           "rho": w.rho, "mu": w.mu, "rng": "device Philox-4x32-10", "fitness": w.fitness,
+                           "parallelism": "replicas" if world > 1 else "single",
+                           "l2": "inputs larger than L2 (rows 16 GB per population)"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -218,13 +218,13 @@ class Population:
 
     def genome_traits(self) -> np.ndarray:
         S = 2 * self.info()["N"]
-        out = np.zeros(S * self.T, np.float32)
+        out = np.zeros(S * self.T, np.float64)
         self._ck(self.L.clotho_get_genome_traits(self.h, _ptr(out)), "get_genome_traits")
         return out.reshape(S, self.T)
 
     def phenotypes(self) -> np.ndarray:
         N = self.info()["N"]
-        out = np.zeros(N * self.T, np.float32)
+        out = np.zeros(N * self.T, np.float64)
         self._ck(self.L.clotho_get_phenotypes(self.h, _ptr(out)), "get_phenotypes")
         return out.reshape(N, self.T)
 

@@ -81,6 +81,8 @@ SIGNATURES = {
     "clotho_timer_begin": (C.c_int, [vp]),
     "clotho_timer_end": (C.c_int, [vp, C.POINTER(C.c_double)]),
     "clotho_launch_count": (u64, [vp]),
+    "clotho_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(vp)]),
+    "clotho_host_free": (C.c_int, [vp]),
 }
 
 _lib = None

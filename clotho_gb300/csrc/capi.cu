@@ -28,7 +28,7 @@ struct PopHost {
 };
 
 struct Geometry {
-    uint32_t Ncap, Scap, Wcap, Aslots, Mcap, EVcap, FXcap, T;
+    uint32_t Ncap, Scap, Wcap, Aslots, Mcap, EVcap, FXcap, T, NB;
 };
 
 Geometry geometry(const clotho_desc& d) {
@@ -42,6 +42,8 @@ Geometry geometry(const clotho_desc& d) {
     g.EVcap = d.max_events ? d.max_events : 1;
     g.FXcap = d.max_fixed ? d.max_fixed : 1;
     g.T = d.traits;
+    g.NB = 1024;
+    while (g.NB < g.Aslots) g.NB <<= 1;
     return g;
 }
 
@@ -55,10 +57,11 @@ std::vector<size_t> sizes_of(const Geometry& g) {
         W * 8, W * 8, W * 8,             // fixmask, accF, accV
         A * 4, A * 8, A * 4, A * T * 4,  // free_list, pos, age, eff
         g.FXcap * 8ull, g.FXcap * 4ull, g.FXcap * T * 4ull,
-        S * 16, N * 16, N * 8, N * 8,    // zg, zi, fit, cdf
-        (N / 1024 + 8) * 8, (S / 1024 + 8) * 4,
+        S * 32, S * 32, N * 32, N * 8, N * 8,    // zg[0], zg[1], zi, fit, cdf
+        (N / 1024 + 8) * 8, ((S > g.NB ? S : g.NB) / 1024 + 8) * 4ull,
         (S + 1) * 4 * 2ull,              // row_cnt, row_off
         S * 4, g.Mcap * 4ull, g.Mcap * 4ull,  // row_cur, row_mut, mut_slot
+        (g.NB + 1ull) * 4 * 2, g.NB * 4ull, A * 8, A * 4,  // bcnt+boff, bcur, bpos, rank
         sizeof(DevStatus),
         // two tape sets: pairs, swap, ev_off, ev_pos, mut_seq, mut_pos, mut_eff
         S * 4, S, (S + 1) * 4, g.EVcap * 8ull, g.Mcap * 4ull, g.Mcap * 8ull, g.Mcap * T * 4ull,
@@ -90,7 +93,7 @@ struct clotho_ctx {
     cudaGraphExec_t graph = nullptr;
     uint32_t graph_N = 0;
     bool in_step = false;
-    uint32_t maxW = 0, maxS = 0, maxN = 0;
+    uint32_t maxW = 0, maxS = 0, maxN = 0, maxNB = 0;
 };
 
 namespace {
@@ -149,14 +152,18 @@ int alloc_pop(clotho_ctx* ctx, const clotho_desc& d, PopHost** out) {
     b.fixmask = (uint64_t*)ptr[k++]; b.accF = (uint64_t*)ptr[k++]; b.accV = (uint64_t*)ptr[k++];
     b.free_list = (uint32_t*)ptr[k++]; b.pos = (double*)ptr[k++]; b.age = (uint32_t*)ptr[k++]; b.eff = (float*)ptr[k++];
     b.fx_pos = (double*)ptr[k++]; b.fx_age = (uint32_t*)ptr[k++]; b.fx_eff = (float*)ptr[k++];
-    b.zg = (float*)ptr[k++]; b.zi = (float*)ptr[k++]; b.fit = (double*)ptr[k++]; b.cdf = (double*)ptr[k++];
+    b.zg[0] = (double*)ptr[k++]; b.zg[1] = (double*)ptr[k++];
+    b.zi = (double*)ptr[k++]; b.fit = (double*)ptr[k++]; b.cdf = (double*)ptr[k++];
     b.scan_part = (double*)ptr[k++]; b.scan_upart = (uint32_t*)ptr[k++];
     b.row_cnt = (uint32_t*)ptr[k++];
     b.row_off = b.row_cnt + (g.Scap + 1);
     b.row_cur = (uint32_t*)ptr[k++]; b.row_mut = (uint32_t*)ptr[k++]; b.mut_slot = (uint32_t*)ptr[k++];
+    b.bcnt = (uint32_t*)ptr[k++];
+    b.boff = b.bcnt + (g.NB + 1);
+    b.bcur = (uint32_t*)ptr[k++]; b.bpos = (double*)ptr[k++]; b.rank = (uint32_t*)ptr[k++];
     b.st = (DevStatus*)ptr[k++];
     b.Scap = g.Scap; b.Ncap = g.Ncap; b.Wcap = g.Wcap; b.Acap = g.Aslots; b.Mcap = g.Mcap;
-    b.EVcap = g.EVcap; b.FXcap = g.FXcap; b.T = g.T;
+    b.EVcap = g.EVcap; b.FXcap = g.FXcap; b.T = g.T; b.NB = g.NB;
     b.mu = d.mu; b.rho = d.rho; b.bias = d.bias; b.p_neutral = d.p_neutral;
     b.eff_mean = d.eff_mean; b.eff_sigma = d.eff_sigma; b.fit_param = d.fit_param;
     b.exp_neg_rho = std::exp(-d.rho);
@@ -200,6 +207,7 @@ int sync_pop_arrays(clotho_ctx* ctx) {
         ctx->maxW = std::max(ctx->maxW, p->dev[0].Wcap);
         ctx->maxS = std::max(ctx->maxS, p->dev[0].Scap);
         ctx->maxN = std::max(ctx->maxN, p->dev[0].Ncap);
+        ctx->maxNB = std::max(ctx->maxNB, p->dev[0].NB);
     }
     if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
     CK(cudaStreamSynchronize(ctx->stream));
@@ -311,12 +319,13 @@ void enqueue_fused_step(clotho_ctx* ctx, uint32_t set, bool philox) {
     launch_fs_finalize(L, pops, n);
     if (!philox) launch_mut_csr_tape(L, pops, n, ctx->maxS);
     launch_mut_resolve(L, pops, n);
+    launch_ranks(L, pops, n, ctx->maxNB);
     if (philox) launch_select_philox(L, pops, n);
     launch_gen(ctx, pops, n, kFuseMut | kFusePheno | kFuseFs);
     launch_individuals(L, pops, n);
     launch_cdf(L, pops, n, ctx->maxN);
     launch_end(L, pops, n);
-    ctx->launches += philox ? 14 : 15;
+    ctx->launches += philox ? 20 : 21;
     for (PopHost* p : ctx->pops) p->acc_valid = true;
 }
 
@@ -559,7 +568,7 @@ int clotho_run_philox(clotho_ctx* ctx, uint32_t N, uint32_t G) {
     }
     for (uint32_t g = 1; g < G; ++g) {
         CK(cudaGraphLaunch(ctx->graph, ctx->stream));
-        ctx->launches += 14;
+        ctx->launches += 20;
     }
     return 0;
 }
@@ -641,7 +650,9 @@ int clotho_crossover(clotho_ctx* ctx, const uint8_t* swap, const uint32_t* ev_of
     if ((rc = h2d(ctx, D.swap, swap, 2ull * N, ctx->stream))) return rc;
     if ((rc = h2d(ctx, D.ev_off, ev_off, 2ull * N + 1, ctx->stream))) return rc;
     if ((rc = h2d(ctx, D.ev_pos, ev_pos, (size_t)ev_total, ctx->stream))) return rc;
-    // item prefix is already set by begin
+    // item prefix is already set by begin; ranks over the current positions
+    launch_ranks(cfg(ctx), ctx->d_pops[0], 1, ctx->maxNB);
+    ctx->launches += 6;
     launch_gen(ctx, ctx->d_pops[0], 1, 0u);
     if ((rc = check_launch(ctx, "crossover"))) return rc;
     CK(cudaStreamSynchronize(ctx->stream));
@@ -773,30 +784,30 @@ int clotho_get_free(clotho_ctx* ctx, uint32_t* dst) {
     return 0;
 }
 
-static int get_float4(clotho_ctx* ctx, const float* src, size_t n, float* dst) {
+static int get_double4(clotho_ctx* ctx, const double* src, size_t n, double* dst) {
     const uint32_t T = ctx->pops[0]->dev[0].T;
-    std::vector<float> tmp(n * 4);
-    if (n) CK(cudaMemcpyAsync(tmp.data(), src, n * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<double> tmp(n * 4);
+    if (n) CK(cudaMemcpyAsync(tmp.data(), src, n * 32, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     for (size_t i = 0; i < n; ++i)
         for (uint32_t t = 0; t < T; ++t) dst[i * T + t] = tmp[i * 4 + t];
     return 0;
 }
 
-int clotho_get_genome_traits(clotho_ctx* ctx, float* dst) {
+int clotho_get_genome_traits(clotho_ctx* ctx, double* dst) {
     if (!ctx) return CLOTHO_E_ARG;
     int rc;
     DevStatus s = read_status(ctx, ctx->pops[0], &rc);
     if (rc) return rc;
-    return get_float4(ctx, ctx->pops[0]->dev[0].zg, 2ull * s.N, dst);
+    return get_double4(ctx, ctx->pops[0]->dev[0].zg[s.cur], 2ull * s.N, dst);
 }
 
-int clotho_get_phenotypes(clotho_ctx* ctx, float* dst) {
+int clotho_get_phenotypes(clotho_ctx* ctx, double* dst) {
     if (!ctx) return CLOTHO_E_ARG;
     int rc;
     DevStatus s = read_status(ctx, ctx->pops[0], &rc);
     if (rc) return rc;
-    return get_float4(ctx, ctx->pops[0]->dev[0].zi, s.N, dst);
+    return get_double4(ctx, ctx->pops[0]->dev[0].zi, s.N, dst);
 }
 
 int clotho_get_fitness(clotho_ctx* ctx, double* dst) {
@@ -835,8 +846,8 @@ int clotho_stats_compute(clotho_ctx* ctx, clotho_stats* out, uint32_t* sfs, uint
     CK(cudaMemsetAsync(d_counts, 0, counts.size() * 4, ctx->stream));
     if (S && s.W) launch_stats(cfg(ctx), ctx->d_pops[0], 0, d_counts, s.W);
     CK(cudaMemcpyAsync(counts.data(), d_counts, counts.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    std::vector<float> zi((size_t)s.N * 4);
-    if (s.N) CK(cudaMemcpyAsync(zi.data(), D.zi, (size_t)s.N * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<double> zi((size_t)s.N * 4);
+    if (s.N) CK(cudaMemcpyAsync(zi.data(), D.zi, (size_t)s.N * 32, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     cudaFree(d_counts);
     ctx->launches += 1;
@@ -888,6 +899,21 @@ int clotho_kernel_time(clotho_ctx* ctx, double* total_ms, uint32_t* launches, ui
     if (launches) *launches = ctx->prof_launches;
     if (rows) *rows = rw[0];
     if (words) *words = rw[1];
+    return 0;
+}
+
+int clotho_host_alloc(size_t bytes, void** out) {
+    if (!out) return CLOTHO_E_ARG;
+    *out = nullptr;
+    if (cudaMallocHost(out, bytes ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        return CLOTHO_E_NOMEM;
+    }
+    return 0;
+}
+
+int clotho_host_free(void* p) {
+    if (p && cudaFreeHost(p) != cudaSuccess) return CLOTHO_E_CUDA;
     return 0;
 }
 

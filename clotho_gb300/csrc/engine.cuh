@@ -46,6 +46,7 @@ struct DevStatus {
     uint32_t last_M;
     uint32_t pad0;
     double   fit_total;    // sum of fitness of the current population
+    double   fixsum[4];    // effect sums of the alleles fixed in this step's parent
 };
 
 struct PopDev {
@@ -60,8 +61,8 @@ struct PopDev {
     double*   fx_pos;      // [FXcap]
     uint32_t* fx_age;      // [FXcap]
     float*    fx_eff;      // [FXcap * T]
-    float*    zg;          // [Scap * 4] per-genome trait sums
-    float*    zi;          // [Ncap * 4] per-individual phenotypes
+    double*   zg[2];       // [Scap * 4] per-genome trait sums, one array per rows buffer
+    double*   zi;          // [Ncap * 4] per-individual phenotypes
     double*   fit;         // [Ncap]
     double*   cdf;         // [Ncap]
     double*   scan_part;   // [Ncap / 1024 + 2]
@@ -78,8 +79,14 @@ struct PopDev {
     uint32_t* row_off;     // [Scap + 1] exclusive prefix of row_cnt
     uint32_t* row_cur;     // [Scap] scatter cursors (zero between steps)
     uint32_t* row_mut;     // [Mcap] mutation indices grouped by row
+    uint32_t* bcnt;        // [NB + 1] positions per bucket (zero between steps)
+    uint32_t* boff;        // [NB + 1] exclusive prefix of bcnt
+    uint32_t* bcur;        // [NB] bucket scatter cursors (zero between steps)
+    double*   bpos;        // [Acap] positions grouped by bucket
+    uint32_t* rank;        // [Acap] rank of each slot's position among the A slots
     DevStatus* st;
     uint32_t Scap, Ncap, Wcap, Acap, Mcap, EVcap, FXcap, T;
+    uint32_t NB, pad2;     // position buckets (power of two)
     double mu, rho, bias, p_neutral, eff_mean, eff_sigma, fit_param;
     double exp_neg_rho, exp_neg_mu;   // Poisson inversion seeds, computed on the host
     uint64_t seed;
@@ -159,6 +166,13 @@ __device__ inline uint32_t poisson_inv(double u, double lambda, double e) {
 
 __device__ inline uint32_t lane_id() { return threadIdx.x & 31u; }
 
+// Monotone bucket of a position in [0,1) (values outside are clamped).
+__device__ inline uint32_t pos_bucket(double x, uint32_t NB) {
+    const double y = x * (double)NB;
+    if (!(y > 0.0)) return 0u;
+    return y >= (double)(NB - 1u) ? NB - 1u : (uint32_t)y;
+}
+
 }  // namespace clotho
 
 // ---------------------------------------------------------------------------
@@ -187,6 +201,8 @@ void launch_end(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_seed_rows(const LaunchCfg&, const PopDev* pops, uint32_t npops, const uint32_t* thr,
                       uint64_t seed, uint32_t A);
 void launch_stats(const LaunchCfg&, const PopDev* pops, uint32_t p, uint32_t* counts, uint32_t A);
+void launch_ranks(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxNB);
+void launch_uscan_buckets(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxNB);
 
 // fuse flags of k_generation
 constexpr uint32_t kFuseMut = 1u, kFusePheno = 2u, kFuseFs = 4u;

@@ -107,6 +107,8 @@ __global__ void __launch_bounds__(1024) k_fs_finalize(const PopDev* __restrict__
     const uint32_t pA = st->pA, pW = st->pW, pS = 2u * st->pN, M = st->M;
     const uint32_t fx_base = st->fixed_total;
     uint32_t totF = 0, totL = 0;
+    __shared__ double s_fx[32][kMaxTraits];
+    double fsum[kMaxTraits] = {0.0, 0.0, 0.0, 0.0};
     if (pA > 0) {
         // pass 1: totals
         uint32_t cf = 0, cl = 0;
@@ -136,6 +138,7 @@ __global__ void __launch_bounds__(1024) k_fs_finalize(const PopDev* __restrict__
                     const uint32_t slot = w * 64u + (uint32_t)(__ffsll((long long)b) - 1);
                     P.free_list[i] = slot;
                     const uint32_t k = fx_base + i;
+                    for (uint32_t t = 0; t < P.T; ++t) fsum[t] += (double)P.eff[(size_t)slot * P.T + t];
                     if (k < P.FXcap) {  // m_fixed.append / m_fixed_traits.append (:315-324)
                         P.fx_pos[k] = P.pos[slot];
                         P.fx_age[k] = P.age[slot];
@@ -151,7 +154,21 @@ __global__ void __launch_bounds__(1024) k_fs_finalize(const PopDev* __restrict__
             base_l += tl;
         }
     }
+    // effect sum of the fixed alleles (every parent row carries them): the
+    // generation pass subtracts it from the carried per-genome sums
+#pragma unroll
+    for (uint32_t t = 0; t < kMaxTraits; ++t) {
+        double v = fsum[t];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31u) == 0) s_fx[threadIdx.x >> 5][t] = v;
+    }
     __syncthreads();
+    if (threadIdx.x < kMaxTraits) {
+        double v = 0.0;
+        for (int i = 0; i < 32; ++i) v += s_fx[i][threadIdx.x];
+        st->fixsum[threadIdx.x] = v;
+    }
     // reset the accumulators for the child of this step
     for (uint32_t w = threadIdx.x; w < P.Wcap; w += 1024u) {
         P.accF[w] = ~0ull;

@@ -88,16 +88,30 @@ void launch_end(const LaunchCfg& L, const PopDev* pops, uint32_t npops) {
 // Exclusive u32 scan of row_cnt[0..S] into row_off[0..S], chunked, per
 // population.  Also zeroes row_cnt and row_cur for the next step.  When
 // set_M is set, row_off[S] (the total) becomes the step's mutation count.
-__global__ void __launch_bounds__(1024) k_uscan_a(const PopDev* __restrict__ pops, uint32_t npops) {
+struct ScanSel {
+    uint32_t* cnt;
+    uint32_t* off;
+    uint32_t* cur;
+    uint32_t L;      // elements (counts) to scan; off gets L entries
+    uint32_t ncur;   // cursors to zero
+};
+// which == 0: per-row mutation counts; which == 1: position buckets
+__device__ inline ScanSel scan_sel(const PopDev& P, int which) {
+    if (which == 0) return ScanSel{P.row_cnt, P.row_off, P.row_cur, 2u * P.st->N + 1u, 2u * P.st->N};
+    return ScanSel{P.bcnt, P.boff, P.bcur, P.NB + 1u, P.NB};
+}
+
+__global__ void __launch_bounds__(1024) k_uscan_a(const PopDev* __restrict__ pops, uint32_t npops, int which) {
     __shared__ uint32_t s_w[32];
     for (uint32_t p = 0; p < npops; ++p) {
         const PopDev& P = pops[p];
-        const uint32_t L = 2u * P.st->N + 1u;
+        const ScanSel Z = scan_sel(P, which);
+        const uint32_t L = Z.L;
         const uint32_t nch = (L + kScanChunk - 1) / kScanChunk;
         for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x) {
             const uint32_t b = c * kScanChunk + threadIdx.x * 4u;
             uint32_t s = 0;
-            for (uint32_t k = 0; k < 4; ++k) s += (b + k < L) ? P.row_cnt[b + k] : 0u;
+            for (uint32_t k = 0; k < 4; ++k) s += (b + k < L) ? Z.cnt[b + k] : 0u;
             s = warp_incl_u32(s);
             if ((threadIdx.x & 31u) == 31u) s_w[threadIdx.x >> 5] = s;
             __syncthreads();
@@ -111,11 +125,11 @@ __global__ void __launch_bounds__(1024) k_uscan_a(const PopDev* __restrict__ pop
     }
 }
 
-__global__ void k_uscan_b(const PopDev* __restrict__ pops, uint32_t npops) {
+__global__ void k_uscan_b(const PopDev* __restrict__ pops, uint32_t npops, int which) {
     const uint32_t p = blockIdx.x;
     if (p >= npops || threadIdx.x != 0) return;
     const PopDev& P = pops[p];
-    const uint32_t L = 2u * P.st->N + 1u;
+    const uint32_t L = scan_sel(P, which).L;
     const uint32_t nch = (L + kScanChunk - 1) / kScanChunk;
     uint32_t acc = 0;
     for (uint32_t c = 0; c < nch; ++c) {
@@ -125,17 +139,19 @@ __global__ void k_uscan_b(const PopDev* __restrict__ pops, uint32_t npops) {
     }
 }
 
-__global__ void __launch_bounds__(1024) k_uscan_c(const PopDev* __restrict__ pops, uint32_t npops, int set_M) {
+__global__ void __launch_bounds__(1024) k_uscan_c(const PopDev* __restrict__ pops, uint32_t npops, int which,
+                                                  int set_M) {
     __shared__ uint32_t s_w[32];
     for (uint32_t p = 0; p < npops; ++p) {
         const PopDev& P = pops[p];
-        const uint32_t S = 2u * P.st->N, L = S + 1u;
+        const ScanSel Z = scan_sel(P, which);
+        const uint32_t S = Z.ncur, L = Z.L;
         const uint32_t nch = (L + kScanChunk - 1) / kScanChunk;
         for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x) {
             const uint32_t b = c * kScanChunk + threadIdx.x * 4u;
             uint32_t v[4], s = 0;
             for (uint32_t k = 0; k < 4; ++k) {
-                v[k] = (b + k < L) ? P.row_cnt[b + k] : 0u;
+                v[k] = (b + k < L) ? Z.cnt[b + k] : 0u;
                 s += v[k];
             }
             const uint32_t incl = warp_incl_u32(s);
@@ -146,9 +162,9 @@ __global__ void __launch_bounds__(1024) k_uscan_c(const PopDev* __restrict__ pop
             uint32_t run = P.scan_upart[c] + woff + incl - s;
             for (uint32_t k = 0; k < 4; ++k) {
                 if (b + k < L) {
-                    P.row_off[b + k] = run;
-                    P.row_cnt[b + k] = 0u;
-                    if (b + k < S) P.row_cur[b + k] = 0u;
+                    Z.off[b + k] = run;
+                    Z.cnt[b + k] = 0u;
+                    if (b + k < S) Z.cur[b + k] = 0u;
                     if (set_M && b + k == S) {
                         DevStatus* st = P.st;
                         if (run > P.Mcap) { st->err |= kErrMut; run = P.Mcap; }
@@ -162,12 +178,17 @@ __global__ void __launch_bounds__(1024) k_uscan_c(const PopDev* __restrict__ pop
     }
 }
 
-static void launch_uscan(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS, int set_M) {
-    const uint32_t nch = (maxS + 1 + kScanChunk - 1) / kScanChunk;
+static void launch_uscan(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxLen, int which,
+                         int set_M) {
+    const uint32_t nch = (maxLen + 1 + kScanChunk - 1) / kScanChunk;
     const uint32_t g = max(1u, min(nch, (uint32_t)L.num_sms * 2u));
-    k_uscan_a<<<g, 1024, 0, L.stream>>>(pops, npops);
-    k_uscan_b<<<npops, 32, 0, L.stream>>>(pops, npops);
-    k_uscan_c<<<g, 1024, 0, L.stream>>>(pops, npops, set_M);
+    k_uscan_a<<<g, 1024, 0, L.stream>>>(pops, npops, which);
+    k_uscan_b<<<npops, 32, 0, L.stream>>>(pops, npops, which);
+    k_uscan_c<<<g, 1024, 0, L.stream>>>(pops, npops, which, set_M);
+}
+
+void launch_uscan_buckets(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxNB) {
+    launch_uscan(L, pops, npops, maxNB, 1, 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -200,7 +221,7 @@ __global__ void k_csr_scatter(const PopDev* __restrict__ pops, uint32_t npops) {
 void launch_mut_csr_tape(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
     const int g = L.num_sms * 2;
     k_csr_count<<<g, 256, 0, L.stream>>>(pops, npops);
-    launch_uscan(L, pops, npops, maxS, 0);
+    launch_uscan(L, pops, npops, maxS, 0, 0);
     k_csr_scatter<<<g, 256, 0, L.stream>>>(pops, npops);
 }
 
@@ -222,7 +243,7 @@ __global__ void k_philox_rowcnt(const PopDev* __restrict__ pops, uint32_t npops)
 }
 void launch_mut_counts_philox(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
     k_philox_rowcnt<<<L.num_sms * 4, 256, 0, L.stream>>>(pops, npops);
-    launch_uscan(L, pops, npops, maxS, 1);
+    launch_uscan(L, pops, npops, maxS, 0, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -347,21 +368,17 @@ __global__ void k_individuals(const PopDev* __restrict__ pops, uint32_t npops) {
         const bool neutral = st->nz_eff == 0;
         if (blockIdx.x == 0 && threadIdx.x == 0) st->all_neutral = neutral ? 1u : 0u;
         const double sig = sqrt(4.0 * (double)N * P.mu);  // normal/quadratic generators
+        const double* zg = P.zg[st->cur];
         for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
-            float4 z;
-            if (neutral) {
-                z = make_float4(1.f, 1.f, 1.f, 1.f);
-            } else {
-                const float4 a = reinterpret_cast<const float4*>(P.zg)[2u * i];
-                const float4 b = reinterpret_cast<const float4*>(P.zg)[2u * i + 1u];
-                z = make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+            double z[4];
+            for (uint32_t t = 0; t < 4; ++t) {
+                if (t >= T) z[t] = 0.0;
+                else if (neutral) z[t] = 1.0;
+                else z[t] = zg[(size_t)(2u * i) * 4u + t] + zg[(size_t)(2u * i + 1u) * 4u + t];
+                P.zi[(size_t)i * 4u + t] = z[t];
             }
-            if (T < 4) z.w = 0.f;
-            if (T < 3) z.z = 0.f;
-            if (T < 2) z.y = 0.f;
-            reinterpret_cast<float4*>(P.zi)[i] = z;
             double f = 1.0;
-            const double z0 = (double)z.x;
+            const double z0 = z[0];
             switch (P.fitness) {
                 case 1: {  // gaussian (normal_fitness_metric.cpp:25-31)
                     const double coeff = (1.0 / sig) * 0.398942280401432677939946059934;
@@ -374,7 +391,7 @@ __global__ void k_individuals(const PopDev* __restrict__ pops, uint32_t npops) {
                     f = (r >= 1.0) ? 0.0 : 1.0 - r;
                 } break;
                 case 3: {  // gaussian_vs
-                    const double ss = (double)z.x * z.x + (double)z.y * z.y + (double)z.z * z.z + (double)z.w * z.w;
+                    const double ss = z[0] * z[0] + z[1] * z[1] + z[2] * z[2] + z[3] * z[3];
                     f = exp(-ss / (2.0 * P.fit_param));
                 } break;
                 default: f = 1.0;

@@ -190,8 +190,10 @@ int  clotho_get_alleles(clotho_ctx *ctx, double *pos, uint32_t *age, float *eff)
 int  clotho_get_fixed(clotho_ctx *ctx, double *pos, uint32_t *age, float *eff);
 /* Free list of the last analysis [free_count]: fixed ascending, then lost ascending. */
 int  clotho_get_free(clotho_ctx *ctx, uint32_t *dst);
-int  clotho_get_genome_traits(clotho_ctx *ctx, float *dst);   /* [2N*T] */
-int  clotho_get_phenotypes(clotho_ctx *ctx, float *dst);      /* [N*T]  */
+/* Per-genome trait sums [2N*T] and individual phenotypes [N*T]: FP32 partial
+ * sums of FP32 effects, accumulated per genome in FP64. */
+int  clotho_get_genome_traits(clotho_ctx *ctx, double *dst);
+int  clotho_get_phenotypes(clotho_ctx *ctx, double *dst);
 int  clotho_get_fitness(clotho_ctx *ctx, double *dst);        /* [N]    */
 int  clotho_get_pairs(clotho_ctx *ctx, uint32_t *dst);        /* [2N] of the last generation */
 
@@ -218,6 +220,12 @@ int  clotho_timer_begin(clotho_ctx *ctx);
 int  clotho_timer_end(clotho_ctx *ctx, double *ms);
 /* Count of kernels this context launched since creation. */
 uint64_t clotho_launch_count(const clotho_ctx *ctx);
+
+/* ---- pinned host memory for tape staging (page-locked, so host->device
+ * copies run at link speed).  No reference counterpart: the reference keeps
+ * its event pool in ordinary host memory (batch_crossover_mtwe.hpp:80-84). */
+int  clotho_host_alloc(size_t bytes, void **out);
+int  clotho_host_free(void *p);
 
 #ifdef __cplusplus
 }

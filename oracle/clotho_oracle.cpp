@@ -439,11 +439,13 @@ struct Engine {
         init(N);
         child->grow(N, A, prm.T);
         std::fill(child->g.begin(), child->g.end(), 0);
-        for (uint32_t r = 0; r < child->rows; ++r) {
-            uint64_t* row = child->row(r);
-            for (uint32_t a = 0; a < A; ++a)
-                if (seed_hash(s, r, a) < thr[a]) row[a / 64] |= 1ull << (a % 64);
-        }
+        partitioned(pool, child->rows, [&](unsigned lo, unsigned hi) {
+            for (uint32_t r = lo; r < hi; ++r) {
+                uint64_t* row = child->row(r);
+                for (uint32_t a = 0; a < A; ++a)
+                    if (seed_hash(s, r, a) < thr[a]) row[a / 64] |= 1ull << (a % 64);
+            }
+        });
         alleles.pos.assign(pos, pos + A);
         alleles.age.assign(A, 0);
         traits.w.assign(A * (size_t)prm.T, 0.0);
