@@ -55,7 +55,7 @@ std::vector<size_t> sizes_of(const Geometry& g) {
     return {
         S * W * 8, S * W * 8,            // rows[0], rows[1]
         W * 8, W * 8, W * 8,             // fixmask, accF, accV
-        A * 4, A * 8, A * 4, A * T * 4,  // free_list, pos, age, eff
+        A * 4, A * 8, A * 4, A * 16,     // free_list, pos, age, eff (traits padded to 4)
         g.FXcap * 8ull, g.FXcap * 4ull, g.FXcap * T * 4ull,
         S * 32, S * 32, N * 32, N * 8, N * 8,    // zg[0], zg[1], zi, fit, cdf
         (N / 1024 + 8) * 8, ((S > g.NB ? S : g.NB) / 1024 + 8) * 4ull,
@@ -93,7 +93,7 @@ struct clotho_ctx {
     cudaGraphExec_t graph = nullptr;
     uint32_t graph_N = 0;
     bool in_step = false;
-    uint32_t maxW = 0, maxS = 0, maxN = 0, maxNB = 0;
+    uint32_t maxW = 0, maxS = 0, maxN = 0, maxNB = 0, maxA = 0;
 };
 
 namespace {
@@ -208,6 +208,7 @@ int sync_pop_arrays(clotho_ctx* ctx) {
         ctx->maxS = std::max(ctx->maxS, p->dev[0].Scap);
         ctx->maxN = std::max(ctx->maxN, p->dev[0].Ncap);
         ctx->maxNB = std::max(ctx->maxNB, p->dev[0].NB);
+        ctx->maxA = std::max(ctx->maxA, p->dev[0].Acap);
     }
     if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
     CK(cudaStreamSynchronize(ctx->stream));
@@ -254,7 +255,7 @@ int prof_collect(clotho_ctx* ctx) {
 
 void launch_gen(clotho_ctx* ctx, const PopDev* pops, uint32_t npops, uint32_t fuse) {
     prof_begin(ctx);
-    launch_generation(cfg(ctx), pops, npops, ctx->d_ctl, ctx->maxW, fuse, ctx->profiling ? 1 : 0);
+    launch_generation(cfg(ctx), pops, npops, ctx->d_ctl, ctx->maxW, ctx->maxA, fuse, ctx->profiling ? 1 : 0);
     prof_end(ctx);
     ctx->launches += 1;
 }
@@ -447,7 +448,7 @@ int clotho_init(clotho_ctx* ctx, uint32_t N0) {
     std::vector<double> ones(N0, 1.0);
     if (N0) CK(cudaMemcpyAsync(D.fit, ones.data(), N0 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemsetAsync(D.pos, 0, (size_t)D.Acap * 8, ctx->stream));
-    CK(cudaMemsetAsync(D.eff, 0, (size_t)D.Acap * D.T * 4, ctx->stream));
+    CK(cudaMemsetAsync(D.eff, 0, (size_t)D.Acap * 16, ctx->stream));
     CK(cudaMemsetAsync(D.age, 0, (size_t)D.Acap * 4, ctx->stream));
     CK(cudaMemsetAsync(D.accF, 0xff, (size_t)D.Wcap * 8, ctx->stream));
     CK(cudaMemsetAsync(D.accV, 0, (size_t)D.Wcap * 8, ctx->stream));
@@ -485,7 +486,11 @@ int clotho_seed_population(clotho_ctx* ctx, uint32_t N, uint32_t A, const double
     CK(cudaMalloc(&d_thr, std::max<size_t>(4, (size_t)A * 4)));
     if (A) {
         CK(cudaMemcpyAsync(D.pos, pos, (size_t)A * 8, cudaMemcpyHostToDevice, ctx->stream));
-        CK(cudaMemcpyAsync(D.eff, eff, (size_t)A * T * 4, cudaMemcpyHostToDevice, ctx->stream));
+        std::vector<float> pad((size_t)A * 4, 0.0f);
+        for (size_t i = 0; i < A; ++i)
+            for (uint32_t t = 0; t < T; ++t) pad[i * 4 + t] = eff[i * T + t];
+        CK(cudaMemcpyAsync(D.eff, pad.data(), (size_t)A * 16, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
         CK(cudaMemcpyAsync(d_thr, thr, (size_t)A * 4, cudaMemcpyHostToDevice, ctx->stream));
     }
     LaunchCfg L = cfg(ctx);
@@ -751,8 +756,12 @@ int clotho_get_alleles(clotho_ctx* ctx, double* pos, uint32_t* age, float* eff) 
     const PopDev& D = p->dev[0];
     if (pos && s.A) CK(cudaMemcpyAsync(pos, D.pos, (size_t)s.A * 8, cudaMemcpyDeviceToHost, ctx->stream));
     if (age && s.A) CK(cudaMemcpyAsync(age, D.age, (size_t)s.A * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    if (eff && s.A) CK(cudaMemcpyAsync(eff, D.eff, (size_t)s.A * D.T * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<float> pad((size_t)s.A * 4);
+    if (eff && s.A) CK(cudaMemcpyAsync(pad.data(), D.eff, (size_t)s.A * 16, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (eff)
+        for (size_t i = 0; i < s.A; ++i)
+            for (uint32_t t = 0; t < D.T; ++t) eff[i * D.T + t] = pad[i * 4 + t];
     return 0;
 }
 

@@ -12,8 +12,8 @@
 namespace clotho {
 
 constexpr uint32_t kMaxTraits = 4;
-constexpr uint32_t kGenThreads = 256;      // 8 warps per CTA in the generation kernel
-constexpr uint32_t kRowsPerItem = 64;      // child rows per scheduling item
+constexpr uint32_t kGenThreads = 512;      // 16 warps per CTA, one CTA per SM, in the generation kernel
+constexpr uint32_t kRowsPerItem = 512;     // child rows per scheduling item
 constexpr uint32_t kMaxEvReg = 16;         // events held in registers
 constexpr uint32_t kMaxEvDevice = 128;     // device-drawn events per gamete
 constexpr uint32_t kMaxMutReg = 32;        // mutations per row held in registers
@@ -57,7 +57,7 @@ struct PopDev {
     uint32_t* free_list;   // [Acap]
     double*   pos;         // [Acap] allele positions (non-negative: ordered as u64)
     uint32_t* age;         // [Acap]
-    float*    eff;         // [Acap * T]
+    float*    eff;         // [Acap * 4] effects, traits padded to 4 (unused traits 0)
     double*   fx_pos;      // [FXcap]
     uint32_t* fx_age;      // [FXcap]
     float*    fx_eff;      // [FXcap * T]
@@ -192,7 +192,7 @@ void launch_mut_counts_philox(const LaunchCfg&, const PopDev* pops, uint32_t npo
 void launch_mut_resolve(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_select_philox(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_generation(const LaunchCfg&, const PopDev* pops, uint32_t npops, WorkCtl* ctl,
-                       uint32_t maxW, uint32_t fuse, int profile);
+                       uint32_t maxW, uint32_t maxA, uint32_t fuse, int profile);
 void launch_mut_scatter(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_phenotype(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_individuals(const LaunchCfg&, const PopDev* pops, uint32_t npops);

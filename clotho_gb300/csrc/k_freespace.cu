@@ -138,11 +138,11 @@ __global__ void __launch_bounds__(1024) k_fs_finalize(const PopDev* __restrict__
                     const uint32_t slot = w * 64u + (uint32_t)(__ffsll((long long)b) - 1);
                     P.free_list[i] = slot;
                     const uint32_t k = fx_base + i;
-                    for (uint32_t t = 0; t < P.T; ++t) fsum[t] += (double)P.eff[(size_t)slot * P.T + t];
+                    for (uint32_t t = 0; t < P.T; ++t) fsum[t] += (double)P.eff[(size_t)slot * 4u + t];
                     if (k < P.FXcap) {  // m_fixed.append / m_fixed_traits.append (:315-324)
                         P.fx_pos[k] = P.pos[slot];
                         P.fx_age[k] = P.age[slot];
-                        for (uint32_t t = 0; t < P.T; ++t) P.fx_eff[(size_t)k * P.T + t] = P.eff[(size_t)slot * P.T + t];
+                        for (uint32_t t = 0; t < P.T; ++t) P.fx_eff[(size_t)k * P.T + t] = P.eff[(size_t)slot * 4u + t];
                     }
                     ++i;
                 }

@@ -25,9 +25,12 @@
 //   free space AND/OR of the finished words, the next generation's
 //              FreeSpaceAnalyzerMT input (free_space_task_population_space_row_interlaced.hpp:51-72).
 //
-// Rows are 64-word chunks, two words (one 128-bit load) per lane; the next
-// chunk's parent words are loaded while the current one is processed.  The
-// kernel is persistent: CTAs take 64-row items from a device counter.
+// Rows are 64-word chunks, two words (one 128-bit load) per lane; parent words
+// are loaded two chunks ahead of use.  The het-bit walk runs the lane's four
+// 32-bit halves as independent chains (branch-free steps) so shared-memory
+// and ALU latencies overlap.  The kernel is persistent: one CTA per SM takes
+// 512-row items from a device counter and its warps claim rows one at a time,
+// so warps never wait on each other inside an item.
 #include "engine.cuh"
 
 namespace clotho {
@@ -35,80 +38,99 @@ namespace clotho {
 namespace {
 
 constexpr uint32_t kWarps = kGenThreads / 32;
-constexpr uint32_t kMaxIv = 8;          // rank intervals held in registers (E <= 16)
 constexpr uint32_t kMaxIvSmem = 64;     // rank intervals in shared memory (E <= 128)
 
-struct Intervals {
+constexpr uint32_t kMaxIv = 8;          // rank intervals held in registers (E <= 16)
+
+// Sorted breakpoint thresholds of one gamete as half-open rank intervals:
+// a het bit switches strand iff its slot rank lies in one of them.
+struct RowXo {
     uint32_t a[kMaxIv];   // interval start (rank)
     uint32_t l[kMaxIv];   // length; 0 = empty
+    const uint2* iv;      // the same intervals in shared memory (any count)
+    uint32_t niv;
 };
 
 template <int NI>
-__device__ __forceinline__ bool in_iv(uint32_t r, const Intervals& iv) {
+__device__ __forceinline__ bool in_iv(uint32_t r, const RowXo& X) {
     bool s = false;
+    if (NI > 0) {
 #pragma unroll
-    for (int k = 0; k < NI; ++k) s |= (r - iv.a[k]) < iv.l[k];
-    return s;
-}
-
-__device__ __forceinline__ bool in_iv_far(uint32_t r, const uint2* iv, uint32_t n) {
-    bool s = false;
-    for (uint32_t k = 0; k < n; ++k) s |= (r - iv[k].x) < iv[k].y;
-    return s;
-}
-
-// Parity mask of one 32-bit half: bits of h whose slot rank is inside an interval.
-template <int NI>
-__device__ __forceinline__ uint32_t sw_mask32(uint32_t h, uint32_t base, const uint32_t* __restrict__ rank,
-                                              const Intervals& iv, const uint2* far, uint32_t nfar) {
-    uint32_t m = 0;
-    while (h) {
-        const uint32_t j = __ffs(h) - 1u;
-        h &= h - 1u;
-        const uint32_t r = __ldg(rank + base + j);
-        bool s;
-        if (NI > 0) s = in_iv<NI>(r, iv);
-        else s = in_iv_far(r, far, nfar);
-        m |= (uint32_t)s << j;
+        for (int k = 0; k < NI; ++k) s |= (r - X.a[k]) < X.l[k];
+    } else {
+        for (uint32_t k = 0; k < X.niv; ++k) s |= (r - X.iv[k].x) < X.iv[k].y;
     }
-    return m;
+    return s;
+}
+
+template <bool SR>
+__device__ __forceinline__ uint32_t slot_rank(uint32_t s, const uint16_t* srank, const uint32_t* __restrict__ grank) {
+    return SR ? (uint32_t)srank[s] : __ldg(grank + s);
+}
+
+// One branch-free step of a het-bit chain: classify the lowest bit of h.
+template <int NI, bool SR>
+__device__ __forceinline__ void xo_step(uint32_t& h, uint32_t& m, uint32_t base, const uint16_t* srank,
+                                        const uint32_t* __restrict__ grank, const RowXo& X) {
+    const bool nz = h != 0u;
+    const uint32_t j = nz ? (uint32_t)(__ffs(h) - 1) : 0u;
+    h &= h - 1u;
+    const uint32_t r = slot_rank<SR>(base + j, srank, grank);
+    const bool s = nz && in_iv<NI>(r, X);
+    m |= (uint32_t)s << j;
+}
+
+// Switched-strand masks of the lane's two words: four interleaved 32-bit chains.
+template <int NI, bool SR>
+__device__ __forceinline__ void classify(uint64_t h0, uint64_t h1, uint32_t s0, const uint16_t* srank,
+                                         const uint32_t* __restrict__ grank, const RowXo& X, uint64_t& m0,
+                                         uint64_t& m1) {
+    uint32_t a = (uint32_t)h0, b = (uint32_t)(h0 >> 32), c = (uint32_t)h1, d = (uint32_t)(h1 >> 32);
+    uint32_t ma = 0, mb = 0, mc = 0, md = 0;
+    while (a | b | c | d) {
+        xo_step<NI, SR>(a, ma, s0, srank, grank, X);
+        xo_step<NI, SR>(b, mb, s0 + 32u, srank, grank, X);
+        xo_step<NI, SR>(c, mc, s0 + 64u, srank, grank, X);
+        xo_step<NI, SR>(d, md, s0 + 96u, srank, grank, X);
+    }
+    m0 = (uint64_t)ma | ((uint64_t)mb << 32);
+    m1 = (uint64_t)mc | ((uint64_t)md << 32);
 }
 
 // Bits of h whose slot position is >= an odd number of the events (direct
 // double compares against the event list; used only for very long lists).
-__device__ __forceinline__ uint32_t sw_mask32_events(uint32_t h, uint32_t base, const double* __restrict__ pos,
-                                                     const double* __restrict__ ev, uint32_t E) {
-    uint32_t m = 0;
+__device__ __forceinline__ uint64_t sw_mask_events(uint64_t h, uint32_t base, const double* __restrict__ pos,
+                                                   const double* __restrict__ ev, uint32_t E) {
+    uint64_t m = 0;
     while (h) {
-        const uint32_t j = __ffs(h) - 1u;
-        h &= h - 1u;
+        const uint32_t j = (uint32_t)(__ffsll((long long)h) - 1);
+        h &= h - 1ull;
         const double p = __ldg(pos + base + j);
         uint32_t c = 0;
         for (uint32_t k = 0; k < E; ++k) c += (__ldg(ev + k) <= p) ? 1u : 0u;
-        m |= (c & 1u) << j;
+        m |= (uint64_t)(c & 1u) << j;
     }
     return m;
 }
 
-__device__ __forceinline__ void acc_effects(uint64_t x, uint32_t base, const float* __restrict__ eff, uint32_t T,
-                                            float sign, float (&d)[kMaxTraits]) {
-    if (T == 4) {
-        while (x) {
-            const uint32_t j = (uint32_t)(__ffsll((long long)x) - 1);
-            x &= x - 1ull;
-            const float4 e = __ldg(reinterpret_cast<const float4*>(eff) + base + j);
-            d[0] = fmaf(sign, e.x, d[0]); d[1] = fmaf(sign, e.y, d[1]);
-            d[2] = fmaf(sign, e.z, d[2]); d[3] = fmaf(sign, e.w, d[3]);
-        }
-    } else {
-        while (x) {
-            const uint32_t j = (uint32_t)(__ffsll((long long)x) - 1);
-            x &= x - 1ull;
-            const float* e = eff + (size_t)(base + j) * T;
-#pragma unroll
-            for (uint32_t t = 0; t < kMaxTraits; ++t)
-                if (t < T) d[t] = fmaf(sign, __ldg(e + t), d[t]);
-        }
+// d += (+1 if the bottom strand brings the allele, -1 if it drops it) * eff
+// over the switched bits of the lane's two words; two chains, two loads in flight.
+__device__ __forceinline__ void switched_effects(uint64_t x0, uint64_t x1, uint64_t b0, uint64_t b1, uint32_t s0,
+                                                 const float4* __restrict__ eff4, float (&d)[kMaxTraits]) {
+    while (x0 | x1) {
+        const bool n0 = x0 != 0ull, n1 = x1 != 0ull;
+        const uint32_t j0 = n0 ? (uint32_t)(__ffsll((long long)x0) - 1) : 0u;
+        const uint32_t j1 = n1 ? (uint32_t)(__ffsll((long long)x1) - 1) : 0u;
+        x0 &= x0 - 1ull;
+        x1 &= x1 - 1ull;
+        const float4 e0 = __ldg(eff4 + s0 + j0);
+        const float4 e1 = __ldg(eff4 + s0 + 64u + j1);
+        const float g0 = n0 ? (((b0 >> j0) & 1ull) ? 1.0f : -1.0f) : 0.0f;
+        const float g1 = n1 ? (((b1 >> j1) & 1ull) ? 1.0f : -1.0f) : 0.0f;
+        d[0] = fmaf(g0, e0.x, fmaf(g1, e1.x, d[0]));
+        d[1] = fmaf(g0, e0.y, fmaf(g1, e1.y, d[1]));
+        d[2] = fmaf(g0, e0.z, fmaf(g1, e1.z, d[2]));
+        d[3] = fmaf(g0, e0.w, fmaf(g1, e1.w, d[3]));
     }
 }
 
@@ -122,29 +144,7 @@ __device__ __forceinline__ uint32_t threshold_rank(const PopDev& P, double e) {
 }
 
 // Per-row crossover mode
-enum XoKind : int { kXoCopy = 0, kXoReg2 = 2, kXoReg4 = 4, kXoReg8 = 8, kXoSmem = -1, kXoEvents = -2 };
-
-template <int NI>
-__device__ __forceinline__ void chunk_xover(uint64_t& x0, uint64_t& x1, uint64_t t0, uint64_t t1, uint64_t b0,
-                                            uint64_t b1, uint32_t w, const PopDev& P, const Intervals& iv,
-                                            const uint2* far, uint32_t nfar, const double* evg, uint32_t E,
-                                            uint64_t& m0, uint64_t& m1) {
-    const uint64_t h0 = t0 ^ b0, h1 = t1 ^ b1;
-    const uint32_t s0 = w * 64u, s1 = s0 + 64u;
-    if (NI >= -1) {
-        m0 = (uint64_t)sw_mask32<NI>((uint32_t)h0, s0, P.rank, iv, far, nfar) |
-             ((uint64_t)sw_mask32<NI>((uint32_t)(h0 >> 32), s0 + 32u, P.rank, iv, far, nfar) << 32);
-        m1 = (uint64_t)sw_mask32<NI>((uint32_t)h1, s1, P.rank, iv, far, nfar) |
-             ((uint64_t)sw_mask32<NI>((uint32_t)(h1 >> 32), s1 + 32u, P.rank, iv, far, nfar) << 32);
-    } else {
-        m0 = (uint64_t)sw_mask32_events((uint32_t)h0, s0, P.pos, evg, E) |
-             ((uint64_t)sw_mask32_events((uint32_t)(h0 >> 32), s0 + 32u, P.pos, evg, E) << 32);
-        m1 = (uint64_t)sw_mask32_events((uint32_t)h1, s1, P.pos, evg, E) |
-             ((uint64_t)sw_mask32_events((uint32_t)(h1 >> 32), s1 + 32u, P.pos, evg, E) << 32);
-    }
-    x0 = (t0 & ~m0) | (b0 & m0);
-    x1 = (t1 & ~m1) | (b1 & m1);
-}
+enum XoKind : int { kXoCopy = 0, kXoIv4 = 4, kXoIv8 = 8, kXoFar = -1, kXoEvents = -2 };
 
 struct RowArgs {
     const uint64_t* top;
@@ -157,29 +157,43 @@ struct RowArgs {
     bool philox;
 };
 
-template <int NI>
-__device__ __forceinline__ void row_body(const PopDev& P, const DevStatus& st, const RowArgs& R, const Intervals& iv,
-                                         const uint2* far, uint32_t nfar, bool do_mut, bool do_ph, bool do_fs,
-                                         uint64_t* sF, uint64_t* sV, float (&d)[kMaxTraits]) {
-    const uint32_t lane = threadIdx.x & 31u;
-    const bool xo = (NI != 0);
-    uint32_t w = 2u * lane;
-    // prefetch of chunk 0
-    ulonglong2 tt = make_ulonglong2(0, 0), bb = make_ulonglong2(0, 0), fm = make_ulonglong2(0, 0);
+__device__ __forceinline__ void load_pair(ulonglong2& t, ulonglong2& b, const RowArgs& R, uint32_t w, bool xo) {
     if (w < R.Wp) {
-        tt = __ldg(reinterpret_cast<const ulonglong2*>(R.top + w));
-        if (xo) bb = __ldg(reinterpret_cast<const ulonglong2*>(R.bot + w));
-        fm = *reinterpret_cast<const ulonglong2*>(P.fixmask + w);
+        t = __ldg(reinterpret_cast<const ulonglong2*>(R.top + w));
+        b = xo ? __ldg(reinterpret_cast<const ulonglong2*>(R.bot + w)) : make_ulonglong2(0, 0);
+    } else {
+        t = make_ulonglong2(0, 0);
+        b = make_ulonglong2(0, 0);
     }
+}
+
+// AND/OR into the CTA accumulators; the atomic is issued only when it would
+// change the word (both operations are monotone, so skipping is exact).
+__device__ __forceinline__ void fold_fs(uint64_t* sF, uint64_t* sV, uint32_t w, uint64_t x0, uint64_t x1) {
+    const ulonglong2 f = *reinterpret_cast<const ulonglong2*>(sF + w);
+    const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(sV + w);
+    if (f.x & ~x0) atomicAnd((unsigned long long*)&sF[w], (unsigned long long)x0);
+    if (f.y & ~x1) atomicAnd((unsigned long long*)&sF[w + 1u], (unsigned long long)x1);
+    if (x0 & ~v.x) atomicOr((unsigned long long*)&sV[w], (unsigned long long)x0);
+    if (x1 & ~v.y) atomicOr((unsigned long long*)&sV[w + 1u], (unsigned long long)x1);
+}
+
+template <int KIND, bool SR>
+__device__ __forceinline__ void row_body(const PopDev& P, const DevStatus& st, const RowArgs& R,
+                                         const uint16_t* srank, const uint64_t* sfix, const RowXo& X, bool do_mut,
+                                         bool do_ph, bool do_fs, uint64_t* sF, uint64_t* sV,
+                                         float (&d)[kMaxTraits]) {
+    const uint32_t lane = threadIdx.x & 31u;
+    constexpr bool xo = (KIND != kXoCopy);
+    const float4* eff4 = reinterpret_cast<const float4*>(P.eff);
+    // two chunks of parent words in flight ahead of the one being processed
+    ulonglong2 t_a, b_a, t_b, b_b;
+    load_pair(t_a, b_a, R, 2u * lane, xo);
+    load_pair(t_b, b_b, R, 2u * lane + 64u, xo);
     for (uint32_t w0 = 0; w0 < R.Wc; w0 += 64u) {
-        w = w0 + 2u * lane;
-        const uint32_t wn = w + 64u;
-        ulonglong2 tn = make_ulonglong2(0, 0), bn = make_ulonglong2(0, 0), fn = make_ulonglong2(0, 0);
-        if (wn < R.Wp) {
-            tn = __ldg(reinterpret_cast<const ulonglong2*>(R.top + wn));
-            if (xo) bn = __ldg(reinterpret_cast<const ulonglong2*>(R.bot + wn));
-            fn = *reinterpret_cast<const ulonglong2*>(P.fixmask + wn);
-        }
+        const uint32_t w = w0 + 2u * lane;
+        ulonglong2 t_c, b_c;
+        load_pair(t_c, b_c, R, w + 128u, xo);
         // XOR masks of this lane's two words from the row's new alleles
         uint64_t mx0 = 0, mx1 = 0;
         if (do_mut && R.mc) {
@@ -202,58 +216,227 @@ __device__ __forceinline__ void row_body(const PopDev& P, const DevStatus& st, c
             }
         }
         if (w < R.Wc) {
-            const uint64_t t0 = tt.x & ~fm.x, t1 = tt.y & ~fm.y;
+            ulonglong2 fm = make_ulonglong2(0, 0);
+            if (w < R.Wp) fm = *reinterpret_cast<const ulonglong2*>(sfix + w);
+            const uint64_t t0 = t_a.x & ~fm.x, t1 = t_a.y & ~fm.y;
             uint64_t x0 = t0, x1 = t1;
             if (xo) {
-                const uint64_t b0 = bb.x & ~fm.x, b1 = bb.y & ~fm.y;
+                const uint64_t b0 = b_a.x & ~fm.x, b1 = b_a.y & ~fm.y;
                 uint64_t m0, m1;
-                chunk_xover<NI>(x0, x1, t0, t1, b0, b1, w, P, iv, far, nfar, R.evg, R.E, m0, m1);
-                if (do_ph) {
-                    // switched bits: +w where the bottom strand brings the allele, -w where it drops it
-                    acc_effects(m0 & b0, w * 64u, P.eff, P.T, 1.0f, d);
-                    acc_effects(m0 & t0, w * 64u, P.eff, P.T, -1.0f, d);
-                    acc_effects(m1 & b1, (w + 1u) * 64u, P.eff, P.T, 1.0f, d);
-                    acc_effects(m1 & t1, (w + 1u) * 64u, P.eff, P.T, -1.0f, d);
+                if (KIND != kXoEvents) {
+                    classify<(KIND > 0 ? KIND : 0), SR>(t0 ^ b0, t1 ^ b1, w * 64u, srank, P.rank, X, m0, m1);
+                } else {
+                    m0 = sw_mask_events(t0 ^ b0, w * 64u, P.pos, R.evg, R.E);
+                    m1 = sw_mask_events(t1 ^ b1, w * 64u + 64u, P.pos, R.evg, R.E);
                 }
+                x0 = (t0 & ~m0) | (b0 & m0);
+                x1 = (t1 & ~m1) | (b1 & m1);
+                if (do_ph) switched_effects(m0, m1, b0, b1, w * 64u, eff4, d);
             }
             x0 ^= mx0;
             x1 ^= mx1;
             *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(x0, x1);
-            if (do_fs) {
-                atomicAnd((unsigned long long*)&sF[w], (unsigned long long)x0);
-                atomicAnd((unsigned long long*)&sF[w + 1u], (unsigned long long)x1);
-                atomicOr((unsigned long long*)&sV[w], (unsigned long long)x0);
-                atomicOr((unsigned long long*)&sV[w + 1u], (unsigned long long)x1);
+            if (do_fs) fold_fs(sF, sV, w, x0, x1);
+        }
+        t_a = t_b; b_a = b_b;
+        t_b = t_c; b_b = b_c;
+    }
+}
+
+// One offspring row, the whole warp.
+template <bool SR>
+__device__ __forceinline__ void gen_row(const PopDev& P, const DevStatus& st, uint32_t g, const uint16_t* srank,
+                                        const uint64_t* sfix, uint2* s_iv, uint32_t* s_thr, bool do_mut,
+                                        bool do_ph, bool do_fs, uint64_t* sF, uint64_t* sV) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t* prow = P.rows[st.cur ^ 1u];
+    uint64_t* crow = P.rows[st.cur];
+    const bool q1 = (P.flags & 1u) != 0;
+    const bool philox = P.mode == kModePhilox;
+    // ---- parent strands and the strand-swap bit of gamete g
+    uint32_t pind = P.pairs[g];
+    if (pind >= st.pN) {
+        if (lane == 0) atomicOr(&P.st->err, kErrParent);
+        pind = 0;
+    }
+    const uint32_t h = g & 1u;
+    bool swap;
+    uint32_t E;
+    const double* evg = nullptr;
+    if (philox) {
+        const U4 x = philox4x32(g, 0u, st.gen, kStreamGamete, P.seed);
+        E = poisson_inv(u01(x.x, x.y), P.rho, P.exp_neg_rho);
+        swap = u01(x.z, x.w) < P.bias;
+        if (q1 && h) E = 0;
+        if (E > kMaxEvDevice) {
+            if (lane == 0) atomicOr(&P.st->err, kErrEvents);
+            E = kMaxEvDevice;
+        }
+    } else {
+        swap = P.swap[g] != 0;
+        const uint32_t e0 = P.ev_off[g], e1 = P.ev_off[g + 1u];
+        E = (q1 && h) ? 0u : e1 - e0;
+        evg = P.ev_pos + e0;
+    }
+    const uint32_t topr = 2u * pind + (swap ? 1u : 0u);
+    RowArgs R;
+    R.top = prow + (size_t)topr * P.Wcap;
+    R.bot = prow + (size_t)(topr ^ 1u) * P.Wcap;
+    R.out = crow + (size_t)g * P.Wcap;
+    R.Wc = st.W;
+    R.Wp = st.pW;
+    R.E = E;
+    R.evg = evg;
+    R.philox = philox;
+
+    // ---- breakpoints -> sorted rank thresholds -> intervals
+    RowXo X;
+#pragma unroll
+    for (uint32_t k = 0; k < kMaxIv; ++k) { X.a[k] = 0; X.l[k] = 0; }
+    X.iv = s_iv;
+    X.niv = 0;
+    int kind = kXoCopy;
+    if (E > 0 && E <= kMaxEvDevice) {
+        for (uint32_t k = lane; k < E; k += 32u) {
+            double e;
+            if (philox) {
+                const U4 a = philox4x32(g, 1u + (k >> 1), st.gen, kStreamGamete, P.seed);
+                e = (k & 1u) ? u01(a.z, a.w) : u01(a.x, a.y);
+            } else {
+                e = __ldg(evg + k);
+            }
+            s_thr[k] = threshold_rank(P, e);
+        }
+        __syncwarp();
+        // stable rank sort of the thresholds
+        uint32_t mine[4], posn[4];
+#pragma unroll
+        for (uint32_t q = 0; q < 4; ++q) {
+            const uint32_t k = lane + 32u * q;
+            mine[q] = (k < E) ? s_thr[k] : 0u;
+            posn[q] = 0;
+        }
+        for (uint32_t j = 0; j < E; ++j) {
+            const uint32_t tj = s_thr[j];
+#pragma unroll
+            for (uint32_t q = 0; q < 4; ++q) {
+                const uint32_t k = lane + 32u * q;
+                posn[q] += (tj < mine[q] || (tj == mine[q] && j < k)) ? 1u : 0u;
             }
         }
-        tt = tn;
-        bb = bn;
-        fm = fn;
+        __syncwarp();
+#pragma unroll
+        for (uint32_t q = 0; q < 4; ++q) {
+            const uint32_t k = lane + 32u * q;
+            if (k < E) s_thr[posn[q]] = mine[q];
+        }
+        __syncwarp();
+        const uint32_t NI = (E + 1u) >> 1;
+        for (uint32_t i = lane; i < NI; i += 32u) {
+            const uint32_t a = s_thr[2u * i];
+            uint32_t l;
+            if (2u * i + 1u < E) l = s_thr[2u * i + 1u] - a;
+            else l = a ? (uint32_t)(0x100000000ull - a) : 0xffffffffu;
+            s_iv[i] = make_uint2(a, l);
+        }
+        __syncwarp();
+        X.niv = NI;
+        if (NI <= kMaxIv) {
+#pragma unroll
+            for (uint32_t k = 0; k < kMaxIv; ++k) {
+                if (k < NI) { X.a[k] = s_iv[k].x; X.l[k] = s_iv[k].y; }
+            }
+            kind = NI <= 4 ? kXoIv4 : kXoIv8;
+        } else {
+            kind = kXoFar;
+        }
+    } else if (E > kMaxEvDevice) {
+        kind = kXoEvents;  // tape rows with very long event lists
+    }
+
+    // ---- new alleles of this row (slot indices), lanes hold up to 32
+    R.mo = 0;
+    R.mc = 0;
+    R.my_slot = 0xffffffffu;
+    float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
+    const float4* eff4 = reinterpret_cast<const float4*>(P.eff);
+    if (do_mut) {
+        R.mo = P.row_off[g];
+        R.mc = P.row_off[g + 1u] - R.mo;
+        if (lane < R.mc) {
+            const uint32_t i = R.mo + lane;
+            const uint32_t mi = philox ? i : P.row_mut[i];
+            R.my_slot = (mi < st.M) ? P.mut_slot[mi] : 0xffffffffu;
+            if (do_ph && R.my_slot != 0xffffffffu) {
+                const float4 e = __ldg(eff4 + R.my_slot);
+                d[0] += e.x; d[1] += e.y; d[2] += e.z; d[3] += e.w;
+            }
+        }
+        if (do_ph && R.mc > 32u && lane == 0) {
+            for (uint32_t j = 32; j < R.mc; ++j) {
+                const uint32_t mi = philox ? R.mo + j : P.row_mut[R.mo + j];
+                if (mi >= st.M) continue;
+                const uint32_t s = P.mut_slot[mi];
+                if (s == 0xffffffffu) continue;
+                const float4 e = __ldg(eff4 + s);
+                d[0] += e.x; d[1] += e.y; d[2] += e.z; d[3] += e.w;
+            }
+        }
+    }
+
+    switch (kind) {
+        case kXoCopy: row_body<kXoCopy, SR>(P, st, R, srank, sfix, X, do_mut, do_ph, do_fs, sF, sV, d); break;
+        case kXoIv4: row_body<kXoIv4, SR>(P, st, R, srank, sfix, X, do_mut, do_ph, do_fs, sF, sV, d); break;
+        case kXoIv8: row_body<kXoIv8, SR>(P, st, R, srank, sfix, X, do_mut, do_ph, do_fs, sF, sV, d); break;
+        case kXoFar: row_body<kXoFar, SR>(P, st, R, srank, sfix, X, do_mut, do_ph, do_fs, sF, sV, d); break;
+        default: row_body<kXoEvents, SR>(P, st, R, srank, sfix, X, do_mut, do_ph, do_fs, sF, sV, d); break;
+    }
+    if (do_ph) {
+        double z[kMaxTraits];
+#pragma unroll
+        for (uint32_t t = 0; t < kMaxTraits; ++t) {
+            double v = (double)d[t];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            z[t] = v;
+        }
+        if (lane < kMaxTraits) {
+            const double zt = P.zg[st.cur ^ 1u][(size_t)topr * 4u + lane];
+            const double zz = lane == 0 ? z[0] : lane == 1 ? z[1] : lane == 2 ? z[2] : z[3];
+            P.zg[st.cur][(size_t)g * 4u + lane] = (zt - P.st->fixsum[lane]) + zz;
+        }
     }
 }
 
 }  // namespace
 
-__global__ void __launch_bounds__(kGenThreads, 3)
+// Dynamic shared memory: [AND acc: maxW][OR acc: maxW][fixed mask: maxW] u64,
+// then (SR) the slot ranks as u16 [maxR].
+template <bool SR>
+__global__ void __launch_bounds__(kGenThreads, 1)
 k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restrict__ ctl, uint32_t fuse,
-             int profile) {
-    extern __shared__ uint64_t s_acc[];  // [2 * maxW]: AND then OR accumulators
+             int profile, uint32_t maxW, uint32_t maxR) {
+    extern __shared__ __align__(16) uint64_t s_dyn[];
     __shared__ uint2 s_iv[kWarps][kMaxIvSmem];
     __shared__ uint32_t s_thr[kWarps][kMaxEvDevice];
-    __shared__ uint32_t s_item;
+    __shared__ uint32_t s_item, s_next;
+    uint64_t* sF = s_dyn;
+    uint64_t* sV = s_dyn + maxW;
+    uint64_t* sfix = s_dyn + 2u * maxW;
+    uint16_t* srank = reinterpret_cast<uint16_t*>(s_dyn + 3u * maxW);
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const bool do_mut = (fuse & kFuseMut) != 0, do_ph = (fuse & kFusePheno) != 0, do_fs = (fuse & kFuseFs) != 0;
     int cur_pop = -1;
     uint32_t cur_W = 0;
-    uint64_t* sF = s_acc;
-    uint64_t* sV = s_acc;
     uint64_t rows_done = 0, words_done = 0;
 
     for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(&ctl->gen_counter, 1u);
+        if (threadIdx.x == 0) {
+            s_item = atomicAdd(&ctl->gen_counter, 1u);
+            s_next = 0;
+        }
         __syncthreads();
         const uint32_t item = s_item;
-        __syncthreads();
         if (item >= ctl->gen_items) break;
         uint32_t p;
         {
@@ -273,189 +456,32 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
                     atomicAnd((unsigned long long*)&Q.accF[w], (unsigned long long)sF[w]);
                     atomicOr((unsigned long long*)&Q.accV[w], (unsigned long long)sV[w]);
                 }
-                __syncthreads();
             }
+            __syncthreads();
             cur_pop = (int)p;
             cur_W = st.W;
-            sV = s_acc + cur_W;
             if (do_fs)
                 for (uint32_t w = threadIdx.x; w < cur_W; w += blockDim.x) { sF[w] = ~0ull; sV[w] = 0ull; }
+            for (uint32_t w = threadIdx.x; w < st.pW; w += blockDim.x) sfix[w] = P.fixmask[w];
+            if (SR)
+                for (uint32_t s = threadIdx.x; s < st.A && s < maxR; s += blockDim.x) srank[s] = (uint16_t)P.rank[s];
             __syncthreads();
         }
-
         const uint32_t S = 2u * st.N;
-        const uint64_t* prow = P.rows[st.cur ^ 1u];
-        uint64_t* crow = P.rows[st.cur];
-        const double* zpar = P.zg[st.cur ^ 1u];
-        double* zcur = P.zg[st.cur];
-        const bool q1 = (P.flags & 1u) != 0;
-        const bool philox = P.mode == kModePhilox;
-        const uint32_t row0 = (item - ctl->item_base[p]) * kRowsPerItem + warp * (kRowsPerItem / kWarps);
-
-        for (uint32_t rr = 0; rr < kRowsPerItem / kWarps; ++rr) {
-            const uint32_t g = row0 + rr;
-            if (g >= S) break;
-            // ---- parent strands and the strand-swap bit of gamete g
-            uint32_t pind = P.pairs[g];
-            if (pind >= st.pN) {
-                if (lane == 0) atomicOr(&P.st->err, kErrParent);
-                pind = 0;
-            }
-            const uint32_t h = g & 1u;
-            bool swap;
-            uint32_t E;
-            const double* evg = nullptr;
-            if (philox) {
-                const U4 x = philox4x32(g, 0u, st.gen, kStreamGamete, P.seed);
-                E = poisson_inv(u01(x.x, x.y), P.rho, P.exp_neg_rho);
-                swap = u01(x.z, x.w) < P.bias;
-                if (q1 && h) E = 0;
-                if (E > kMaxEvDevice) {
-                    if (lane == 0) atomicOr(&P.st->err, kErrEvents);
-                    E = kMaxEvDevice;
-                }
-            } else {
-                swap = P.swap[g] != 0;
-                const uint32_t e0 = P.ev_off[g], e1 = P.ev_off[g + 1u];
-                E = (q1 && h) ? 0u : e1 - e0;
-                evg = P.ev_pos + e0;
-            }
-            const uint32_t topr = 2u * pind + (swap ? 1u : 0u);
-            RowArgs R;
-            R.top = prow + (size_t)topr * P.Wcap;
-            R.bot = prow + (size_t)(topr ^ 1u) * P.Wcap;
-            R.out = crow + (size_t)g * P.Wcap;
-            R.Wc = st.W;
-            R.Wp = st.pW;
-            R.E = E;
-            R.evg = evg;
-            R.philox = philox;
-
-            // ---- breakpoints -> sorted rank thresholds -> intervals
-            Intervals iv;
-#pragma unroll
-            for (uint32_t k = 0; k < kMaxIv; ++k) { iv.a[k] = 0; iv.l[k] = 0; }
-            uint32_t nfar = 0;
-            int kind = kXoCopy;
-            if (E > 0 && E <= kMaxEvDevice) {
-                // thresholds, lane-strided, into the warp's shared buffer
-                for (uint32_t k = lane; k < E; k += 32u) {
-                    double e;
-                    if (philox) {
-                        const U4 a = philox4x32(g, 1u + (k >> 1), st.gen, kStreamGamete, P.seed);
-                        e = (k & 1u) ? u01(a.z, a.w) : u01(a.x, a.y);
-                    } else {
-                        e = __ldg(evg + k);
-                    }
-                    s_thr[warp][k] = threshold_rank(P, e);
-                }
-                __syncwarp();
-                // stable rank sort of the thresholds
-                uint32_t mine[4], posn[4];
-#pragma unroll
-                for (uint32_t q = 0; q < 4; ++q) {
-                    const uint32_t k = lane + 32u * q;
-                    mine[q] = (k < E) ? s_thr[warp][k] : 0u;
-                    posn[q] = 0;
-                }
-                for (uint32_t j = 0; j < E; ++j) {
-                    const uint32_t tj = s_thr[warp][j];
-#pragma unroll
-                    for (uint32_t q = 0; q < 4; ++q) {
-                        const uint32_t k = lane + 32u * q;
-                        posn[q] += (tj < mine[q] || (tj == mine[q] && j < k)) ? 1u : 0u;
-                    }
-                }
-                __syncwarp();
-#pragma unroll
-                for (uint32_t q = 0; q < 4; ++q) {
-                    const uint32_t k = lane + 32u * q;
-                    if (k < E) s_thr[warp][posn[q]] = mine[q];
-                }
-                __syncwarp();
-                const uint32_t NI = (E + 1u) >> 1;
-                for (uint32_t i = lane; i < NI; i += 32u) {
-                    const uint32_t a = s_thr[warp][2u * i];
-                    uint32_t l;
-                    if (2u * i + 1u < E) l = s_thr[warp][2u * i + 1u] - a;
-                    else l = a ? (uint32_t)(0x100000000ull - a) : 0xffffffffu;
-                    s_iv[warp][i] = make_uint2(a, l);
-                }
-                __syncwarp();
-                if (NI <= kMaxIv) {
-#pragma unroll
-                    for (uint32_t k = 0; k < kMaxIv; ++k) {
-                        if (k < NI) { iv.a[k] = s_iv[warp][k].x; iv.l[k] = s_iv[warp][k].y; }
-                    }
-                    kind = NI <= 2 ? kXoReg2 : (NI <= 4 ? kXoReg4 : kXoReg8);
-                } else {
-                    nfar = NI;
-                    kind = kXoSmem;
-                }
-            } else if (E > kMaxEvDevice) {
-                kind = kXoEvents;  // tape rows with very long event lists
-            }
-
-            // ---- new alleles of this row (slot indices), lanes hold up to 32
-            R.mo = 0;
-            R.mc = 0;
-            R.my_slot = 0xffffffffu;
-            float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
-            if (do_mut) {
-                R.mo = P.row_off[g];
-                R.mc = P.row_off[g + 1u] - R.mo;
-                if (lane < R.mc) {
-                    const uint32_t i = R.mo + lane;
-                    const uint32_t mi = philox ? i : P.row_mut[i];
-                    R.my_slot = (mi < st.M) ? P.mut_slot[mi] : 0xffffffffu;
-                    if (do_ph && R.my_slot != 0xffffffffu) {
-#pragma unroll
-                        for (uint32_t t = 0; t < kMaxTraits; ++t)
-                            if (t < P.T) d[t] += __ldg(P.eff + (size_t)R.my_slot * P.T + t);
-                    }
-                }
-                if (do_ph && R.mc > 32u && lane == 0) {
-                    for (uint32_t j = 32; j < R.mc; ++j) {
-                        const uint32_t mi = philox ? R.mo + j : P.row_mut[R.mo + j];
-                        if (mi >= st.M) continue;
-                        const uint32_t s = P.mut_slot[mi];
-                        if (s == 0xffffffffu) continue;
-#pragma unroll
-                        for (uint32_t t = 0; t < kMaxTraits; ++t)
-                            if (t < P.T) d[t] += __ldg(P.eff + (size_t)s * P.T + t);
-                    }
-                }
-            }
-
-            const uint2* far = s_iv[warp];
-            switch (kind) {
-                case kXoCopy: row_body<0>(P, st, R, iv, far, 0, do_mut, do_ph, do_fs, sF, sV, d); break;
-                case kXoReg2: row_body<2>(P, st, R, iv, far, 0, do_mut, do_ph, do_fs, sF, sV, d); break;
-                case kXoReg4: row_body<4>(P, st, R, iv, far, 0, do_mut, do_ph, do_fs, sF, sV, d); break;
-                case kXoReg8: row_body<8>(P, st, R, iv, far, 0, do_mut, do_ph, do_fs, sF, sV, d); break;
-                case kXoSmem: row_body<-1>(P, st, R, iv, far, nfar, do_mut, do_ph, do_fs, sF, sV, d); break;
-                default: row_body<-2>(P, st, R, iv, far, 0, do_mut, do_ph, do_fs, sF, sV, d); break;
-            }
-            if (do_ph) {
-                double z[kMaxTraits];
-#pragma unroll
-                for (uint32_t t = 0; t < kMaxTraits; ++t) {
-                    double v = (double)d[t];
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                    z[t] = v;
-                }
-                if (lane < kMaxTraits) {
-                    const double zt = zpar[(size_t)topr * 4u + lane];
-                    const double zz = lane == 0 ? z[0] : lane == 1 ? z[1] : lane == 2 ? z[2] : z[3];
-                    zcur[(size_t)g * 4u + lane] = (zt - P.st->fixsum[lane]) + zz;
-                }
-            }
+        const uint32_t r0 = (item - ctl->item_base[p]) * kRowsPerItem;
+        const uint32_t r1 = min(S, r0 + kRowsPerItem);
+        for (;;) {
+            uint32_t k = 0;
+            if (lane == 0) k = atomicAdd(&s_next, 1u);
+            const uint32_t g = r0 + __shfl_sync(0xffffffffu, k, 0);
+            if (g >= r1) break;
+            gen_row<SR>(P, st, g, srank, sfix, s_iv[warp], s_thr[warp], do_mut, do_ph, do_fs, sF, sV);
             if (profile && lane == 0) { rows_done += 1; words_done += st.W; }
         }
-    }
-    if (cur_pop >= 0 && do_fs) {
         __syncthreads();
+    }
+    __syncthreads();
+    if (cur_pop >= 0 && do_fs) {
         const PopDev& Q = pops[cur_pop];
         for (uint32_t w = threadIdx.x; w < cur_W; w += blockDim.x) {
             atomicAnd((unsigned long long*)&Q.accF[w], (unsigned long long)sF[w]);
@@ -468,23 +494,24 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     }
 }
 
+// Shared-memory rank table: u16 ranks are used when every population has
+// A <= 65,536 and the layout fits the opt-in shared-memory limit.
 void launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, WorkCtl* ctl, uint32_t maxW,
-                       uint32_t fuse, int profile) {
-    const size_t smem = 2ull * maxW * sizeof(uint64_t);
-    static size_t configured = 0;
-    static size_t occ_smem = ~(size_t)0;
-    static int occ = 1;
-    if (smem > 48u * 1024u && smem > configured) {
-        cudaFuncSetAttribute(k_generation, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        configured = smem;
+                       uint32_t maxA, uint32_t fuse, int profile) {
+    const size_t static_smem = sizeof(uint2) * kWarps * kMaxIvSmem + sizeof(uint32_t) * kWarps * kMaxEvDevice + 64;
+    const size_t base = 3ull * maxW * sizeof(uint64_t);
+    uint32_t maxR = (maxA <= 65536u) ? ((maxA + 7u) & ~7u) : 0u;
+    if (base + 2ull * maxR + static_smem > 227u * 1024u) maxR = 0;
+    const size_t smem = base + 2ull * maxR;
+    static size_t configured[2] = {0, 0};
+    const int sr = maxR > 0 ? 1 : 0;
+    if (smem + static_smem > 48u * 1024u && smem > configured[sr]) {
+        if (sr) cudaFuncSetAttribute(k_generation<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        else cudaFuncSetAttribute(k_generation<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        configured[sr] = smem;
     }
-    if (occ_smem != smem) {
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_generation, kGenThreads, smem);
-        occ = per_sm < 1 ? 1 : per_sm;
-        occ_smem = smem;
-    }
-    k_generation<<<L.num_sms * occ, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile);
+    if (sr) k_generation<true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, maxR);
+    else k_generation<false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, 0u);
 }
 
 // ---------------------------------------------------------------------------
@@ -552,8 +579,8 @@ __global__ void __launch_bounds__(256) k_phenotype(const PopDev* __restrict__ po
             const uint64_t* r = rows + (size_t)g * P.Wcap;
             for (uint32_t w = 2u * lane; w < W; w += 64u) {
                 const ulonglong2 x = *reinterpret_cast<const ulonglong2*>(r + w);
-                acc_effects(x.x, w * 64u, P.eff, P.T, 1.0f, d);
-                acc_effects(x.y, (w + 1u) * 64u, P.eff, P.T, 1.0f, d);
+                // all set bits, sign +1 (b = x, so every bit counts as brought in)
+                switched_effects(x.x, x.y, x.x, x.y, w * 64u, reinterpret_cast<const float4*>(P.eff), d);
             }
 #pragma unroll
             for (uint32_t t = 0; t < kMaxTraits; ++t) {

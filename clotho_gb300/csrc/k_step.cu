@@ -287,9 +287,9 @@ __global__ void k_mut_resolve(const PopDev* __restrict__ pops, uint32_t npops) {
             P.pos[slot] = pos;
             P.age[slot] = gen;
             for (uint32_t t = 0; t < T; ++t) {
-                const float old = P.eff[(size_t)slot * T + t];
+                const float old = P.eff[(size_t)slot * 4u + t];
                 nz_delta += (e[t] != 0.0f) - (old != 0.0f);
-                P.eff[(size_t)slot * T + t] = e[t];
+                P.eff[(size_t)slot * 4u + t] = e[t];
             }
         }
         if (nz_delta) atomicAdd(&st->nz_eff, nz_delta);

@@ -9,10 +9,11 @@ the tape; libclotho_gpu.so replays the same tape.  Bar:
   * phenotypes: the GPU carries each genome's sum from its parent row and adds
     the switched alleles' effects as FP32 lane sums folded into FP64; the FP64
     oracle re-sums every set bit.  Each generation contributes at most the error
-    of an FP32 sum of n terms, so the tolerance written here is
-    |z_gpu - z_fp64| <= (g + 1) * (n + 1) * 2^-24 * sum|w_i|
-    over the n set bits of the individual (both genomes), g generations after
-    the last full evaluation;
+    of an FP32 sum of n terms of magnitude <= sum|w|, and carried sums inherit
+    their ancestors' residue, so the tolerance written here is population-wide:
+    |z_gpu - z_fp64| <= (g + 1) * 2^-24 * max_i[(n_i + 1) * sum_i|w|]
+    with n_i the set bits and sum_i|w| the absolute effect sum of individual i
+    (both genomes), g generations after the last full evaluation;
   * fitness: equal to the metric applied to the GPU phenotype in FP64
     (rtol 1e-12), and within the propagated phenotype bound of the oracle.
 """
@@ -53,7 +54,8 @@ def pheno_bound(rows, eff, gens=0):
     n = bits.sum(axis=1)                  # [S]
     s_ind = s[0::2] + s[1::2]
     n_ind = (n[0::2] + n[1::2])[:, None]
-    return (gens + 1.0) * (n_ind + 1.0) * 2.0 ** -24 * s_ind + 1e-30
+    worst = ((n_ind + 1.0) * s_ind).max(axis=0) if len(s_ind) else np.zeros(s.shape[1])
+    return (gens + 1.0) * 2.0 ** -24 * np.broadcast_to(worst, s_ind.shape) + 1e-30
 
 
 def fitness_of(z, kind, fit_param, N, mu):
