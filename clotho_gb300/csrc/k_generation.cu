@@ -97,6 +97,75 @@ __device__ __forceinline__ void classify(uint64_t h0, uint64_t h1, uint32_t s0, 
     m1 = (uint64_t)mc | ((uint64_t)md << 32);
 }
 
+constexpr uint32_t kQueueCap = 512;    // het bits per warp-chunk handled by the balanced path
+
+// Warp-balanced classification of one 64-word chunk.  Each lane pushes the
+// het bits of its two words into the warp's queue (slot, plus bit 31 when the
+// bottom strand carries the allele); the whole warp then classifies the queue
+// four entries per lane at a time, ORs switched bits into the warp's chunk
+// mask and adds +-effect for each switched allele.  H = total het bits.
+template <int NI, bool SR>
+__device__ __forceinline__ void classify_balanced(uint64_t h0, uint64_t h1, uint64_t b0, uint64_t b1, uint32_t w,
+                                                  uint32_t w0, uint32_t off, uint32_t H, uint32_t* Q,
+                                                  uint32_t* SM, const uint16_t* srank,
+                                                  const uint32_t* __restrict__ grank, const RowXo& X,
+                                                  const float4* __restrict__ eff4, bool do_ph,
+                                                  float (&d)[kMaxTraits], uint64_t& m0, uint64_t& m1) {
+    const uint32_t lane = threadIdx.x & 31u;
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) SM[4u * lane + k] = 0u;
+    uint32_t q = off;
+    const uint32_t hh[4] = {(uint32_t)h0, (uint32_t)(h0 >> 32), (uint32_t)h1, (uint32_t)(h1 >> 32)};
+    const uint32_t bb[4] = {(uint32_t)b0, (uint32_t)(b0 >> 32), (uint32_t)b1, (uint32_t)(b1 >> 32)};
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) {
+        const uint32_t base = w * 64u + 32u * k;
+        for (uint32_t x = hh[k]; x; x &= x - 1u) {
+            const uint32_t j = (uint32_t)(__ffs(x) - 1);
+            Q[q++] = (base + j) | (((bb[k] >> j) & 1u) << 31);
+        }
+    }
+    __syncwarp();
+    const uint32_t sbase = w0 * 64u;
+    for (uint32_t ib = 0; ib < H; ib += 128u) {
+        uint32_t e[4];
+        bool sw[4];
+#pragma unroll
+        for (uint32_t k = 0; k < 4; ++k) {
+            const uint32_t i = ib + lane + 32u * k;
+            e[k] = (i < H) ? Q[i] : 0u;
+            const uint32_t slot = e[k] & 0x7fffffffu;
+            const uint32_t r = slot_rank<SR>(slot, srank, grank);
+            sw[k] = (i < H) && in_iv<NI>(r, X);
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < 4; ++k) {
+            if (sw[k]) {
+                const uint32_t loc = (e[k] & 0x7fffffffu) - sbase;
+                atomicOr(&SM[loc >> 5], 1u << (loc & 31u));
+            }
+        }
+        if (do_ph) {
+            float4 ef[4];
+#pragma unroll
+            for (uint32_t k = 0; k < 4; ++k)
+                ef[k] = sw[k] ? __ldg(eff4 + (e[k] & 0x7fffffffu)) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (uint32_t k = 0; k < 4; ++k) {
+                const float g = sw[k] ? ((e[k] >> 31) ? 1.0f : -1.0f) : 0.0f;
+                d[0] = fmaf(g, ef[k].x, d[0]);
+                d[1] = fmaf(g, ef[k].y, d[1]);
+                d[2] = fmaf(g, ef[k].z, d[2]);
+                d[3] = fmaf(g, ef[k].w, d[3]);
+            }
+        }
+    }
+    __syncwarp();
+    m0 = (uint64_t)SM[4u * lane] | ((uint64_t)SM[4u * lane + 1u] << 32);
+    m1 = (uint64_t)SM[4u * lane + 2u] | ((uint64_t)SM[4u * lane + 3u] << 32);
+    __syncwarp();
+}
+
 // Bits of h whose slot position is >= an odd number of the events (direct
 // double compares against the event list; used only for very long lists).
 __device__ __forceinline__ uint64_t sw_mask_events(uint64_t h, uint32_t base, const double* __restrict__ pos,
@@ -180,9 +249,9 @@ __device__ __forceinline__ void fold_fs(uint64_t* sF, uint64_t* sV, uint32_t w, 
 
 template <int KIND, bool SR>
 __device__ __forceinline__ void row_body(const PopDev& P, const DevStatus& st, const RowArgs& R,
-                                         const uint16_t* srank, const uint64_t* sfix, const RowXo& X, bool do_mut,
-                                         bool do_ph, bool do_fs, uint64_t* sF, uint64_t* sV,
-                                         float (&d)[kMaxTraits]) {
+                                         const uint16_t* srank, const uint64_t* sfix, const RowXo& X, uint32_t* Q,
+                                         uint32_t* SM, bool do_mut, bool do_ph, bool do_fs, uint64_t* sF,
+                                         uint64_t* sV, float (&d)[kMaxTraits]) {
     const uint32_t lane = threadIdx.x & 31u;
     constexpr bool xo = (KIND != kXoCopy);
     const float4* eff4 = reinterpret_cast<const float4*>(P.eff);
@@ -215,24 +284,41 @@ __device__ __forceinline__ void row_body(const PopDev& P, const DevStatus& st, c
                 else if (sw == w + 1u) mx1 ^= 1ull << (s & 63u);
             }
         }
-        if (w < R.Wc) {
-            ulonglong2 fm = make_ulonglong2(0, 0);
-            if (w < R.Wp) fm = *reinterpret_cast<const ulonglong2*>(sfix + w);
-            const uint64_t t0 = t_a.x & ~fm.x, t1 = t_a.y & ~fm.y;
-            uint64_t x0 = t0, x1 = t1;
-            if (xo) {
-                const uint64_t b0 = b_a.x & ~fm.x, b1 = b_a.y & ~fm.y;
-                uint64_t m0, m1;
-                if (KIND != kXoEvents) {
-                    classify<(KIND > 0 ? KIND : 0), SR>(t0 ^ b0, t1 ^ b1, w * 64u, srank, P.rank, X, m0, m1);
-                } else {
-                    m0 = sw_mask_events(t0 ^ b0, w * 64u, P.pos, R.evg, R.E);
-                    m1 = sw_mask_events(t1 ^ b1, w * 64u + 64u, P.pos, R.evg, R.E);
+        const bool live = w < R.Wc;
+        ulonglong2 fm = make_ulonglong2(0, 0);
+        if (live && w < R.Wp) fm = *reinterpret_cast<const ulonglong2*>(sfix + w);
+        const uint64_t t0 = t_a.x & ~fm.x, t1 = t_a.y & ~fm.y;
+        uint64_t x0 = t0, x1 = t1;
+        if (xo) {
+            const uint64_t b0 = b_a.x & ~fm.x, b1 = b_a.y & ~fm.y;
+            const uint64_t h0 = live ? (t0 ^ b0) : 0ull, h1 = live ? (t1 ^ b1) : 0ull;
+            uint64_t m0, m1;
+            if (KIND != kXoEvents) {
+                // warp prefix of het counts decides between the balanced queue and per-lane chains
+                const uint32_t c = (uint32_t)(__popcll(h0) + __popcll(h1));
+                uint32_t incl = c;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= (uint32_t)o) incl += y;
                 }
-                x0 = (t0 & ~m0) | (b0 & m0);
-                x1 = (t1 & ~m1) | (b1 & m1);
+                const uint32_t H = __shfl_sync(0xffffffffu, incl, 31);
+                if (H <= kQueueCap) {
+                    classify_balanced<(KIND > 0 ? KIND : 0), SR>(h0, h1, b0, b1, w, w0, incl - c, H, Q, SM, srank,
+                                                                  P.rank, X, eff4, do_ph, d, m0, m1);
+                } else {
+                    classify<(KIND > 0 ? KIND : 0), SR>(h0, h1, w * 64u, srank, P.rank, X, m0, m1);
+                    if (do_ph) switched_effects(m0, m1, b0, b1, w * 64u, eff4, d);
+                }
+            } else {
+                m0 = sw_mask_events(h0, w * 64u, P.pos, R.evg, R.E);
+                m1 = sw_mask_events(h1, w * 64u + 64u, P.pos, R.evg, R.E);
                 if (do_ph) switched_effects(m0, m1, b0, b1, w * 64u, eff4, d);
             }
+            x0 = (t0 & ~m0) | (b0 & m0);
+            x1 = (t1 & ~m1) | (b1 & m1);
+        }
+        if (live) {
             x0 ^= mx0;
             x1 ^= mx1;
             *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(x0, x1);
@@ -246,8 +332,9 @@ __device__ __forceinline__ void row_body(const PopDev& P, const DevStatus& st, c
 // One offspring row, the whole warp.
 template <bool SR>
 __device__ __forceinline__ void gen_row(const PopDev& P, const DevStatus& st, uint32_t g, const uint16_t* srank,
-                                        const uint64_t* sfix, uint2* s_iv, uint32_t* s_thr, bool do_mut,
-                                        bool do_ph, bool do_fs, uint64_t* sF, uint64_t* sV) {
+                                        const uint64_t* sfix, uint2* s_iv, uint32_t* s_thr, uint32_t* Q,
+                                        uint32_t* SM, bool do_mut, bool do_ph, bool do_fs, uint64_t* sF,
+                                        uint64_t* sV) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t* prow = P.rows[st.cur ^ 1u];
     uint64_t* crow = P.rows[st.cur];
@@ -385,11 +472,11 @@ __device__ __forceinline__ void gen_row(const PopDev& P, const DevStatus& st, ui
     }
 
     switch (kind) {
-        case kXoCopy: row_body<kXoCopy, SR>(P, st, R, srank, sfix, X, do_mut, do_ph, do_fs, sF, sV, d); break;
-        case kXoIv4: row_body<kXoIv4, SR>(P, st, R, srank, sfix, X, do_mut, do_ph, do_fs, sF, sV, d); break;
-        case kXoIv8: row_body<kXoIv8, SR>(P, st, R, srank, sfix, X, do_mut, do_ph, do_fs, sF, sV, d); break;
-        case kXoFar: row_body<kXoFar, SR>(P, st, R, srank, sfix, X, do_mut, do_ph, do_fs, sF, sV, d); break;
-        default: row_body<kXoEvents, SR>(P, st, R, srank, sfix, X, do_mut, do_ph, do_fs, sF, sV, d); break;
+        case kXoCopy: row_body<kXoCopy, SR>(P, st, R, srank, sfix, X, Q, SM, do_mut, do_ph, do_fs, sF, sV, d); break;
+        case kXoIv4: row_body<kXoIv4, SR>(P, st, R, srank, sfix, X, Q, SM, do_mut, do_ph, do_fs, sF, sV, d); break;
+        case kXoIv8: row_body<kXoIv8, SR>(P, st, R, srank, sfix, X, Q, SM, do_mut, do_ph, do_fs, sF, sV, d); break;
+        case kXoFar: row_body<kXoFar, SR>(P, st, R, srank, sfix, X, Q, SM, do_mut, do_ph, do_fs, sF, sV, d); break;
+        default: row_body<kXoEvents, SR>(P, st, R, srank, sfix, X, Q, SM, do_mut, do_ph, do_fs, sF, sV, d); break;
     }
     if (do_ph) {
         double z[kMaxTraits];
@@ -419,6 +506,8 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     extern __shared__ __align__(16) uint64_t s_dyn[];
     __shared__ uint2 s_iv[kWarps][kMaxIvSmem];
     __shared__ uint32_t s_thr[kWarps][kMaxEvDevice];
+    __shared__ uint32_t s_q[kWarps][kQueueCap];
+    __shared__ uint32_t s_sm[kWarps][128];
     __shared__ uint32_t s_item, s_next;
     uint64_t* sF = s_dyn;
     uint64_t* sV = s_dyn + maxW;
@@ -475,7 +564,8 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             if (lane == 0) k = atomicAdd(&s_next, 1u);
             const uint32_t g = r0 + __shfl_sync(0xffffffffu, k, 0);
             if (g >= r1) break;
-            gen_row<SR>(P, st, g, srank, sfix, s_iv[warp], s_thr[warp], do_mut, do_ph, do_fs, sF, sV);
+            gen_row<SR>(P, st, g, srank, sfix, s_iv[warp], s_thr[warp], s_q[warp], s_sm[warp], do_mut, do_ph, do_fs,
+                        sF, sV);
             if (profile && lane == 0) { rows_done += 1; words_done += st.W; }
         }
         __syncthreads();
@@ -498,7 +588,8 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
 // A <= 65,536 and the layout fits the opt-in shared-memory limit.
 void launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, WorkCtl* ctl, uint32_t maxW,
                        uint32_t maxA, uint32_t fuse, int profile) {
-    const size_t static_smem = sizeof(uint2) * kWarps * kMaxIvSmem + sizeof(uint32_t) * kWarps * kMaxEvDevice + 64;
+    const size_t static_smem = sizeof(uint2) * kWarps * kMaxIvSmem + sizeof(uint32_t) * kWarps * kMaxEvDevice +
+                               sizeof(uint32_t) * kWarps * (kQueueCap + 128) + 64;
     const size_t base = 3ull * maxW * sizeof(uint64_t);
     uint32_t maxR = (maxA <= 65536u) ? ((maxA + 7u) & ~7u) : 0u;
     if (base + 2ull * maxR + static_smem > 227u * 1024u) maxR = 0;
