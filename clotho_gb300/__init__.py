@@ -110,6 +110,14 @@ class Population:
         self._ck(self.L.clotho_seed_population(self.h, N, len(pos), _ptr(pos), _ptr(eff), _ptr(thr), seed),
                  "seed_population")
 
+    def load_population(self, N: int, rows, pos, eff):
+        """Explicit start from rows in the reference layout (2N x ceil(A/512)*8 words)."""
+        rows = np.ascontiguousarray(rows, np.uint64)
+        pos = np.ascontiguousarray(pos, np.float64)
+        eff = np.ascontiguousarray(eff, np.float32)
+        self._ck(self.L.clotho_load_population(self.h, N, len(pos), _ptr(rows), _ptr(pos), _ptr(eff)),
+                 "load_population")
+
     # ---- fused generation (Engine::simulate)
     def simulate(self, tape):
         t = tape if isinstance(tape, GenTape) else GenTape(tape.N, tape.M, tape.pairs, tape.swap, tape.ev_off,

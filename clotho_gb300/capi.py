@@ -54,6 +54,7 @@ SIGNATURES = {
     "clotho_sync": (C.c_int, [vp]),
     "clotho_init": (C.c_int, [vp, u32]),
     "clotho_seed_population": (C.c_int, [vp, u32, u32, vp, vp, vp, u64]),
+    "clotho_load_population": (C.c_int, [vp, u32, u32, vp, vp, vp]),
     "clotho_generation_tape": (C.c_int, [vp, C.POINTER(GenTape)]),
     "clotho_generation_philox": (C.c_int, [vp, u32]),
     "clotho_run_philox": (C.c_int, [vp, u32, u32]),

@@ -461,9 +461,9 @@ int clotho_init(clotho_ctx* ctx, uint32_t N0) {
     return 0;
 }
 
-int clotho_seed_population(clotho_ctx* ctx, uint32_t N, uint32_t A, const double* pos, const float* eff,
-                           const uint32_t* thr, uint64_t seed) {
-    if (!ctx || (A && (!pos || !eff || !thr))) return CLOTHO_E_ARG;
+// Shared set-up of an explicit or seeded start: status, allele tables, then
+// (after the caller fills the rows) reduction, phenotype and fitness.
+static int start_population(clotho_ctx* ctx, uint32_t N, uint32_t A, const double* pos, const float* eff) {
     PopHost* p = ctx->pops[0];
     const PopDev& D = p->dev[0];
     if (A > D.Acap || ref_width(A) > D.Wcap) return fail(ctx, CLOTHO_E_CAPACITY, "A exceeds max_alleles");
@@ -482,8 +482,6 @@ int clotho_seed_population(clotho_ctx* ctx, uint32_t N, uint32_t A, const double
     s.fit_const = 1;
     s.fit_total = (double)N;
     CK(cudaMemcpyAsync(D.st, &s, sizeof(s), cudaMemcpyHostToDevice, ctx->stream));
-    uint32_t* d_thr = nullptr;
-    CK(cudaMalloc(&d_thr, std::max<size_t>(4, (size_t)A * 4)));
     if (A) {
         CK(cudaMemcpyAsync(D.pos, pos, (size_t)A * 8, cudaMemcpyHostToDevice, ctx->stream));
         std::vector<float> pad((size_t)A * 4, 0.0f);
@@ -491,20 +489,63 @@ int clotho_seed_population(clotho_ctx* ctx, uint32_t N, uint32_t A, const double
             for (uint32_t t = 0; t < T; ++t) pad[i * 4 + t] = eff[i * T + t];
         CK(cudaMemcpyAsync(D.eff, pad.data(), (size_t)A * 16, cudaMemcpyHostToDevice, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
-        CK(cudaMemcpyAsync(d_thr, thr, (size_t)A * 4, cudaMemcpyHostToDevice, ctx->stream));
     }
+    return 0;
+}
+
+static int finish_start(clotho_ctx* ctx) {
+    PopHost* p = ctx->pops[0];
     LaunchCfg L = cfg(ctx);
-    launch_seed_rows(L, ctx->d_pops[0], 0, d_thr, seed, A);
     launch_fs_reduce(L, ctx->d_pops[0], 1, ctx->maxW, 0u);
     launch_phenotype(L, ctx->d_pops[0], 1);
     launch_individuals(L, ctx->d_pops[0], 1);
     launch_cdf(L, ctx->d_pops[0], 1, ctx->maxN);
-    ctx->launches += 10;
-    if ((rc = check_launch(ctx, "seed"))) return rc;
+    ctx->launches += 6;
+    int rc = check_launch(ctx, "start");
+    if (rc) return rc;
     CK(cudaStreamSynchronize(ctx->stream));
-    cudaFree(d_thr);
     p->acc_valid = true;
     return 0;
+}
+
+int clotho_load_population(clotho_ctx* ctx, uint32_t N, uint32_t A, const uint64_t* rows, const double* pos,
+                           const float* eff) {
+    if (!ctx || (A && (!pos || !eff || !rows))) return CLOTHO_E_ARG;
+    int rc = start_population(ctx, N, A, pos, eff);
+    if (rc) return rc;
+    const PopDev& D = ctx->pops[0]->dev[0];
+    const size_t W = ref_width(A), S = 2ull * N;
+    if (S * W) {
+        // keep only slots < A (the reference never sets bits past its allele count)
+        std::vector<uint64_t> tmp(rows, rows + S * W);
+        for (size_t r = 0; r < S; ++r)
+            for (size_t w = 0; w < W; ++w) {
+                const size_t b = w * 64;
+                uint64_t valid = (b + 64 <= A) ? ~0ull : (b >= A ? 0ull : ((1ull << (A - b)) - 1ull));
+                tmp[r * W + w] &= valid;
+            }
+        CK(cudaMemcpy2DAsync(D.rows[0], (size_t)D.Wcap * 8, tmp.data(), W * 8, W * 8, S, cudaMemcpyHostToDevice,
+                             ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return finish_start(ctx);
+}
+
+int clotho_seed_population(clotho_ctx* ctx, uint32_t N, uint32_t A, const double* pos, const float* eff,
+                           const uint32_t* thr, uint64_t seed) {
+    if (!ctx || (A && (!pos || !eff || !thr))) return CLOTHO_E_ARG;
+    {
+        int rc0 = start_population(ctx, N, A, pos, eff);
+        if (rc0) return rc0;
+        uint32_t* d_thr = nullptr;
+        CK(cudaMalloc(&d_thr, std::max<size_t>(4, (size_t)A * 4)));
+        if (A) CK(cudaMemcpyAsync(d_thr, thr, (size_t)A * 4, cudaMemcpyHostToDevice, ctx->stream));
+        launch_seed_rows(cfg(ctx), ctx->d_pops[0], 0, d_thr, seed, A);
+        ctx->launches += 1;
+        CK(cudaStreamSynchronize(ctx->stream));
+        cudaFree(d_thr);
+        return finish_start(ctx);
+    }
 }
 
 int clotho_generation_tape(clotho_ctx* ctx, const clotho_gen_tape* tape) {

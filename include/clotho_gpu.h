@@ -140,6 +140,12 @@ int  clotho_init(clotho_ctx *ctx, uint32_t N0);
 int  clotho_seed_population(clotho_ctx *ctx, uint32_t N, uint32_t A, const double *pos,
                             const float *eff, const uint32_t *thr, uint64_t seed);
 
+/* Explicit start: rows [2N * ceil(A/512)*8] words in the reference layout
+ * (bits at slots >= A are ignored), positions pos[A], effects eff[A*T];
+ * ages 0.  Phenotypes and fitness are evaluated. */
+int  clotho_load_population(clotho_ctx *ctx, uint32_t N, uint32_t A, const uint64_t *rows,
+                            const double *pos, const float *eff);
+
 /* ---- fused generation (the hot path) ------------------------------------ */
 /* Engine::simulate() (engine_batched_task.hpp:163-223) with the tape standing
  * in for the RNG draws: free space + fixed removal (FreeSpaceAnalyzerMT,

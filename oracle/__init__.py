@@ -67,6 +67,7 @@ def lib():
         L.orc_destroy.argtypes = [vp]
         L.orc_init.argtypes = [vp, C.c_uint32]
         L.orc_seed_population.argtypes = [vp, C.c_uint32, C.c_uint32, vp, vp, vp, C.c_uint64]
+        L.orc_load_population.argtypes = [vp, C.c_uint32, C.c_uint32, vp, vp, vp]
         L.orc_step_tape.argtypes = [vp, C.POINTER(OrcTape)]
         L.orc_step_tape.restype = C.c_int
         L.orc_step_record.argtypes = [vp, C.c_uint32]
@@ -140,6 +141,12 @@ class Oracle:
         eff = np.ascontiguousarray(eff, np.float32)
         thr = np.ascontiguousarray(thr, np.uint32)
         self.L.orc_seed_population(self.h, N, len(pos), _p(pos), _p(eff), _p(thr), seed)
+
+    def load_population(self, N, rows, pos, eff):
+        rows = np.ascontiguousarray(rows, np.uint64)
+        pos = np.ascontiguousarray(pos, np.float64)
+        eff = np.ascontiguousarray(eff, np.float32)
+        self.L.orc_load_population(self.h, N, len(pos), _p(rows), _p(pos), _p(eff))
 
     def step_tape(self, tape: Tape):
         s = tape.as_struct()

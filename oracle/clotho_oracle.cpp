@@ -453,6 +453,17 @@ struct Engine {
         evaluate_child();
     }
 
+    void load(uint32_t N, uint32_t A, const uint64_t* rows, const double* pos, const float* eff) {
+        init(N);
+        child->grow(N, A, prm.T);
+        std::copy(rows, rows + (size_t)child->rows * child->B, child->g.begin());
+        alleles.pos.assign(pos, pos + A);
+        alleles.age.assign(A, 0);
+        traits.w.assign(A * (size_t)prm.T, 0.0);
+        for (size_t i = 0; i < (size_t)A * prm.T; ++i) traits.w[i] = (double)eff[i];
+        evaluate_child();
+    }
+
     // child_max_alleles :287-301
     static size_t child_max_alleles(size_t Np, size_t Fp, size_t Mc) {
         return (Fp >= Mc) ? Np : Np + (Mc - Fp);
@@ -669,6 +680,10 @@ void orc_init(void* h, uint32_t N0) { static_cast<Engine*>(h)->init(N0); }
 void orc_seed_population(void* h, uint32_t N, uint32_t A, const double* pos, const float* eff,
                          const uint32_t* thr, uint64_t seed) {
     static_cast<Engine*>(h)->seed(N, A, pos, eff, thr, seed);
+}
+void orc_load_population(void* h, uint32_t N, uint32_t A, const uint64_t* rows, const double* pos,
+                         const float* eff) {
+    static_cast<Engine*>(h)->load(N, A, rows, pos, eff);
 }
 int orc_step_tape(void* h, const orc_tape* t) { return static_cast<Engine*>(h)->step(*t); }
 int orc_step_record(void* h, uint32_t N) { return static_cast<Engine*>(h)->step_record(N); }

@@ -92,6 +92,10 @@ void  orc_init(void *h, uint32_t N0);
  * The same rule is implemented by the device (clotho_seed_population). */
 void  orc_seed_population(void *h, uint32_t N, uint32_t A, const double *pos,
                           const float *eff, const uint32_t *thr, uint64_t seed);
+/* Explicit start: 2N rows of ceil(A/512)*8 words, positions pos[A], effects
+ * eff[A*T]; ages 0.  Phenotypes and fitness are evaluated. */
+void  orc_load_population(void *h, uint32_t N, uint32_t A, const uint64_t *rows,
+                          const double *pos, const float *eff);
 /* One generation consuming a tape.  Returns 0 or a negative error. */
 int   orc_step_tape(void *h, const orc_tape *t);
 /* One generation drawing from the oracle's own RNG in the reference's draw

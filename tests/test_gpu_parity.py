@@ -249,3 +249,21 @@ def test_philox_mode_runs_and_is_deterministic():
     assert np.array_equal(a.rows(), b.rows())
     assert np.array_equal(a.phenotypes(), b.phenotypes())
     assert a.info()["A"] > 100
+
+
+@pytest.mark.parametrize("q1", [True, False])
+def test_crossover_fixture_on_gpu(q1):
+    # unittest/data_spaces/crossover_test.cpp:37-111 restated (tests/test_oracle_kat.py)
+    from tests.test_oracle_kat import crossover_engine_case, bit
+    (N, rows, pos, eff), tape, kid = crossover_engine_case(q1)
+    orc = oracle.Oracle(T=1, mu=0.0, rho=0.0, p_neutral=1.0, q1=q1, threads=1)
+    gpu = cg.Population(N, 150, 1, mu=0.0, rho=0.0, p_neutral=1.0, q1=q1, max_events=16, max_mutations=16)
+    orc.load_population(N, rows, pos, eff)
+    gpu.load_population(N, rows, pos, eff)
+    assert np.array_equal(gpu.rows(), orc.rows())
+    orc.step_tape(tape)
+    gpu.simulate(tape)
+    child = gpu.rows()
+    assert np.array_equal(child, orc.rows())
+    for a, want in ((77, True), (33, False), (88, True), (99, False), (22, True), (15, True)):
+        assert bit(child, kid, a) == want, a
