@@ -17,6 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(OUT_DIR, "libclotho_gpu.so")
+DRIVER_PATH = os.path.join(OUT_DIR, "qtlsim_gb300")
+CPP_DIR = os.path.join(HERE, "cpp")
 SOURCES = ["capi.cu", "k_freespace.cu", "k_step.cu", "k_generation.cu"]
 HEADERS = ["engine.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -63,6 +65,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
         list(ex.map(run, jobs))
     if force or jobs or _stale(LIB_PATH, objs):
         run([nv, *ARCH, "-shared", "-cudart", "static", "-o", LIB_PATH, *objs])
+    # C++ driver over the policy adapters (host code only, linked to the library)
+    drv_src = [os.path.join(CPP_DIR, "qtlsim_gb300.cpp"), os.path.join(CPP_DIR, "clotho_gb300.hpp")]
+    if force or _stale(DRIVER_PATH, drv_src + [LIB_PATH]):
+        cxx = os.environ.get("CXX", "g++")
+        run([cxx, "-O2", "-std=c++17", drv_src[0], "-o", DRIVER_PATH, "-L", OUT_DIR, "-lclotho_gpu",
+             "-Wl,-rpath,$ORIGIN"])
     return LIB_PATH
 
 

@@ -1,0 +1,373 @@
+// clotho_gb300.hpp -- C++ policy adapters over the C-ABI (include/clotho_gpu.h).
+//
+// Header-only mirror of the stage policies that
+// Engine<RNG,Real,Block,Size,batched_task> selects through its member
+// typedefs (examples/QTLSim/engine_batched_task.hpp:84-103).  Each adapter keeps
+// the reference member names and argument meaning; the work runs in
+// libclotho_gpu.so.  EngineGB300 restates Engine::simulate()
+// (engine_batched_task.hpp:163-223): the host draws the generation's random
+// numbers in the reference's order into an event tape and the device does the
+// rest.  Errors throw clotho::gb300::Error (the reference asserts).
+#pragma once
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/clotho_gpu.h"
+
+namespace clotho {
+namespace gb300 {
+
+struct Error : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+inline void check(int rc, clotho_ctx* ctx, const char* what) {
+    if (rc != CLOTHO_OK)
+        throw Error(std::string(what) + " failed (" + std::to_string(rc) + "): " + clotho_last_error(ctx));
+}
+
+// Simulation parameters with the reference's configuration keys.
+struct Parameters {
+    uint32_t max_individuals = 10000;  // population_growth predefined default (predefined_population_growth_generator.cpp:21)
+    uint32_t max_alleles = 1u << 16;
+    uint32_t traits = 1;               // traits.N (trait_count_parameter.hpp:23)
+    double mu = 1e-4;                  // mutation.mu (mutation_rate_parameter.hpp:24)
+    double rho = 1e-4;                 // recombination.rho (recombination_rate_parameter.hpp:24)
+    double bias = 0.5;                 // recombination.sequence_bias.p (sequence_bias_parameter.hpp:23)
+    double p_neutral = 0.5;            // neutral.p (neutral_parameter.hpp:35)
+    double eff_mean = 0.0, eff_sigma = 1.0;  // traits.mean / traits.sigma
+    int fitness = CLOTHO_FIT_GAUSSIAN;       // fitness.name
+    double fit_param = 1.0;                  // fitness.params.scale (quadratic) or Vs
+    bool q1 = true;                    // second gamete never recombines (reference behaviour)
+    uint64_t seed = 1;
+};
+
+// Owns one resident population (clotho_ctx).
+class Context {
+public:
+    explicit Context(const Parameters& p) : p_(p) {
+        clotho_desc d{};
+        d.max_individuals = p.max_individuals;
+        d.max_alleles = p.max_alleles;
+        d.traits = p.traits;
+        const double S = 2.0 * p.max_individuals;
+        d.max_events = (uint32_t)(S * p.rho + 10.0 * std::sqrt(S * p.rho + 1.0) + 64);
+        d.max_mutations = (uint32_t)(S * p.mu + 10.0 * std::sqrt(S * p.mu + 1.0) + 64);
+        d.max_fixed = std::max<uint32_t>(1024, p.max_alleles);
+        d.fitness = p.fitness;
+        d.flags = p.q1 ? CLOTHO_FLAG_Q1 : 0u;
+        d.fit_param = p.fit_param;
+        d.mu = p.mu;
+        d.rho = p.rho;
+        d.bias = p.bias;
+        d.p_neutral = p.p_neutral;
+        d.eff_mean = p.eff_mean;
+        d.eff_sigma = p.eff_sigma;
+        d.seed = p.seed;
+        if (clotho_create(&d, &ctx_) != CLOTHO_OK) throw Error("clotho_create failed");
+    }
+    ~Context() {
+        if (ctx_) clotho_destroy(ctx_);
+    }
+    Context(const Context&) = delete;
+    Context& operator=(const Context&) = delete;
+    clotho_ctx* get() const { return ctx_; }
+    const Parameters& params() const { return p_; }
+    clotho_info info() const {
+        clotho_info i{};
+        check(clotho_get_info(ctx_, &i), ctx_, "clotho_get_info");
+        return i;
+    }
+
+private:
+    Parameters p_;
+    clotho_ctx* ctx_ = nullptr;
+};
+
+// ---- FreeSpaceAnalyzerMT<population_space_row> (free_space_mt_population_space_row_interlaced.hpp:41-89)
+// with the free_space_details accessors (free_space_details.hpp:193-277).
+class FreeSpaceGPU {
+public:
+    typedef uint32_t size_type;
+    typedef std::vector<size_type>::const_iterator iterator;
+
+    template <class PoolType>
+    void operator()(Context* ss, PoolType&) {
+        uint32_t c[3];
+        check(clotho_free_space(ss->get(), c), ss->get(), "clotho_free_space");
+        fixed_ = c[0];
+        lost_ = c[1];
+        idx_.assign(c[2], 0);
+        if (c[2]) check(clotho_get_free(ss->get(), idx_.data()), ss->get(), "clotho_get_free");
+        width_ = ss->info().A;
+    }
+    size_type fixed_size() const { return fixed_; }
+    size_type lost_size() const { return lost_; }
+    size_type free_size() const { return fixed_ + lost_; }
+    size_type variable_count() const { return width_ - free_size(); }
+    iterator free_begin() const { return idx_.begin(); }
+    iterator free_end() const { return idx_.end(); }
+    iterator fixed_begin() const { return idx_.begin(); }
+    iterator fixed_end() const { return idx_.begin() + fixed_; }
+    iterator lost_begin() const { return idx_.begin() + fixed_; }
+    iterator lost_end() const { return idx_.end(); }
+
+private:
+    std::vector<size_type> idx_;
+    size_type fixed_ = 0, lost_ = 0, width_ = 0;
+};
+
+// ---- SelectionGenerator<RNG, fitness_selection<GeneralFitness>>
+// (general_fitness_selection_generator.hpp:45-113): N (id0,id1) pairs,
+// uniform when every fitness is equal, else fitness-proportional.
+template <class RNG>
+class SelectionGPU {
+public:
+    typedef std::vector<std::pair<uint32_t, uint32_t>> mate_pair_vector;
+
+    explicit SelectionGPU(RNG* rng) : rng_(rng) {}
+
+    void update(const std::vector<double>& fit, unsigned N) {
+        pairs_.clear();
+        const size_t M = fit.size();
+        bool constant = true;
+        for (size_t i = 1; i < M && constant; ++i) constant = fit[i] == fit[0];
+        if (constant) {
+            std::uniform_int_distribution<uint32_t> uni(0, M ? (uint32_t)(M - 1) : 0u);
+            while (pairs_.size() < N) {
+                uint32_t a = uni(*rng_), b = uni(*rng_);
+                pairs_.emplace_back(a, b);
+            }
+        } else {
+            std::discrete_distribution<uint32_t> disc(fit.begin(), fit.end());
+            while (pairs_.size() < N) {
+                uint32_t a = disc(*rng_), b = disc(*rng_);
+                pairs_.emplace_back(a, b);
+            }
+        }
+    }
+    const mate_pair_vector& getMatePairs() const { return pairs_; }
+    unsigned individual_count() const { return (unsigned)pairs_.size(); }
+
+private:
+    RNG* rng_;
+    mate_pair_vector pairs_;
+};
+
+// ---- BatchCrossoverMTWE (batch_crossover_mtwe.hpp:51-145): the event pool,
+// lookup and bias pool are drawn on the host in the reference's order; the
+// splice runs on the device.
+template <class RNG>
+class CrossoverGPU {
+public:
+    CrossoverGPU(RNG* rng, double rho, double bias) : rng_(rng), rho_(rho), bias_(bias) {}
+
+    template <class Selection, class PoolType>
+    void operator()(const Selection& parents, Context* /*parental*/, Context* offspring, PoolType&) {
+        const size_t S = 2 * parents.individual_count();
+        draw(S);
+        std::vector<uint32_t> pairs;
+        pairs.reserve(S);
+        for (const auto& pr : parents.getMatePairs()) {
+            pairs.push_back(pr.first);
+            pairs.push_back(pr.second);
+        }
+        check(clotho_set_pairs(offspring->get(), pairs.data()), offspring->get(), "clotho_set_pairs");
+        check(clotho_crossover(offspring->get(), swap_.data(), lookup_.data(), events_.data()), offspring->get(),
+              "clotho_crossover");
+    }
+    // fill_event_pool / fill_bias_pool (:117-145)
+    void draw(size_t gametes) {
+        std::poisson_distribution<uint32_t> n_events(rho_);
+        std::uniform_real_distribution<double> pos(0.0, 1.0);
+        std::bernoulli_distribution b(bias_);
+        lookup_.clear();
+        events_.clear();
+        for (size_t g = 0; g < gametes; ++g) {
+            lookup_.push_back((uint32_t)events_.size());
+            uint32_t n = rho_ > 0 ? n_events(*rng_) : 0u;
+            while (n--) events_.push_back(pos(*rng_));
+        }
+        lookup_.push_back((uint32_t)events_.size());
+        swap_.resize(gametes);
+        for (size_t g = 0; g < gametes; ++g) swap_[g] = b(*rng_) ? 1 : 0;
+    }
+    const std::vector<uint32_t>& lookup() const { return lookup_; }
+    const std::vector<double>& events() const { return events_; }
+    const std::vector<uint8_t>& bias() const { return swap_; }
+
+private:
+    RNG* rng_;
+    double rho_, bias_;
+    std::vector<uint32_t> lookup_;
+    std::vector<double> events_;
+    std::vector<uint8_t> swap_;
+};
+
+// ---- BatchMutationMT (batch_mutation_mt.hpp:57-81) with the allele and trait
+// generators: per mutation target row, position, then per trait neutral draw
+// and Normal effect.
+template <class RNG>
+class MutationGPU {
+public:
+    MutationGPU(RNG* rng, const Parameters& p) : rng_(rng), p_(p) {}
+
+    uint32_t generateNewMutation(unsigned N_hap) {  // mutation_allocator.hpp:41-47
+        std::poisson_distribution<uint32_t> d(p_.mu * N_hap);
+        return p_.mu > 0 ? d(*rng_) : 0u;
+    }
+
+    template <class PoolType>
+    void operator()(Context* pop, unsigned M, unsigned S, PoolType&) {
+        std::uniform_int_distribution<uint32_t> seq(0, S ? S - 1 : 0);
+        std::uniform_real_distribution<double> pos(0.0, 1.0);
+        std::bernoulli_distribution neutral(p_.p_neutral);
+        std::normal_distribution<double> w(p_.eff_mean, p_.eff_sigma);
+        seq_.resize(M);
+        pos_.resize(M);
+        eff_.assign((size_t)M * p_.traits, 0.0f);
+        for (unsigned i = 0; i < M; ++i) {
+            seq_[i] = seq(*rng_);
+            pos_[i] = pos(*rng_);
+            for (unsigned t = 0; t < p_.traits; ++t)
+                if (!neutral(*rng_)) eff_[(size_t)i * p_.traits + t] = (float)w(*rng_);
+        }
+        check(clotho_mutate(pop->get(), seq_.data(), pos_.data(), eff_.data()), pop->get(), "clotho_mutate");
+    }
+
+private:
+    RNG* rng_;
+    Parameters p_;
+    std::vector<uint32_t> seq_;
+    std::vector<double> pos_;
+    std::vector<float> eff_;
+};
+
+// ---- BatchPhenotypeMT<population_space_row> (batch_phenotype_mt_population_space_row.hpp:62-104)
+class PhenotypeGPU {
+public:
+    template <class PoolType>
+    void operator()(Context* /*parent*/, Context* pop, PoolType&) {
+        check(clotho_phenotype(pop->get()), pop->get(), "clotho_phenotype");
+    }
+    std::vector<double> phenotypes(Context* pop) const {
+        clotho_info i = pop->info();
+        std::vector<double> z((size_t)i.N * pop->params().traits);
+        check(clotho_get_phenotypes(pop->get(), z.data()), pop->get(), "clotho_get_phenotypes");
+        return z;
+    }
+};
+
+// ---- GeneralFitness (general_fitness.hpp:101-119) with the toolkit metric.
+class FitnessGPU {
+public:
+    void operator()(Context* pop) { check(clotho_fitness(pop->get()), pop->get(), "clotho_fitness"); }
+    std::vector<double> values(Context* pop) const {
+        clotho_info i = pop->info();
+        std::vector<double> f(i.N);
+        check(clotho_get_fitness(pop->get(), f.data()), pop->get(), "clotho_get_fitness");
+        return f;
+    }
+};
+
+// ---- Engine<...> restated on the device (engine_batched_task.hpp:110-223).
+// staged = true drives the policies one by one; false uses the fused call.
+template <class RNG = std::mt19937_64>
+class EngineGB300 {
+public:
+    EngineGB300(RNG* rng, const Parameters& p)
+        : rng_(rng), pop_(p), sel_(rng), xover_(rng, p.rho, p.bias), mut_(rng, p), N_(p.max_individuals),
+          fit_(p.max_individuals, 1.0) {  // GeneralFitness::resize fills 1.0 (general_fitness.hpp:230-235)
+        check(clotho_init(pop_.get(), N_), pop_.get(), "clotho_init");
+    }
+
+    void simulate(bool staged = false) {
+        const auto t0 = std::chrono::steady_clock::now();
+        const unsigned N = N_;
+        const uint32_t M = mut_.generateNewMutation(2 * N);
+        if (staged) {
+            int pool = 0;
+            check(clotho_begin_generation(pop_.get(), N, M), pop_.get(), "clotho_begin_generation");
+            free_(&pop_, pool);
+            sel_.update(fit_, N);
+            xover_(sel_, &pop_, &pop_, pool);
+            mut_(&pop_, M, 2 * N, pool);
+            pheno_(&pop_, &pop_, pool);
+            fitness_(&pop_);
+            check(clotho_end_generation(pop_.get()), pop_.get(), "clotho_end_generation");
+        } else {
+            sel_.update(fit_, N);
+            xover_.draw(2 * (size_t)N);
+            std::vector<uint32_t> pairs;
+            pairs.reserve(2 * (size_t)N);
+            for (const auto& pr : sel_.getMatePairs()) {
+                pairs.push_back(pr.first);
+                pairs.push_back(pr.second);
+            }
+            int pool = 0;
+            (void)pool;
+            std::uniform_int_distribution<uint32_t> seq(0, 2 * N - 1);
+            std::uniform_real_distribution<double> pos(0.0, 1.0);
+            std::bernoulli_distribution neutral(pop_.params().p_neutral);
+            std::normal_distribution<double> w(pop_.params().eff_mean, pop_.params().eff_sigma);
+            const unsigned T = pop_.params().traits;
+            std::vector<uint32_t> ms(M);
+            std::vector<double> mp(M);
+            std::vector<float> me((size_t)M * T, 0.0f);
+            for (uint32_t i = 0; i < M; ++i) {
+                ms[i] = seq(*rng_);
+                mp[i] = pos(*rng_);
+                for (unsigned t = 0; t < T; ++t)
+                    if (!neutral(*rng_)) me[(size_t)i * T + t] = (float)w(*rng_);
+            }
+            clotho_gen_tape tape{N, M, pairs.data(), xover_.bias().data(), xover_.lookup().data(),
+                                 xover_.events().data(), ms.data(), mp.data(), me.data()};
+            check(clotho_generation_tape(pop_.get(), &tape), pop_.get(), "clotho_generation_tape");
+        }
+        fit_ = fitness_.values(&pop_);
+        const auto t1 = std::chrono::steady_clock::now();
+        sim_times_.push_back(std::chrono::duration<double>(t1 - t0).count());
+        clotho_info i = pop_.info();
+        free_sizes_.push_back(i.free_count);
+        var_sizes_.push_back(i.variable_count);
+        fixed_sizes_.push_back(i.fixed_count);
+    }
+
+    Context& population() { return pop_; }
+
+    // getPerformanceResults (engine_batched_task.hpp:233-242) as JSON
+    std::string performance_json() const {
+        auto arr = [](const auto& v) {
+            std::string s = "[";
+            for (size_t k = 0; k < v.size(); ++k) s += (k ? "," : "") + std::to_string(v[k]);
+            return s + "]";
+        };
+        return std::string("{\"performance\":{\"simulate\":") + arr(sim_times_) + "},\"memory\":{\"free_count\":" +
+               arr(free_sizes_) + ",\"variable_count\":" + arr(var_sizes_) + ",\"fixed_count\":" +
+               arr(fixed_sizes_) + "}}";
+    }
+
+private:
+    RNG* rng_;
+    Context pop_;
+    FreeSpaceGPU free_;
+    SelectionGPU<RNG> sel_;
+    CrossoverGPU<RNG> xover_;
+    MutationGPU<RNG> mut_;
+    PhenotypeGPU pheno_;
+    FitnessGPU fitness_;
+    unsigned N_;
+    std::vector<double> fit_;
+    std::vector<double> sim_times_;
+    std::vector<uint32_t> free_sizes_, var_sizes_, fixed_sizes_;
+};
+
+}  // namespace gb300
+}  // namespace clotho
