@@ -281,3 +281,138 @@ class Population:
     @property
     def launches(self) -> int:
         return int(self.L.clotho_launch_count(self.h))
+
+
+def make_desc(N: int, max_alleles: int, traits: int = 1, *, mu: float = 1e-4, rho: float = 1e-4, bias: float = 0.5,
+              p_neutral: float = 0.5, eff_mean: float = 0.0, eff_sigma: float = 1.0, fitness: str = "constant",
+              fit_param: float = 1.0, seed: int = 1, q1: bool = True, max_events: int | None = None,
+              max_mutations: int | None = None, max_fixed: int | None = None) -> capi.Desc:
+    S = 2 * N
+    if max_events is None:
+        max_events = int(S * rho + 10 * np.sqrt(S * rho + 1) + 64)
+    if max_mutations is None:
+        max_mutations = int(S * mu + 10 * np.sqrt(S * mu + 1) + 64)
+    if max_fixed is None:
+        max_fixed = max(1024, max_alleles)
+    return capi.Desc(N, max_alleles, traits, max_events, max_mutations, max_fixed, FITNESS[fitness],
+                     FLAG_Q1 if q1 else 0, fit_param, mu, rho, bias, p_neutral, eff_mean, eff_sigma, seed)
+
+
+def footprint_of(desc: capi.Desc) -> int:
+    """Device bytes a population with this descriptor holds (admission control)."""
+    return int(capi.load().clotho_footprint_for(C.byref(desc)))
+
+
+def device_memory() -> tuple[int, int]:
+    f, t = C.c_size_t(), C.c_size_t()
+    rc = capi.load().clotho_mem_info(C.byref(f), C.byref(t))
+    if rc != 0:
+        raise ClothoError("clotho_mem_info failed")
+    return f.value, t.value
+
+
+class Batch:
+    """Many resident populations in one context: every generation is one
+    launch per stage over all of them, replayable from one CUDA graph."""
+
+    def __init__(self, descs=()):
+        self.L = capi.load()
+        self.descs = list(descs)
+        arr = (capi.Desc * max(1, len(self.descs)))(*self.descs)
+        h = C.c_void_p()
+        rc = self.L.clotho_batch_create(arr if self.descs else None, len(self.descs), C.byref(h))
+        if rc != 0:
+            raise ClothoError(f"clotho_batch_create failed ({rc})")
+        self.h = h
+        self.N = [d.max_individuals for d in self.descs]
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            msg = self.L.clotho_last_error(self.h)
+            raise ClothoError(f"{what}: rc={rc}: {msg.decode() if msg else ''}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.clotho_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self):
+        return int(self.L.clotho_pop_count(self.h))
+
+    def add(self, desc: capi.Desc, N0: int | None = None) -> int:
+        idx = C.c_uint32()
+        self._ck(self.L.clotho_pop_add(self.h, C.byref(desc), C.byref(idx)), "pop_add")
+        self.descs.append(desc)
+        self.N.append(desc.max_individuals if N0 is None else N0)
+        self._ck(self.L.clotho_pop_init(self.h, idx.value, self.N[-1]), "pop_init")
+        return idx.value
+
+    def remove(self, index: int):
+        self._ck(self.L.clotho_pop_remove(self.h, index), "pop_remove")
+        del self.descs[index]
+        del self.N[index]
+
+    def init(self):
+        for i, n in enumerate(self.N):
+            self._ck(self.L.clotho_pop_init(self.h, i, n), "pop_init")
+
+    def step(self):
+        if not self.N:
+            return
+        n = np.ascontiguousarray(self.N, np.uint32)
+        self._ck(self.L.clotho_batch_generation_philox(self.h, _ptr(n)), "batch_generation_philox")
+
+    def run(self, G: int):
+        if not self.N or G <= 0:
+            return
+        n = np.ascontiguousarray(self.N, np.uint32)
+        self._ck(self.L.clotho_batch_run_philox(self.h, _ptr(n), G), "batch_run_philox")
+
+    def set_rows_per_item(self, rows: int):
+        self._ck(self.L.clotho_set_rows_per_item(self.h, rows), "set_rows_per_item")
+
+    def sync(self):
+        self._ck(self.L.clotho_sync(self.h), "sync")
+
+    def info(self, i: int) -> dict:
+        inf = capi.Info()
+        self._ck(self.L.clotho_pop_info(self.h, i, C.byref(inf)), "pop_info")
+        return {n: getattr(inf, n) for n, _ in capi.Info._fields_}
+
+    def rows(self, i: int) -> np.ndarray:
+        inf = self.info(i)
+        out = np.zeros((2 * inf["N"], inf["W"]), np.uint64)
+        self._ck(self.L.clotho_pop_rows(self.h, i, _ptr(out), out.size), "pop_rows")
+        return out
+
+    def stats(self, i: int, sfs_len: int = 0) -> dict:
+        st = capi.Stats()
+        sfs = np.zeros(sfs_len, np.uint32) if sfs_len else None
+        self._ck(self.L.clotho_pop_stats(self.h, i, C.byref(st), _ptr(sfs), sfs_len), "pop_stats")
+        d = {"segregating": st.segregating, "fixed_now": st.fixed_now, "mean_fitness": st.mean_fitness,
+             "heterozygosity": st.heterozygosity}
+        if sfs is not None:
+            d["sfs"] = sfs
+        return d
+
+    @property
+    def footprint(self) -> int:
+        return int(self.L.clotho_footprint(self.h))
+
+    @property
+    def launches(self) -> int:
+        return int(self.L.clotho_launch_count(self.h))
+
+    def timer_begin(self):
+        self._ck(self.L.clotho_timer_begin(self.h), "timer_begin")
+
+    def timer_end(self) -> float:
+        ms = C.c_double()
+        self._ck(self.L.clotho_timer_end(self.h, C.byref(ms)), "timer_end")
+        return ms.value

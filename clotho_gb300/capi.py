@@ -83,6 +83,18 @@ SIGNATURES = {
     "clotho_timer_end": (C.c_int, [vp, C.POINTER(C.c_double)]),
     "clotho_launch_count": (u64, [vp]),
     "clotho_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(vp)]),
+    "clotho_batch_create": (C.c_int, [vp, u32, C.POINTER(vp)]),
+    "clotho_pop_count": (u32, [vp]),
+    "clotho_pop_add": (C.c_int, [vp, C.POINTER(Desc), C.POINTER(u32)]),
+    "clotho_pop_remove": (C.c_int, [vp, u32]),
+    "clotho_pop_init": (C.c_int, [vp, u32, u32]),
+    "clotho_pop_info": (C.c_int, [vp, u32, C.POINTER(Info)]),
+    "clotho_pop_rows": (C.c_int, [vp, u32, vp, C.c_size_t]),
+    "clotho_pop_stats": (C.c_int, [vp, u32, C.POINTER(Stats), vp, u32]),
+    "clotho_batch_generation_philox": (C.c_int, [vp, vp]),
+    "clotho_batch_run_philox": (C.c_int, [vp, vp, u32]),
+    "clotho_set_rows_per_item": (C.c_int, [vp, u32]),
+    "clotho_mem_info": (C.c_int, [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     "clotho_host_free": (C.c_int, [vp]),
 }
 

@@ -91,7 +91,7 @@ struct clotho_ctx {
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     uint64_t launches = 0;
     cudaGraphExec_t graph = nullptr;
-    uint32_t graph_N = 0;
+    std::vector<uint32_t> graph_key;
     bool in_step = false;
     uint32_t maxW = 0, maxS = 0, maxN = 0, maxNB = 0, maxA = 0;
 };
@@ -369,6 +369,11 @@ int clotho_create(const clotho_desc* desc, clotho_ctx** out) {
         return CLOTHO_E_NOMEM;
     }
     cudaMemsetAsync(ctx->d_ctl, 0, sizeof(WorkCtl), ctx->stream);
+    {
+        const uint32_t rpi = kRowsPerItem;
+        cudaMemcpyAsync(&ctx->d_ctl->rows_per_item, &rpi, 4, cudaMemcpyHostToDevice, ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+    }
     PopHost* p = nullptr;
     int rc = alloc_pop(ctx, *desc, &p);
     if (rc) {
@@ -431,9 +436,9 @@ int clotho_sync(clotho_ctx* ctx) {
 
 uint64_t clotho_launch_count(const clotho_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
-int clotho_init(clotho_ctx* ctx, uint32_t N0) {
-    if (!ctx) return CLOTHO_E_ARG;
-    PopHost* p = ctx->pops[0];
+static int init_pop(clotho_ctx* ctx, uint32_t idx, uint32_t N0) {
+    if (!ctx || idx >= ctx->pops.size()) return fail(ctx, CLOTHO_E_ARG, "no such population");
+    PopHost* p = ctx->pops[idx];
     const PopDev& D = p->dev[0];
     if (N0 > D.Ncap) return fail(ctx, CLOTHO_E_CAPACITY, "N0 exceeds max_individuals");
     CK(cudaStreamSynchronize(ctx->stream));
@@ -454,12 +459,18 @@ int clotho_init(clotho_ctx* ctx, uint32_t N0) {
     CK(cudaMemsetAsync(D.accV, 0, (size_t)D.Wcap * 8, ctx->stream));
     CK(cudaMemsetAsync(D.row_cnt, 0, ((size_t)D.Scap + 1) * 4, ctx->stream));
     CK(cudaMemsetAsync(D.row_cur, 0, (size_t)D.Scap * 4, ctx->stream));
+    CK(cudaMemsetAsync(D.bcnt, 0, ((size_t)D.NB + 1) * 4, ctx->stream));
+    CK(cudaMemsetAsync(D.bcur, 0, (size_t)D.NB * 4, ctx->stream));
+    CK(cudaMemsetAsync(D.zg[0], 0, (size_t)D.Scap * 32, ctx->stream));
+    CK(cudaMemsetAsync(D.zg[1], 0, (size_t)D.Scap * 32, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     p->acc_valid = true;  // A == 0: the first analysis is skipped (free_space_mt...:46)
     p->ready = true;
     p->hostN = N0;
     return 0;
 }
+
+int clotho_init(clotho_ctx* ctx, uint32_t N0) { return init_pop(ctx, 0, N0); }
 
 // Shared set-up of an explicit or seeded start: status, allele tables, then
 // (after the caller fills the rows) reduction, phenotype and fitness.
@@ -601,7 +612,8 @@ int clotho_run_philox(clotho_ctx* ctx, uint32_t N, uint32_t G) {
             if ((rc = clotho_generation_philox(ctx, N))) return rc;
         return 0;
     }
-    if (!ctx->graph || ctx->graph_N != N) {
+    const std::vector<uint32_t> key(ctx->pops.size(), N);
+    if (!ctx->graph || ctx->graph_key != key) {
         if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
         cudaGraph_t gr;
         CK(cudaStreamSynchronize(ctx->stream));
@@ -610,7 +622,7 @@ int clotho_run_philox(clotho_ctx* ctx, uint32_t N, uint32_t G) {
         CK(cudaStreamEndCapture(ctx->stream, &gr));
         CK(cudaGraphInstantiate(&ctx->graph, gr, 0));
         cudaGraphDestroy(gr);
-        ctx->graph_N = N;
+        ctx->graph_key = key;
     }
     for (uint32_t g = 1; g < G; ++g) {
         CK(cudaGraphLaunch(ctx->graph, ctx->stream));
@@ -751,11 +763,11 @@ int clotho_end_generation(clotho_ctx* ctx) {
 }
 
 // ---- read-back -------------------------------------------------------------
-int clotho_get_info(clotho_ctx* ctx, clotho_info* out) {
-    if (!ctx || !out) return CLOTHO_E_ARG;
+static int info_of(clotho_ctx* ctx, uint32_t idx, clotho_info* out) {
+    if (!ctx || !out || idx >= ctx->pops.size()) return fail(ctx, CLOTHO_E_ARG, "no such population");
     CK(cudaStreamSynchronize(ctx->copy_stream));
     int rc;
-    DevStatus s = read_status(ctx, ctx->pops[0], &rc);
+    DevStatus s = read_status(ctx, ctx->pops[idx], &rc);
     if (rc) return rc;
     out->generation = s.gen;
     out->N = s.N;
@@ -773,10 +785,12 @@ int clotho_get_info(clotho_ctx* ctx, clotho_info* out) {
     return 0;
 }
 
-int clotho_get_rows(clotho_ctx* ctx, uint64_t* dst, size_t dst_words) {
-    if (!ctx) return CLOTHO_E_ARG;
+int clotho_get_info(clotho_ctx* ctx, clotho_info* out) { return info_of(ctx, 0, out); }
+
+static int rows_of(clotho_ctx* ctx, uint32_t idx, uint64_t* dst, size_t dst_words) {
+    if (!ctx || idx >= ctx->pops.size()) return fail(ctx, CLOTHO_E_ARG, "no such population");
     int rc;
-    PopHost* p = ctx->pops[0];
+    PopHost* p = ctx->pops[idx];
     DevStatus s = read_status(ctx, p, &rc);
     if (rc) return rc;
     const size_t S = 2ull * s.N, W = s.W;
@@ -787,6 +801,8 @@ int clotho_get_rows(clotho_ctx* ctx, uint64_t* dst, size_t dst_words) {
     CK(cudaStreamSynchronize(ctx->stream));
     return 0;
 }
+
+int clotho_get_rows(clotho_ctx* ctx, uint64_t* dst, size_t dst_words) { return rows_of(ctx, 0, dst, dst_words); }
 
 int clotho_get_alleles(clotho_ctx* ctx, double* pos, uint32_t* age, float* eff) {
     if (!ctx) return CLOTHO_E_ARG;
@@ -882,10 +898,10 @@ int clotho_get_pairs(clotho_ctx* ctx, uint32_t* dst) {
     return 0;
 }
 
-int clotho_stats_compute(clotho_ctx* ctx, clotho_stats* out, uint32_t* sfs, uint32_t sfs_len) {
-    if (!ctx || !out) return CLOTHO_E_ARG;
+static int stats_of(clotho_ctx* ctx, uint32_t idx, clotho_stats* out, uint32_t* sfs, uint32_t sfs_len) {
+    if (!ctx || !out || idx >= ctx->pops.size()) return fail(ctx, CLOTHO_E_ARG, "no such population");
     int rc;
-    PopHost* p = ctx->pops[0];
+    PopHost* p = ctx->pops[idx];
     DevStatus s = read_status(ctx, p, &rc);
     if (rc) return rc;
     const PopDev& D = p->dev[0];
@@ -894,7 +910,7 @@ int clotho_stats_compute(clotho_ctx* ctx, clotho_stats* out, uint32_t* sfs, uint
     uint32_t* d_counts = nullptr;
     CK(cudaMalloc(&d_counts, counts.size() * 4));
     CK(cudaMemsetAsync(d_counts, 0, counts.size() * 4, ctx->stream));
-    if (S && s.W) launch_stats(cfg(ctx), ctx->d_pops[0], 0, d_counts, s.W);
+    if (S && s.W) launch_stats(cfg(ctx), ctx->d_pops[0], idx, d_counts, s.W);
     CK(cudaMemcpyAsync(counts.data(), d_counts, counts.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
     std::vector<double> zi((size_t)s.N * 4);
     if (s.N) CK(cudaMemcpyAsync(zi.data(), D.zi, (size_t)s.N * 32, cudaMemcpyDeviceToHost, ctx->stream));
@@ -923,6 +939,10 @@ int clotho_stats_compute(clotho_ctx* ctx, clotho_stats* out, uint32_t* sfs, uint
         out->mean_phenotype[t] = s.N ? m / s.N : 0.0;
     }
     return 0;
+}
+
+int clotho_stats_compute(clotho_ctx* ctx, clotho_stats* out, uint32_t* sfs, uint32_t sfs_len) {
+    return stats_of(ctx, 0, out, sfs, sfs_len);
 }
 
 // ---- timing --------------------------------------------------------------
@@ -980,6 +1000,145 @@ int clotho_timer_end(clotho_ctx* ctx, double* ms) {
     float f = 0.f;
     CK(cudaEventElapsedTime(&f, ctx->t0, ctx->t1));
     if (ms) *ms = f;
+    return 0;
+}
+
+// ---- batched and served populations --------------------------------------
+int clotho_batch_create(const clotho_desc* descs, uint32_t n, clotho_ctx** out) {
+    if (!out || (n && !descs) || n > kMaxPops) return CLOTHO_E_ARG;
+    *out = nullptr;
+    clotho_ctx* ctx = nullptr;
+    if (n == 0) {
+        // an empty context for a serving loop: create with a tiny population, then drop it
+        clotho_desc d{};
+        d.max_individuals = 1;
+        d.max_alleles = 64;
+        d.traits = 1;
+        int rc = clotho_create(&d, &ctx);
+        if (rc) return rc;
+        free_pop(ctx->pops[0]);
+        ctx->pops.clear();
+        rc = sync_pop_arrays(ctx);
+        if (rc) { clotho_destroy(ctx); return rc; }
+        *out = ctx;
+        return 0;
+    }
+    int rc = clotho_create(&descs[0], &ctx);
+    if (rc) return rc;
+    for (uint32_t i = 1; i < n; ++i) {
+        PopHost* p = nullptr;
+        rc = alloc_pop(ctx, descs[i], &p);
+        if (rc) { clotho_destroy(ctx); return rc; }
+        ctx->pops.push_back(p);
+    }
+    rc = sync_pop_arrays(ctx);
+    if (rc) { clotho_destroy(ctx); return rc; }
+    *out = ctx;
+    return 0;
+}
+
+uint32_t clotho_pop_count(const clotho_ctx* ctx) { return ctx ? (uint32_t)ctx->pops.size() : 0u; }
+
+int clotho_pop_add(clotho_ctx* ctx, const clotho_desc* desc, uint32_t* index) {
+    if (!ctx || !desc) return CLOTHO_E_ARG;
+    if (ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "a staged generation is in progress");
+    if (ctx->pops.size() >= kMaxPops) return fail(ctx, CLOTHO_E_CAPACITY, "256 populations resident");
+    CK(cudaStreamSynchronize(ctx->stream));
+    PopHost* p = nullptr;
+    int rc = alloc_pop(ctx, *desc, &p);
+    if (rc) return rc;
+    ctx->pops.push_back(p);
+    rc = sync_pop_arrays(ctx);
+    if (rc) return rc;
+    if (index) *index = (uint32_t)ctx->pops.size() - 1;
+    return 0;
+}
+
+int clotho_pop_remove(clotho_ctx* ctx, uint32_t index) {
+    if (!ctx || index >= ctx->pops.size()) return fail(ctx, CLOTHO_E_ARG, "no such population");
+    CK(cudaStreamSynchronize(ctx->copy_stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    free_pop(ctx->pops[index]);
+    ctx->pops.erase(ctx->pops.begin() + index);
+    return sync_pop_arrays(ctx);
+}
+
+int clotho_pop_init(clotho_ctx* ctx, uint32_t index, uint32_t N0) { return init_pop(ctx, index, N0); }
+
+int clotho_pop_info(clotho_ctx* ctx, uint32_t index, clotho_info* out) { return info_of(ctx, index, out); }
+
+int clotho_pop_rows(clotho_ctx* ctx, uint32_t index, uint64_t* dst, size_t dst_words) {
+    return rows_of(ctx, index, dst, dst_words);
+}
+
+int clotho_pop_stats(clotho_ctx* ctx, uint32_t index, clotho_stats* out, uint32_t* sfs, uint32_t sfs_len) {
+    return stats_of(ctx, index, out, sfs, sfs_len);
+}
+
+int clotho_batch_generation_philox(clotho_ctx* ctx, const uint32_t* N) {
+    int rc = require_ready(ctx);
+    if (rc) return rc;
+    if (!N) return fail(ctx, CLOTHO_E_ARG, "null N");
+    if (ctx->pops.empty()) return 0;
+    if (ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "a staged generation is in progress");
+    for (size_t i = 0; i < ctx->pops.size(); ++i) {
+        if (N[i] > ctx->pops[i]->dev[2].Ncap) return fail(ctx, CLOTHO_E_CAPACITY, "N exceeds max_individuals");
+        ctx->h_hdr[2 * i] = N[i];
+        ctx->h_hdr[2 * i + 1] = 0;
+    }
+    CK(cudaMemcpyAsync(ctx->d_hdr[2], ctx->h_hdr, 8 * ctx->pops.size(), cudaMemcpyHostToDevice, ctx->stream));
+    enqueue_fused_step(ctx, 2, true);
+    if ((rc = check_launch(ctx, "batch_generation_philox"))) return rc;
+    for (size_t i = 0; i < ctx->pops.size(); ++i) ctx->pops[i]->hostN = N[i];
+    return 0;
+}
+
+int clotho_batch_run_philox(clotho_ctx* ctx, const uint32_t* N, uint32_t G) {
+    int rc = require_ready(ctx);
+    if (rc) return rc;
+    if (G == 0 || ctx->pops.empty()) return 0;
+    if ((rc = clotho_batch_generation_philox(ctx, N))) return rc;
+    if (G == 1) return 0;
+    if (ctx->profiling) {
+        for (uint32_t g = 1; g < G; ++g)
+            if ((rc = clotho_batch_generation_philox(ctx, N))) return rc;
+        return 0;
+    }
+    std::vector<uint32_t> key(N, N + ctx->pops.size());
+    if (!ctx->graph || ctx->graph_key != key) {
+        if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+        cudaGraph_t gr;
+        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_fused_step(ctx, 2, true);
+        CK(cudaStreamEndCapture(ctx->stream, &gr));
+        CK(cudaGraphInstantiate(&ctx->graph, gr, 0));
+        cudaGraphDestroy(gr);
+        ctx->graph_key = key;
+    }
+    for (uint32_t g = 1; g < G; ++g) {
+        CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+        ctx->launches += 20;
+    }
+    return 0;
+}
+
+int clotho_set_rows_per_item(clotho_ctx* ctx, uint32_t rows) {
+    if (!ctx || rows == 0 || rows > 65536) return CLOTHO_E_ARG;
+    CK(cudaMemcpyAsync(&ctx->d_ctl->rows_per_item, &rows, 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+    return 0;
+}
+
+int clotho_mem_info(size_t* free_bytes, size_t* total_bytes) {
+    size_t f = 0, t = 0;
+    if (cudaMemGetInfo(&f, &t) != cudaSuccess) {
+        cudaGetLastError();
+        return CLOTHO_E_CUDA;
+    }
+    if (free_bytes) *free_bytes = f;
+    if (total_bytes) *total_bytes = t;
     return 0;
 }
 

@@ -13,7 +13,7 @@ namespace clotho {
 
 constexpr uint32_t kMaxTraits = 4;
 constexpr uint32_t kGenThreads = 512;      // 16 warps per CTA, one CTA per SM, in the generation kernel
-constexpr uint32_t kRowsPerItem = 512;     // child rows per scheduling item
+constexpr uint32_t kRowsPerItem = 512;     // default child rows per scheduling item (tunable)
 constexpr uint32_t kMaxEvReg = 16;         // events held in registers
 constexpr uint32_t kMaxEvDevice = 128;     // device-drawn events per gamete
 constexpr uint32_t kMaxMutReg = 32;        // mutations per row held in registers
@@ -100,6 +100,8 @@ struct PopDev {
 struct WorkCtl {
     uint32_t gen_counter;           // dynamic item counter of k_generation
     uint32_t gen_items;             // total items
+    uint32_t rows_per_item;         // scheduling granularity (set by the host)
+    uint32_t pad;
     uint32_t item_base[257];        // item prefix per population (<= 256 pops)
     uint64_t rows_done;             // profiling: rows processed
     uint64_t words_done;            // profiling: words written

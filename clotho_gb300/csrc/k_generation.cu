@@ -557,8 +557,9 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             __syncthreads();
         }
         const uint32_t S = 2u * st.N;
-        const uint32_t r0 = (item - ctl->item_base[p]) * kRowsPerItem;
-        const uint32_t r1 = min(S, r0 + kRowsPerItem);
+        const uint32_t rpi = ctl->rows_per_item ? ctl->rows_per_item : kRowsPerItem;
+        const uint32_t r0 = (item - ctl->item_base[p]) * rpi;
+        const uint32_t r1 = min(S, r0 + rpi);
         for (;;) {
             uint32_t k = 0;
             if (lane == 0) k = atomicAdd(&s_next, 1u);

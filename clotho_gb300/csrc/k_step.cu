@@ -53,7 +53,8 @@ __global__ void k_begin(const PopDev* __restrict__ pops, uint32_t npops, const u
         st->N = N;
         st->M = M;
         st->cur ^= 1u;
-        s_items[p] = (2u * N + kRowsPerItem - 1u) / kRowsPerItem;
+        const uint32_t rpi = ctl->rows_per_item ? ctl->rows_per_item : kRowsPerItem;
+        s_items[p] = (2u * N + rpi - 1u) / rpi;
     }
     __syncthreads();
     if (p == 0) {

@@ -233,6 +233,33 @@ uint64_t clotho_launch_count(const clotho_ctx *ctx);
 int  clotho_host_alloc(size_t bytes, void **out);
 int  clotho_host_free(void *p);
 
+/* ---- batched and served populations ------------------------------------
+ * One context can hold up to 256 resident populations of uneven N, allele
+ * width and trait count.  Every step runs one launch per stage over all of
+ * them (the kernels walk a descriptor table), and clotho_batch_run_philox
+ * replays the step from one CUDA graph.  Populations join and leave between
+ * steps, which is what a continuous-batching serving loop needs.  No reference
+ * counterpart: the reference runs one population per process
+ * (examples/QTLSim/qtlsim_main.cpp:117-179). */
+int  clotho_batch_create(const clotho_desc *descs, uint32_t n, clotho_ctx **out);
+uint32_t clotho_pop_count(const clotho_ctx *ctx);
+/* Allocate and append a population (its index goes to *index). */
+int  clotho_pop_add(clotho_ctx *ctx, const clotho_desc *desc, uint32_t *index);
+/* Free a population; later indices shift down by one. */
+int  clotho_pop_remove(clotho_ctx *ctx, uint32_t index);
+int  clotho_pop_init(clotho_ctx *ctx, uint32_t index, uint32_t N0);
+int  clotho_pop_info(clotho_ctx *ctx, uint32_t index, clotho_info *out);
+int  clotho_pop_rows(clotho_ctx *ctx, uint32_t index, uint64_t *dst, size_t dst_words);
+int  clotho_pop_stats(clotho_ctx *ctx, uint32_t index, clotho_stats *out, uint32_t *sfs, uint32_t sfs_len);
+/* One device-drawn generation of every population (N[i] offspring). */
+int  clotho_batch_generation_philox(clotho_ctx *ctx, const uint32_t *N);
+/* G such generations, replayed from one captured CUDA graph. */
+int  clotho_batch_run_philox(clotho_ctx *ctx, const uint32_t *N, uint32_t G);
+/* Rows per scheduling item of the generation kernel (autotuner knob). */
+int  clotho_set_rows_per_item(clotho_ctx *ctx, uint32_t rows);
+/* Free and total device memory (admission control). */
+int  clotho_mem_info(size_t *free_bytes, size_t *total_bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,102 @@
+"""Batched and served forms: many populations per launch, continuous batching.
+Every population's draws depend only on its own seed and generation, so its
+genomes and statistics must be bit-identical alone and in the mix."""
+import numpy as np
+import pytest
+
+from tests.conftest import gpu_available
+
+pytestmark = pytest.mark.gpu
+
+if not gpu_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+import clotho_gb300 as cg  # noqa: E402
+from clotho_gb300 import serving, autotune  # noqa: E402
+
+SPECS = [
+    dict(N=700, T=1, mu=0.05, rho=0.5, fitness="constant", seed=11),
+    dict(N=3000, T=4, mu=0.01, rho=5.0, fitness="gaussian", seed=12),
+    dict(N=150, T=2, mu=0.2, rho=1.0, fitness="gaussian_vs", fit_param=20.0, seed=13),
+    dict(N=1200, T=3, mu=0.02, rho=2.0, fitness="quadratic", fit_param=5.0, seed=14),
+    dict(N=64, T=1, mu=0.5, rho=0.1, fitness="gaussian_vs", fit_param=2.0, seed=15),
+]
+
+
+def desc_of(s):
+    kw = {k: v for k, v in s.items() if k not in ("N", "T")}
+    return cg.make_desc(s["N"], 1 << 14, s["T"], p_neutral=0.3, **kw)
+
+
+def alone(s, G):
+    d = desc_of(s)
+    pop = cg.Population(s["N"], 1 << 14, s["T"], mu=s["mu"], rho=s["rho"], fitness=s["fitness"],
+                        fit_param=s.get("fit_param", 1.0), p_neutral=0.3, seed=s["seed"], max_events=d.max_events,
+                        max_mutations=d.max_mutations, max_fixed=d.max_fixed)
+    pop.init(s["N"])
+    pop.run_philox(s["N"], G)
+    pop.check()
+    return pop.rows(), pop.stats(64)
+
+
+def test_batch_equals_alone():
+    G = 25
+    b = cg.Batch([desc_of(s) for s in SPECS])
+    b.init()
+    b.run(G)
+    b.sync()
+    for i, s in enumerate(SPECS):
+        assert b.info(i)["device_error"] == 0
+        rows, st = alone(s, G)
+        assert np.array_equal(b.rows(i), rows), i
+        bs = b.stats(i, 64)
+        assert bs["segregating"] == st["segregating"] and np.array_equal(bs["sfs"], st["sfs"])
+        assert bs["mean_fitness"] == st["mean_fitness"]
+
+
+def test_rows_per_item_does_not_change_results():
+    G = 6
+    outs = []
+    for rpi in (64, 1024):
+        b = cg.Batch([desc_of(s) for s in SPECS[:3]])
+        b.init()
+        b.set_rows_per_item(rpi)
+        b.run(G)
+        outs.append([b.rows(i) for i in range(3)])
+    for a, c in zip(*outs):
+        assert np.array_equal(a, c)
+
+
+def test_autotuner_picks_a_candidate(tmp_path):
+    b = cg.Batch([desc_of(s) for s in SPECS])
+    b.init()
+    best = autotune.tune(b, gens_per_trial=1, cache_path=str(tmp_path / "tune.json"))
+    assert best in autotune.CANDIDATES
+    assert autotune.tune(b, cache_path=str(tmp_path / "tune.json")) == best  # cached
+
+
+def test_serving_results_match_plain_engine():
+    jobs = serving.synthetic_jobs(10, rate=200.0, seed=3, N_range=(200, 3000), G_range=(10, 40))
+    plain = [serving.Job(**{k: getattr(j, k) for k in ("id", "N", "mu", "rho", "T", "G", "seed", "arrival")})
+             for j in jobs]
+    srv = serving.Server(budget_bytes=8 << 30, max_slots=4)
+    s1 = srv.run_open_loop(jobs)
+    s2 = serving.run_plain(plain)
+    assert s1["jobs"] == s2["jobs"] == 10 and s1["errors"] == 0
+    by_id = {j.id: j for j in plain}
+    for j in srv.finished:
+        a, b = j.result, by_id[j.id].result
+        assert a["sfs"] == b["sfs"] and a["segregating"] == b["segregating"]
+        assert a["mean_fitness"] == b["mean_fitness"] and a["generation"] == b["generation"] == j.G
+
+
+def test_admission_waits_for_memory():
+    jobs = serving.synthetic_jobs(4, rate=1000.0, seed=5, N_range=(500, 600), G_range=(5, 5))
+    one = cg.footprint_of(jobs[0].desc())
+    srv = serving.Server(budget_bytes=int(one * 1.5), max_slots=8)   # room for one job at a time
+    s = srv.run_open_loop(jobs)
+    assert s["jobs"] == 4 and s["errors"] == 0
+    # never more than one resident: admissions are strictly after the previous job finished
+    fin = sorted(srv.finished, key=lambda j: j.admitted)
+    for a, b in zip(fin, fin[1:]):
+        assert b.admitted >= a.done - 1e-6
