@@ -52,6 +52,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-gens", type=int, default=4)
     p.add_argument("--kernel-only", action="store_true", help="seed + eager generations only (ncu runs)")
+    p.add_argument("--no-batched", action="store_true", help="skip the batched and serving measurements")
     return p.parse_args()
 
 
@@ -207,6 +208,65 @@ def run_cpu_oracle(w, N, steps, warmup, threads):
     return 2.0 * N * steps / dt, dt, info, stages
 
 
+def batched_and_serving():
+    """Batched replicates and continuous-batching serving against the plain
+    engine one job at a time, on scaled synthetic job mixes (the published
+    mixes need terabytes of bitsets; see the workload notes)."""
+    import numpy as np
+    import clotho_gb300 as cg
+    from clotho_gb300 import serving, autotune
+
+    # ---- batched: 256 populations, N log-U[1e3,2e4], mu U[1e-3,1e-2], rho U[0.1,5], T 1-4, G=100
+    jobs = serving.synthetic_jobs(256, rate=1e9, seed=11, N_range=(1_000, 20_000), G_range=(100, 100))
+    G = 100
+    b = cg.Batch([j.desc() for j in jobs])
+    b.init()
+    tuned = autotune.tune(b, gens_per_trial=2)
+    b2 = cg.Batch([j.desc() for j in jobs])
+    b2.init()
+    b2.set_rows_per_item(tuned)
+    b2.sync()
+    t0 = time.perf_counter()
+    b2.run(G)
+    b2.sync()
+    t_batched = time.perf_counter() - t0
+    errs = sum(1 for i in range(len(jobs)) if b2.info(i)["device_error"])
+    b.close()
+    b2.close()
+    # plain: the same jobs one at a time
+    sample = jobs
+    t0 = time.perf_counter()
+    for j in sample:
+        d = j.desc()
+        pop = cg.Population(j.N, j.max_alleles(), j.T, mu=j.mu, rho=j.rho, fitness=j.fitness,
+                            fit_param=j.fit_param, p_neutral=j.p_neutral, seed=j.seed, max_events=d.max_events,
+                            max_mutations=d.max_mutations, max_fixed=d.max_fixed)
+        pop.init(j.N)
+        pop.run_philox(j.N, G)
+        pop.sync()
+        pop.close()
+    t_plain = (time.perf_counter() - t0) / len(sample) * len(jobs)
+    batched = {"workload": "256 populations, N log-U[1e3,2e4], mu U[1e-3,1e-2], rho U[0.1,5], T 1-4, G=100",
+               "jobs_per_s": len(jobs) / t_batched, "plain_jobs_per_s": len(jobs) / t_plain,
+               "speedup": t_plain / t_batched, "rows_per_item": tuned, "device_errors": errs,
+               "plain_note": "plain = the same 256 jobs run one at a time through clotho_run_philox"}
+
+    # ---- serving: open-loop Poisson arrivals, both arms on the same job list
+    sjobs = serving.synthetic_jobs(240, rate=120.0, seed=21, N_range=(1_000, 20_000), G_range=(20, 100))
+    pjobs = [serving.Job(**{k: getattr(j, k) for k in ("id", "N", "mu", "rho", "T", "G", "seed", "arrival")})
+             for j in sjobs]
+    srv = serving.Server(budget_bytes=64 << 30, max_slots=256)
+    s_srv = srv.run_open_loop(sjobs)
+    s_plain = serving.run_plain(pjobs)
+    same = sum(1 for j, p in zip(sorted(srv.finished, key=lambda x: x.id), pjobs)
+               if j.result["sfs"] == p.result["sfs"] and j.result["mean_fitness"] == p.result["mean_fitness"])
+    serve = {"workload": "240 jobs, Poisson arrivals 120/s, N log-U[1e3,2e4], G U[20,100], mu U[1e-3,1e-2], "
+                         "rho U[0.1,5], T 1-4",
+             "served": s_srv, "plain": s_plain, "speedup_jobs_per_s": s_srv["jobs_per_s"] / s_plain["jobs_per_s"],
+             "identical_results": same}
+    return batched, serve
+
+
 def reference_arm(args, rank):
     from clotho_gb300.workloads import LARGE_N
     if rank != 0:
@@ -336,6 +396,11 @@ def main():
                           f"allele load (A={oinfo['A']}, W={oinfo['B']}), 2 generations, {dt:.1f} s"),
                "stage_seconds": stages}
 
+    batched = serve = None
+    if rank == 0 and world == 1 and not args.no_batched:
+        pop.close()
+        batched, serve = batched_and_serving()
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -344,7 +409,8 @@ def main():
                            "rho": w.rho, "mu": w.mu, "rng": "device Philox-4x32-10", "fitness": w.fitness,
                            "parallelism": "replicas" if world > 1 else "single",
                            "l2": "inputs larger than L2 (rows 16 GB per population)"},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+                "batched": batched, "serving": serve}
         print(json.dumps(line), flush=True)
 
 
