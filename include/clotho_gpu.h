@@ -260,6 +260,26 @@ int  clotho_set_rows_per_item(clotho_ctx *ctx, uint32_t rows);
 /* Free and total device memory (admission control). */
 int  clotho_mem_info(size_t *free_bytes, size_t *total_bytes);
 
+/* ---- free-space analysis that allocates nothing --------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (their device memory is owned by another allocator, or allocation is
+ * forbidden after start-up): the analysis of clotho_free_space on rows the
+ * caller owns, with its working state in a fixed array inside the library.
+ *   rows       device pointer, S rows of row_stride_words words (reference
+ *              layout; row_stride_words >= ceil(A/512)*8)
+ *   free_list  device pointer, room for ceil(A/512)*512 entries: fixed slots
+ *              ascending, then lost slots ascending
+ *   counts     device pointer to {fixed, lost, free}
+ *   stream     cudaStream_t to run on (NULL: the default stream)
+ * At most 16,384 words per row (A <= 1,048,576); larger A returns
+ * CLOTHO_E_CAPACITY.  The fixed array (256 KB) stays on every device that
+ * loaded the library until the process exits.  The first call on a device
+ * looks up the array's address; make it before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race, so order them on one
+ * stream.  Work is enqueued on `stream`; results are ready when it completes. */
+int  clotho_free_space_noalloc(const uint64_t *rows, uint32_t S, uint32_t row_stride_words, uint32_t A,
+                               uint32_t *free_list, uint32_t *counts, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
