@@ -61,7 +61,9 @@ std::vector<size_t> sizes_of(const Geometry& g) {
         (N / 1024 + 8) * 8, ((S > g.NB ? S : g.NB) / 1024 + 8) * 4ull,
         (S + 1) * 4 * 2ull,              // row_cnt, row_off
         S * 4, g.Mcap * 4ull, g.Mcap * 4ull,  // row_cur, row_mut, mut_slot
-        (g.NB + 1ull) * 4 * 2, g.NB * 4ull, A * 8, A * 4,  // bcnt+boff, bcur, bpos, rank
+        (g.NB + 1ull) * 4 * 2, g.NB * 4ull, A * 8, A * 4, A * 4,  // bcnt+boff, bcur, bpos, bslot, rank
+        A <= kSufMaxSlots ? A * 4 : 0,                            // inv
+        A <= kSufMaxSlots ? (A / 64 + 1) * W * 8 : 0,             // suf
         sizeof(DevStatus),
         // two tape sets: pairs, swap, ev_off, ev_pos, mut_seq, mut_pos, mut_eff
         S * 4, S, (S + 1) * 4, g.EVcap * 8ull, g.Mcap * 4ull, g.Mcap * 8ull, g.Mcap * T * 4ull,
@@ -134,6 +136,7 @@ int alloc_pop(clotho_ctx* ctx, const clotho_desc& d, PopHost** out) {
     std::vector<void*> ptr(sz.size(), nullptr);
     for (size_t i = 0; i < sz.size(); ++i) {
         void* q = nullptr;
+        if (sz[i] == 0) continue;  // optional table not used at this capacity
         cudaError_t e = cudaMalloc(&q, align256(sz[i]));
         if (e != cudaSuccess) {
             cudaGetLastError();
@@ -145,7 +148,8 @@ int alloc_pop(clotho_ctx* ctx, const clotho_desc& d, PopHost** out) {
         ptr[i] = q;
     }
     // zero the tables (cheap) and the status
-    for (size_t i = 2; i < sz.size(); ++i) cudaMemsetAsync(ptr[i], 0, sz[i], ctx->stream);
+    for (size_t i = 2; i < sz.size(); ++i)
+        if (sz[i]) cudaMemsetAsync(ptr[i], 0, sz[i], ctx->stream);
     PopDev b{};
     size_t k = 0;
     b.rows[0] = (uint64_t*)ptr[k++]; b.rows[1] = (uint64_t*)ptr[k++];
@@ -160,7 +164,8 @@ int alloc_pop(clotho_ctx* ctx, const clotho_desc& d, PopHost** out) {
     b.row_cur = (uint32_t*)ptr[k++]; b.row_mut = (uint32_t*)ptr[k++]; b.mut_slot = (uint32_t*)ptr[k++];
     b.bcnt = (uint32_t*)ptr[k++];
     b.boff = b.bcnt + (g.NB + 1);
-    b.bcur = (uint32_t*)ptr[k++]; b.bpos = (double*)ptr[k++]; b.rank = (uint32_t*)ptr[k++];
+    b.bcur = (uint32_t*)ptr[k++]; b.bpos = (double*)ptr[k++]; b.bslot = (uint32_t*)ptr[k++];
+    b.rank = (uint32_t*)ptr[k++]; b.inv = (uint32_t*)ptr[k++]; b.suf = (uint64_t*)ptr[k++];
     b.st = (DevStatus*)ptr[k++];
     b.Scap = g.Scap; b.Ncap = g.Ncap; b.Wcap = g.Wcap; b.Acap = g.Aslots; b.Mcap = g.Mcap;
     b.EVcap = g.EVcap; b.FXcap = g.FXcap; b.T = g.T; b.NB = g.NB;
@@ -320,7 +325,7 @@ void enqueue_fused_step(clotho_ctx* ctx, uint32_t set, bool philox) {
     launch_fs_finalize(L, pops, n);
     if (!philox) launch_mut_csr_tape(L, pops, n, ctx->maxS);
     launch_mut_resolve(L, pops, n);
-    launch_ranks(L, pops, n, ctx->maxNB);
+    launch_ranks(L, pops, n, ctx->maxNB, ctx->maxW, ctx->maxA <= kSufMaxSlots);
     if (philox) launch_select_philox(L, pops, n);
     launch_gen(ctx, pops, n, kFuseMut | kFusePheno | kFuseFs);
     launch_individuals(L, pops, n);
@@ -709,7 +714,7 @@ int clotho_crossover(clotho_ctx* ctx, const uint8_t* swap, const uint32_t* ev_of
     if ((rc = h2d(ctx, D.ev_off, ev_off, 2ull * N + 1, ctx->stream))) return rc;
     if ((rc = h2d(ctx, D.ev_pos, ev_pos, (size_t)ev_total, ctx->stream))) return rc;
     // item prefix is already set by begin; ranks over the current positions
-    launch_ranks(cfg(ctx), ctx->d_pops[0], 1, ctx->maxNB);
+    launch_ranks(cfg(ctx), ctx->d_pops[0], 1, ctx->maxNB, ctx->maxW, ctx->maxA <= kSufMaxSlots);
     ctx->launches += 6;
     launch_gen(ctx, ctx->d_pops[0], 1, 0u);
     if ((rc = check_launch(ctx, "crossover"))) return rc;

@@ -18,6 +18,7 @@ constexpr uint32_t kMaxEvReg = 16;         // events held in registers
 constexpr uint32_t kMaxEvDevice = 128;     // device-drawn events per gamete
 constexpr uint32_t kMaxMutReg = 32;        // mutations per row held in registers
 constexpr uint32_t kWordAlign = 64;        // row stride granularity (words)
+constexpr uint32_t kSufMaxSlots = 65536;   // allele capacity up to which the suffix-table classifier runs
 
 // sticky device error bits (CLOTHO_DEVERR_* in clotho_gpu.h)
 constexpr uint32_t kErrAlleles = 1u, kErrFixed = 2u, kErrEvents = 4u, kErrParent = 8u,
@@ -83,7 +84,10 @@ struct PopDev {
     uint32_t* boff;        // [NB + 1] exclusive prefix of bcnt
     uint32_t* bcur;        // [NB] bucket scatter cursors (zero between steps)
     double*   bpos;        // [Acap] positions grouped by bucket
-    uint32_t* rank;        // [Acap] rank of each slot's position among the A slots
+    uint32_t* bslot;       // [Acap] slot of each bpos entry
+    uint32_t* rank;        // [Acap] rank of each slot (position, then slot index) among the A slots
+    uint32_t* inv;         // [Acap] slot of each rank (Acap <= kSufMaxSlots, else null)
+    uint64_t* suf;         // [(Acap/64 + 1) * Wcap] suffix table of the crossover classifier (or null)
     DevStatus* st;
     uint32_t Scap, Ncap, Wcap, Acap, Mcap, EVcap, FXcap, T;
     uint32_t NB, pad2;     // position buckets (power of two)
@@ -203,7 +207,7 @@ void launch_end(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_seed_rows(const LaunchCfg&, const PopDev* pops, uint32_t npops, const uint32_t* thr,
                       uint64_t seed, uint32_t A);
 void launch_stats(const LaunchCfg&, const PopDev* pops, uint32_t p, uint32_t* counts, uint32_t A);
-void launch_ranks(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxNB);
+void launch_ranks(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxNB, uint32_t maxW, bool suf);
 void launch_uscan_buckets(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxNB);
 
 // fuse flags of k_generation

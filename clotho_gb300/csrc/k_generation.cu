@@ -5,16 +5,15 @@
 //   crossover  batch_crossover_taskwe<...population_space_row>::run_crossover_task
 //              (crossover/batch_crossover_taskwe_population_space_row.hpp:157-217)
 //              and block_crossover::crossover (crossover/block_crossover.hpp:46-63):
-//              only heterozygous bits are classified; a bit takes the bottom
-//              strand iff an odd number of breakpoints is <= its position
-//              (upper_bound in region_classifier, classifiers/region_classifier.hpp:62-77).
-//              Positions are replaced by integer ranks (rank(s) = #{slots with a
-//              smaller position}); breakpoint e becomes r(e) = #{slots with
-//              position < e}, and e <= pos(s)  <=>  r(e) <= rank(s) for every slot,
-//              ties included.  Sorted thresholds pair into half-open rank
-//              intervals; a het bit switches strand iff its rank lies in one.
-//              Fixed columns are masked on load: the in-register form of
-//              remove_fixed_allele (population_space_row_block.hpp:127-147).
+//              a heterozygous bit takes the bottom strand iff an odd number of
+//              breakpoints is <= its position (upper_bound in region_classifier,
+//              classifiers/region_classifier.hpp:62-77).  Positions are replaced by
+//              integer ranks: rank(s) = #{slots t with pos(t) < pos(s), or equal
+//              position and t < s} (a bijection onto [0, A)); breakpoint e becomes
+//              r(e) = #{slots with pos < e}, and e <= pos(s)  <=>  r(e) <= rank(s)
+//              for every slot, ties included.  Fixed columns are masked on load:
+//              the in-register form of remove_fixed_allele
+//              (population_space_row_block.hpp:127-147).
 //   mutation   XOR of the row's new alleles (population_space_row_block.hpp:111-125)
 //              in registers before the store.
 //   phenotype  z(child) = z(top strand) - sum(fixed) + sum(switched bits: bottom-top)
@@ -25,161 +24,50 @@
 //   free space AND/OR of the finished words, the next generation's
 //              FreeSpaceAnalyzerMT input (free_space_task_population_space_row_interlaced.hpp:51-72).
 //
+// Two crossover classifiers:
+//   suffix table (A <= 65,536 slots): the switch mask of a gamete with rank
+//              thresholds r_1..r_E is XOR_k G(r_k), G(r) = {slots with rank >= r}.
+//              G at every multiple of 64 is a per-generation table in L2
+//              (suf[g * Wcap + w], built by k_suf_build); G(r) differs from the
+//              nearest table row by at most 32 slots, which the warp toggles in
+//              its own correction bitmap in shared memory.  Per word: E table
+//              loads and XORs, no per-bit work.
+//   intervals  (wider allele spaces): sorted thresholds pair into half-open rank
+//              intervals; every heterozygous bit is classified by its rank.
+//
 // Rows are 64-word chunks, two words (one 128-bit load) per lane; parent words
-// are loaded two chunks ahead of use.  The het-bit walk runs the lane's four
-// 32-bit halves as independent chains (branch-free steps) so shared-memory
-// and ALU latencies overlap.  The kernel is persistent: one CTA per SM takes
-// 512-row items from a device counter and its warps claim rows one at a time,
-// so warps never wait on each other inside an item.
+// are loaded two chunks ahead of use and the whole parent row is prefetched
+// into L2 at row start.  Effects of switched alleles are gathered from a
+// per-warp queue, four entries per lane, so lanes stay balanced.  The kernel is
+// persistent: one CTA per SM takes items of rows from a device counter and its
+// warps claim rows one at a time, so warps never wait on each other inside an item.
 #include "engine.cuh"
 
 namespace clotho {
 
 namespace {
 
+// Rare paths: inlined (measured faster than out-of-line calls for this kernel).
+#define CLOTHO_COLD __forceinline__
+
 constexpr uint32_t kWarps = kGenThreads / 32;
 constexpr uint32_t kMaxIvSmem = 64;     // rank intervals in shared memory (E <= 128)
-
 constexpr uint32_t kMaxIv = 8;          // rank intervals held in registers (E <= 16)
+constexpr uint32_t kQueueCap = 512;     // entries of the per-warp queue (power of two)
 
-// Sorted breakpoint thresholds of one gamete as half-open rank intervals:
-// a het bit switches strand iff its slot rank lies in one of them.
-struct RowXo {
-    uint32_t a[kMaxIv];   // interval start (rank)
-    uint32_t l[kMaxIv];   // length; 0 = empty
-    const uint2* iv;      // the same intervals in shared memory (any count)
-    uint32_t niv;
-};
+// ---------------------------------------------------------------------------
+// shared pieces
 
-template <int NI>
-__device__ __forceinline__ bool in_iv(uint32_t r, const RowXo& X) {
-    bool s = false;
-    if (NI > 0) {
-#pragma unroll
-        for (int k = 0; k < NI; ++k) s |= (r - X.a[k]) < X.l[k];
-    } else {
-        for (uint32_t k = 0; k < X.niv; ++k) s |= (r - X.iv[k].x) < X.iv[k].y;
-    }
-    return s;
-}
-
-template <bool SR>
-__device__ __forceinline__ uint32_t slot_rank(uint32_t s, const uint16_t* srank, const uint32_t* __restrict__ grank) {
-    return SR ? (uint32_t)srank[s] : __ldg(grank + s);
-}
-
-// One branch-free step of a het-bit chain: classify the lowest bit of h.
-template <int NI, bool SR>
-__device__ __forceinline__ void xo_step(uint32_t& h, uint32_t& m, uint32_t base, const uint16_t* srank,
-                                        const uint32_t* __restrict__ grank, const RowXo& X) {
-    const bool nz = h != 0u;
-    const uint32_t j = nz ? (uint32_t)(__ffs(h) - 1) : 0u;
-    h &= h - 1u;
-    const uint32_t r = slot_rank<SR>(base + j, srank, grank);
-    const bool s = nz && in_iv<NI>(r, X);
-    m |= (uint32_t)s << j;
-}
-
-// Switched-strand masks of the lane's two words: four interleaved 32-bit chains.
-template <int NI, bool SR>
-__device__ __forceinline__ void classify(uint64_t h0, uint64_t h1, uint32_t s0, const uint16_t* srank,
-                                         const uint32_t* __restrict__ grank, const RowXo& X, uint64_t& m0,
-                                         uint64_t& m1) {
-    uint32_t a = (uint32_t)h0, b = (uint32_t)(h0 >> 32), c = (uint32_t)h1, d = (uint32_t)(h1 >> 32);
-    uint32_t ma = 0, mb = 0, mc = 0, md = 0;
-    while (a | b | c | d) {
-        xo_step<NI, SR>(a, ma, s0, srank, grank, X);
-        xo_step<NI, SR>(b, mb, s0 + 32u, srank, grank, X);
-        xo_step<NI, SR>(c, mc, s0 + 64u, srank, grank, X);
-        xo_step<NI, SR>(d, md, s0 + 96u, srank, grank, X);
-    }
-    m0 = (uint64_t)ma | ((uint64_t)mb << 32);
-    m1 = (uint64_t)mc | ((uint64_t)md << 32);
-}
-
-constexpr uint32_t kQueueCap = 512;    // het bits per warp-chunk handled by the balanced path
-
-// Warp-balanced classification of one 64-word chunk.  Each lane pushes the
-// het bits of its two words into the warp's queue (slot, plus bit 31 when the
-// bottom strand carries the allele); the whole warp then classifies the queue
-// four entries per lane at a time, ORs switched bits into the warp's chunk
-// mask and adds +-effect for each switched allele.  H = total het bits.
-template <int NI, bool SR>
-__device__ __forceinline__ void classify_balanced(uint64_t h0, uint64_t h1, uint64_t b0, uint64_t b1, uint32_t w,
-                                                  uint32_t w0, uint32_t off, uint32_t H, uint32_t* Q,
-                                                  uint32_t* SM, const uint16_t* srank,
-                                                  const uint32_t* __restrict__ grank, const RowXo& X,
-                                                  const float4* __restrict__ eff4, bool do_ph,
-                                                  float (&d)[kMaxTraits], uint64_t& m0, uint64_t& m1) {
+// L2 prefetch of [p, p + bytes) in 2 KB pieces, one piece per lane.
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
     const uint32_t lane = threadIdx.x & 31u;
-#pragma unroll
-    for (uint32_t k = 0; k < 4; ++k) SM[4u * lane + k] = 0u;
-    uint32_t q = off;
-    const uint32_t hh[4] = {(uint32_t)h0, (uint32_t)(h0 >> 32), (uint32_t)h1, (uint32_t)(h1 >> 32)};
-    const uint32_t bb[4] = {(uint32_t)b0, (uint32_t)(b0 >> 32), (uint32_t)b1, (uint32_t)(b1 >> 32)};
-#pragma unroll
-    for (uint32_t k = 0; k < 4; ++k) {
-        const uint32_t base = w * 64u + 32u * k;
-        for (uint32_t x = hh[k]; x; x &= x - 1u) {
-            const uint32_t j = (uint32_t)(__ffs(x) - 1);
-            Q[q++] = (base + j) | (((bb[k] >> j) & 1u) << 31);
-        }
+    const uint32_t off = lane * 2048u;
+    if (off < bytes) {
+        const uint32_t n = min(2048u, bytes - off);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(reinterpret_cast<const char*>(p) + off),
+                     "r"(n)
+                     : "memory");
     }
-    __syncwarp();
-    const uint32_t sbase = w0 * 64u;
-    for (uint32_t ib = 0; ib < H; ib += 128u) {
-        uint32_t e[4];
-        bool sw[4];
-#pragma unroll
-        for (uint32_t k = 0; k < 4; ++k) {
-            const uint32_t i = ib + lane + 32u * k;
-            e[k] = (i < H) ? Q[i] : 0u;
-            const uint32_t slot = e[k] & 0x7fffffffu;
-            const uint32_t r = slot_rank<SR>(slot, srank, grank);
-            sw[k] = (i < H) && in_iv<NI>(r, X);
-        }
-#pragma unroll
-        for (uint32_t k = 0; k < 4; ++k) {
-            if (sw[k]) {
-                const uint32_t loc = (e[k] & 0x7fffffffu) - sbase;
-                atomicOr(&SM[loc >> 5], 1u << (loc & 31u));
-            }
-        }
-        if (do_ph) {
-            float4 ef[4];
-#pragma unroll
-            for (uint32_t k = 0; k < 4; ++k)
-                ef[k] = sw[k] ? __ldg(eff4 + (e[k] & 0x7fffffffu)) : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-            for (uint32_t k = 0; k < 4; ++k) {
-                const float g = sw[k] ? ((e[k] >> 31) ? 1.0f : -1.0f) : 0.0f;
-                d[0] = fmaf(g, ef[k].x, d[0]);
-                d[1] = fmaf(g, ef[k].y, d[1]);
-                d[2] = fmaf(g, ef[k].z, d[2]);
-                d[3] = fmaf(g, ef[k].w, d[3]);
-            }
-        }
-    }
-    __syncwarp();
-    m0 = (uint64_t)SM[4u * lane] | ((uint64_t)SM[4u * lane + 1u] << 32);
-    m1 = (uint64_t)SM[4u * lane + 2u] | ((uint64_t)SM[4u * lane + 3u] << 32);
-    __syncwarp();
-}
-
-// Bits of h whose slot position is >= an odd number of the events (direct
-// double compares against the event list; used only for very long lists).
-__device__ __forceinline__ uint64_t sw_mask_events(uint64_t h, uint32_t base, const double* __restrict__ pos,
-                                                   const double* __restrict__ ev, uint32_t E) {
-    uint64_t m = 0;
-    while (h) {
-        const uint32_t j = (uint32_t)(__ffsll((long long)h) - 1);
-        h &= h - 1ull;
-        const double p = __ldg(pos + base + j);
-        uint32_t c = 0;
-        for (uint32_t k = 0; k < E; ++k) c += (__ldg(ev + k) <= p) ? 1u : 0u;
-        m |= (uint64_t)(c & 1u) << j;
-    }
-    return m;
 }
 
 // d += (+1 if the bottom strand brings the allele, -1 if it drops it) * eff
@@ -203,6 +91,22 @@ __device__ __forceinline__ void switched_effects(uint64_t x0, uint64_t x1, uint6
     }
 }
 
+// Bits of h whose slot position is >= an odd number of the events (direct
+// double compares against the event list; used only for very long lists).
+__device__ __forceinline__ uint64_t sw_mask_events(uint64_t h, uint32_t base, const double* __restrict__ pos,
+                                                   const double* __restrict__ ev, uint32_t E) {
+    uint64_t m = 0;
+    while (h) {
+        const uint32_t j = (uint32_t)(__ffsll((long long)h) - 1);
+        h &= h - 1ull;
+        const double p = __ldg(pos + base + j);
+        uint32_t c = 0;
+        for (uint32_t k = 0; k < E; ++k) c += (__ldg(ev + k) <= p) ? 1u : 0u;
+        m |= (uint64_t)(c & 1u) << j;
+    }
+    return m;
+}
+
 // r(e) = #{slots with position < e} through the position buckets.
 __device__ __forceinline__ uint32_t threshold_rank(const PopDev& P, double e) {
     const uint32_t b = pos_bucket(e, P.NB);
@@ -212,9 +116,6 @@ __device__ __forceinline__ uint32_t threshold_rank(const PopDev& P, double e) {
     return r;
 }
 
-// Per-row crossover mode
-enum XoKind : int { kXoCopy = 0, kXoIv4 = 4, kXoIv8 = 8, kXoFar = -1, kXoEvents = -2 };
-
 struct RowArgs {
     const uint64_t* top;
     const uint64_t* bot;
@@ -222,6 +123,8 @@ struct RowArgs {
     uint32_t Wc, Wp;
     uint32_t mc, mo, my_slot;
     uint32_t E;
+    uint32_t topr;
+    double zbase;         // lanes 0..3: z(top strand) - sum(fixed effects), trait = lane
     const double* evg;
     bool philox;
 };
@@ -247,100 +150,39 @@ __device__ __forceinline__ void fold_fs(uint64_t* sF, uint64_t* sV, uint32_t w, 
     if (x1 & ~v.y) atomicOr((unsigned long long*)&sV[w + 1u], (unsigned long long)x1);
 }
 
-template <int KIND, bool SR>
-__device__ __forceinline__ void row_body(const PopDev& P, const DevStatus& st, const RowArgs& R,
-                                         const uint16_t* srank, const uint64_t* sfix, const RowXo& X, uint32_t* Q,
-                                         uint32_t* SM, bool do_mut, bool do_ph, bool do_fs, uint64_t* sF,
-                                         uint64_t* sV, float (&d)[kMaxTraits]) {
-    const uint32_t lane = threadIdx.x & 31u;
-    constexpr bool xo = (KIND != kXoCopy);
-    const float4* eff4 = reinterpret_cast<const float4*>(P.eff);
-    // two chunks of parent words in flight ahead of the one being processed
-    ulonglong2 t_a, b_a, t_b, b_b;
-    load_pair(t_a, b_a, R, 2u * lane, xo);
-    load_pair(t_b, b_b, R, 2u * lane + 64u, xo);
-    for (uint32_t w0 = 0; w0 < R.Wc; w0 += 64u) {
-        const uint32_t w = w0 + 2u * lane;
-        ulonglong2 t_c, b_c;
-        load_pair(t_c, b_c, R, w + 128u, xo);
-        // XOR masks of this lane's two words from the row's new alleles
-        uint64_t mx0 = 0, mx1 = 0;
-        if (do_mut && R.mc) {
-            const uint32_t lim = R.mc < 32u ? R.mc : 32u;
-            for (uint32_t j = 0; j < lim; ++j) {
-                const uint32_t s = __shfl_sync(0xffffffffu, R.my_slot, j);
-                if (s == 0xffffffffu) continue;
-                const uint32_t sw = s >> 6;
-                if (sw == w) mx0 ^= 1ull << (s & 63u);
-                else if (sw == w + 1u) mx1 ^= 1ull << (s & 63u);
-            }
-            for (uint32_t j = 32; j < R.mc; ++j) {  // rows with more than 32 new alleles
-                const uint32_t mi = R.philox ? R.mo + j : P.row_mut[R.mo + j];
-                if (mi >= st.M) continue;
-                const uint32_t s = P.mut_slot[mi];
-                if (s == 0xffffffffu) continue;
-                const uint32_t sw = s >> 6;
-                if (sw == w) mx0 ^= 1ull << (s & 63u);
-                else if (sw == w + 1u) mx1 ^= 1ull << (s & 63u);
-            }
-        }
-        const bool live = w < R.Wc;
-        ulonglong2 fm = make_ulonglong2(0, 0);
-        if (live && w < R.Wp) fm = *reinterpret_cast<const ulonglong2*>(sfix + w);
-        const uint64_t t0 = t_a.x & ~fm.x, t1 = t_a.y & ~fm.y;
-        uint64_t x0 = t0, x1 = t1;
-        if (xo) {
-            const uint64_t b0 = b_a.x & ~fm.x, b1 = b_a.y & ~fm.y;
-            const uint64_t h0 = live ? (t0 ^ b0) : 0ull, h1 = live ? (t1 ^ b1) : 0ull;
-            uint64_t m0, m1;
-            if (KIND != kXoEvents) {
-                // warp prefix of het counts decides between the balanced queue and per-lane chains
-                const uint32_t c = (uint32_t)(__popcll(h0) + __popcll(h1));
-                uint32_t incl = c;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= (uint32_t)o) incl += y;
-                }
-                const uint32_t H = __shfl_sync(0xffffffffu, incl, 31);
-                if (H <= kQueueCap) {
-                    classify_balanced<(KIND > 0 ? KIND : 0), SR>(h0, h1, b0, b1, w, w0, incl - c, H, Q, SM, srank,
-                                                                  P.rank, X, eff4, do_ph, d, m0, m1);
-                } else {
-                    classify<(KIND > 0 ? KIND : 0), SR>(h0, h1, w * 64u, srank, P.rank, X, m0, m1);
-                    if (do_ph) switched_effects(m0, m1, b0, b1, w * 64u, eff4, d);
-                }
-            } else {
-                m0 = sw_mask_events(h0, w * 64u, P.pos, R.evg, R.E);
-                m1 = sw_mask_events(h1, w * 64u + 64u, P.pos, R.evg, R.E);
-                if (do_ph) switched_effects(m0, m1, b0, b1, w * 64u, eff4, d);
-            }
-            x0 = (t0 & ~m0) | (b0 & m0);
-            x1 = (t1 & ~m1) | (b1 & m1);
-        }
-        if (live) {
-            x0 ^= mx0;
-            x1 ^= mx1;
-            *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(x0, x1);
-            if (do_fs) fold_fs(sF, sV, w, x0, x1);
-        }
-        t_a = t_b; b_a = b_b;
-        t_b = t_c; b_b = b_c;
+// XOR masks of the lane's two words (w, w+1) from the row's new alleles.
+// Called by the whole warp (the shuffles need every lane).
+__device__ __forceinline__ void mutation_masks(const PopDev& P, const DevStatus& st, const RowArgs& R, uint32_t w,
+                                               uint64_t& mx0, uint64_t& mx1) {
+    mx0 = 0;
+    mx1 = 0;
+    const uint32_t lim = R.mc < 32u ? R.mc : 32u;
+    for (uint32_t j = 0; j < lim; ++j) {
+        const uint32_t s = __shfl_sync(0xffffffffu, R.my_slot, j);
+        if (s == 0xffffffffu) continue;
+        const uint32_t sw = s >> 6;
+        if (sw == w) mx0 ^= 1ull << (s & 63u);
+        else if (sw == w + 1u) mx1 ^= 1ull << (s & 63u);
+    }
+    for (uint32_t j = 32; j < R.mc; ++j) {  // rows with more than 32 new alleles
+        const uint32_t mi = R.philox ? R.mo + j : P.row_mut[R.mo + j];
+        if (mi >= st.M) continue;
+        const uint32_t s = P.mut_slot[mi];
+        if (s == 0xffffffffu) continue;
+        const uint32_t sw = s >> 6;
+        if (sw == w) mx0 ^= 1ull << (s & 63u);
+        else if (sw == w + 1u) mx1 ^= 1ull << (s & 63u);
     }
 }
 
-// One offspring row, the whole warp.
-template <bool SR>
-__device__ __forceinline__ void gen_row(const PopDev& P, const DevStatus& st, uint32_t g, const uint16_t* srank,
-                                        const uint64_t* sfix, uint2* s_iv, uint32_t* s_thr, uint32_t* Q,
-                                        uint32_t* SM, bool do_mut, bool do_ph, bool do_fs, uint64_t* sF,
-                                        uint64_t* sV) {
+// Parents, strand swap and breakpoint count of gamete g; the new alleles of
+// the row (lanes hold up to 32 slot indices) and their effects.
+__device__ __forceinline__ void row_setup(const PopDev& P, const DevStatus& st, uint32_t g, bool do_mut,
+                                          bool do_ph, bool gather, RowArgs& R, float (&d)[kMaxTraits]) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t* prow = P.rows[st.cur ^ 1u];
-    uint64_t* crow = P.rows[st.cur];
     const bool q1 = (P.flags & 1u) != 0;
     const bool philox = P.mode == kModePhilox;
-    // ---- parent strands and the strand-swap bit of gamete g
     uint32_t pind = P.pairs[g];
     if (pind >= st.pN) {
         if (lane == 0) atomicOr(&P.st->err, kErrParent);
@@ -366,16 +208,610 @@ __device__ __forceinline__ void gen_row(const PopDev& P, const DevStatus& st, ui
         evg = P.ev_pos + e0;
     }
     const uint32_t topr = 2u * pind + (swap ? 1u : 0u);
-    RowArgs R;
+    R.topr = topr;
     R.top = prow + (size_t)topr * P.Wcap;
     R.bot = prow + (size_t)(topr ^ 1u) * P.Wcap;
-    R.out = crow + (size_t)g * P.Wcap;
+    R.out = P.rows[st.cur] + (size_t)g * P.Wcap;
     R.Wc = st.W;
     R.Wp = st.pW;
     R.E = E;
     R.evg = evg;
     R.philox = philox;
+    R.zbase = 0.0;
+    if (do_ph && lane < kMaxTraits)
+        R.zbase = P.zg[st.cur ^ 1u][(size_t)topr * 4u + lane] - P.st->fixsum[lane];
 
+    R.mo = 0;
+    R.mc = 0;
+    R.my_slot = 0xffffffffu;
+    const float4* eff4 = reinterpret_cast<const float4*>(P.eff);
+    if (do_mut) {
+        R.mo = P.row_off[g];
+        R.mc = P.row_off[g + 1u] - R.mo;
+        if (lane < R.mc) {
+            const uint32_t i = R.mo + lane;
+            const uint32_t mi = philox ? i : P.row_mut[i];
+            R.my_slot = (mi < st.M) ? P.mut_slot[mi] : 0xffffffffu;
+            if (gather && R.my_slot != 0xffffffffu) {
+                const float4 e = __ldg(eff4 + R.my_slot);
+                d[0] += e.x; d[1] += e.y; d[2] += e.z; d[3] += e.w;
+            }
+        }
+        if (gather && R.mc > 32u && lane == 0) {
+            for (uint32_t j = 32; j < R.mc; ++j) {
+                const uint32_t mi = philox ? R.mo + j : P.row_mut[R.mo + j];
+                if (mi >= st.M) continue;
+                const uint32_t s = P.mut_slot[mi];
+                if (s == 0xffffffffu) continue;
+                const float4 e = __ldg(eff4 + s);
+                d[0] += e.x; d[1] += e.y; d[2] += e.z; d[3] += e.w;
+            }
+        }
+    }
+}
+
+// Breakpoint k of the row as a double.
+__device__ __forceinline__ double row_event(const PopDev& P, const DevStatus& st, const RowArgs& R, uint32_t g,
+                                            uint32_t k) {
+    if (R.philox) {
+        const U4 a = philox4x32(g, 1u + (k >> 1), st.gen, kStreamGamete, P.seed);
+        return (k & 1u) ? u01(a.z, a.w) : u01(a.x, a.y);
+    }
+    return __ldg(R.evg + k);
+}
+
+// z(child genome g) = z(top strand) - sum(fixed effects) + the row's delta (FP64 warp sum).
+__device__ __forceinline__ void row_phenotype(const PopDev& P, const DevStatus& st, uint32_t g, const RowArgs& R,
+                                              const float (&d)[kMaxTraits]) {
+    const uint32_t lane = threadIdx.x & 31u;
+    double z[kMaxTraits];
+#pragma unroll
+    for (uint32_t t = 0; t < kMaxTraits; ++t) {
+        double v = (double)d[t];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        z[t] = v;
+    }
+    if (lane < kMaxTraits) {
+        const double zz = lane == 0 ? z[0] : lane == 1 ? z[1] : lane == 2 ? z[2] : z[3];
+        P.zg[st.cur][(size_t)g * 4u + lane] = R.zbase + zz;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Suffix-table rows.
+//
+// Setup builds the row's whole switch mask in the warp's mask bitmap (shared
+// memory, one bit per slot): the correction slots of every breakpoint are
+// toggled first, then XOR_k suf[g_k] is folded in, many table loads in flight
+// at a time.  The streaming loop reads (and clears) two mask words per lane
+// per chunk, so it waits on nothing but the parent words, which are loaded
+// two chunks ahead.
+//
+// Effects of switched alleles go through the per-warp queue (slot | sign << 31)
+// and are gathered four per lane.  A row gathers the smaller of two sets: the
+// switched heterozygous bits (z = z(top) + sum (bottom - top) w), or, when the
+// breakpoints switch more than half of the rank space, the unswitched ones
+// (z = z(bottom) + sum (top - bottom) w); both give the same phenotype up to
+// FP32 rounding.
+
+struct WarpSmem {
+    uint32_t q[kQueueCap];            // effect queue: slot | sign << 31
+    uint32_t go[kMaxEvDevice];        // table row offset per event
+    uint32_t rr[kMaxEvDevice];        // rank threshold per event
+};
+
+__device__ __forceinline__ void add4(float (&d)[kMaxTraits], const float4& e) {
+    d[0] += e.x;
+    d[1] += e.y;
+    d[2] += e.z;
+    d[3] += e.w;
+}
+
+__device__ CLOTHO_COLD float4 effects_direct(uint64_t m0, uint64_t m1, uint64_t b0, uint64_t b1, uint32_t s0,
+                                              const float4* __restrict__ eff4) {
+    float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
+    switched_effects(m0, m1, b0, b1, s0, eff4, d);
+    return make_float4(d[0], d[1], d[2], d[3]);
+}
+
+#ifndef CLOTHO_ROUND_LANE
+#define CLOTHO_ROUND_LANE 4
+#endif
+#ifndef CLOTHO_TABLE_INFLIGHT
+#define CLOTHO_TABLE_INFLIGHT 16
+#endif
+constexpr uint32_t kRoundLane = CLOTHO_ROUND_LANE;   // queue entries gathered per lane per round
+constexpr uint32_t kRound = 32u * kRoundLane;
+constexpr uint32_t kTableInflight = CLOTHO_TABLE_INFLIGHT;
+
+// Effects of queue entries [head, head + n), n <= kRound, kRoundLane per lane.
+__device__ __forceinline__ void effq_round(const uint32_t* Q, uint32_t head, uint32_t n,
+                                           const float4* __restrict__ eff4, float (&d)[kMaxTraits]) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t e[kRoundLane];
+    bool ok[kRoundLane];
+#pragma unroll
+    for (uint32_t k = 0; k < kRoundLane; ++k) {
+        const uint32_t i = lane + 32u * k;
+        ok[k] = i < n;
+        e[k] = ok[k] ? Q[(head + i) & (kQueueCap - 1u)] : 0u;
+    }
+    float4 ef[kRoundLane];
+#pragma unroll
+    for (uint32_t k = 0; k < kRoundLane; ++k)
+        ef[k] = ok[k] ? __ldg(eff4 + (e[k] & 0x7fffffffu)) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (uint32_t k = 0; k < kRoundLane; ++k) {
+        const float s = ok[k] ? ((e[k] >> 31) ? 1.0f : -1.0f) : 0.0f;
+        d[0] = fmaf(s, ef[k].x, d[0]);
+        d[1] = fmaf(s, ef[k].y, d[1]);
+        d[2] = fmaf(s, ef[k].z, d[2]);
+        d[3] = fmaf(s, ef[k].w, d[3]);
+    }
+}
+
+// Queue the gathered bits (g0, g1) of the lane's words w, w+1 (sign +1 where
+// s0/s1 has the bit) and gather every complete round.
+__device__ __forceinline__ void effq_push(uint64_t g0, uint64_t g1, uint64_t s0, uint64_t s1, uint32_t w,
+                                          uint32_t* Q, uint32_t& head, uint32_t& tail,
+                                          const float4* __restrict__ eff4, float (&d)[kMaxTraits]) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t c = (uint32_t)(__popcll(g0) + __popcll(g1));
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    const uint32_t H = __shfl_sync(0xffffffffu, incl, 31);
+    if (H == 0u) return;
+    if (H > kQueueCap - kRound) {  // denser than the queue takes: per-lane chains
+        add4(d, effects_direct(g0, g1, s0, s1, w * 64u, eff4));
+        return;
+    }
+    uint32_t i = tail + incl - c;
+    uint64_t x0 = g0, x1 = g1;
+    while (x0 | x1) {
+        const bool lo = x0 != 0ull;
+        const uint64_t x = lo ? x0 : x1;
+        const uint32_t j = (uint32_t)(__ffsll((long long)x) - 1);
+        const uint32_t sb = (uint32_t)(((lo ? s0 : s1) >> j) & 1ull);
+        Q[i & (kQueueCap - 1u)] = (w * 64u + (lo ? 0u : 64u) + j) | (sb << 31);
+        ++i;
+        const uint64_t xc = x & (x - 1ull);
+        if (lo) x0 = xc; else x1 = xc;
+    }
+    tail += H;
+    __syncwarp();
+    while (tail - head >= kRound) {
+        effq_round(Q, head, kRound, eff4, d);
+        head += kRound;
+    }
+    __syncwarp();
+}
+
+__device__ CLOTHO_COLD ulonglong2 mutation_masks_tail(const PopDev& P, uint32_t M, uint32_t mo, uint32_t mc,
+                                                       bool philox, uint32_t w) {
+    ulonglong2 x = make_ulonglong2(0, 0);
+    for (uint32_t j = 32; j < mc; ++j) {  // rows with more than 32 new alleles
+        const uint32_t mi = philox ? mo + j : P.row_mut[mo + j];
+        if (mi >= M) continue;
+        const uint32_t s = P.mut_slot[mi];
+        if (s == 0xffffffffu) continue;
+        const uint32_t sw = s >> 6;
+        if (sw == w) x.x ^= 1ull << (s & 63u);
+        else if (sw == w + 1u) x.y ^= 1ull << (s & 63u);
+    }
+    return x;
+}
+
+// XOR masks of the lane's words w, w+1 from the row's new alleles (whole warp).
+__device__ __forceinline__ void row_mutations(const PopDev& P, uint32_t M, const RowArgs& R, uint32_t w,
+                                              uint64_t& mx0, uint64_t& mx1) {
+    mx0 = 0;
+    mx1 = 0;
+    const uint32_t lim = R.mc < 32u ? R.mc : 32u;
+    for (uint32_t j = 0; j < lim; ++j) {
+        const uint32_t s = __shfl_sync(0xffffffffu, R.my_slot, j);
+        if (s == 0xffffffffu) continue;
+        const uint32_t sw = s >> 6;
+        if (sw == w) mx0 ^= 1ull << (s & 63u);
+        else if (sw == w + 1u) mx1 ^= 1ull << (s & 63u);
+    }
+    if (R.mc > 32u) {
+        const ulonglong2 x = mutation_masks_tail(P, M, R.mo, R.mc, R.philox, w);
+        mx0 ^= x.x;
+        mx1 ^= x.y;
+    }
+}
+
+// Copy rows (no breakpoint): the top strand with the fixed columns cleared and
+// the new alleles added; the bottom-strand registers of the crossover loop
+// hold more of the top strand here, six chunks ahead.
+__device__ __forceinline__ void row_body_copy(const PopDev& P, uint32_t M, const RowArgs& R, const uint64_t* sfix,
+                                              bool do_mut, bool do_fs, uint64_t* sF, uint64_t* sV) {
+    const uint32_t lane = threadIdx.x & 31u;
+    constexpr uint32_t D = 6;
+    ulonglong2 t[D];
+#pragma unroll
+    for (uint32_t j = 0; j < D; ++j) {
+        const uint32_t w = 2u * lane + 64u * j;
+        t[j] = (w < R.Wp) ? __ldg(reinterpret_cast<const ulonglong2*>(R.top + w)) : make_ulonglong2(0, 0);
+    }
+    for (uint32_t w0 = 0; w0 < R.Wc; w0 += 64u) {
+        const uint32_t w = w0 + 2u * lane;
+        const ulonglong2 cur = t[0];
+#pragma unroll
+        for (uint32_t j = 0; j + 1 < D; ++j) t[j] = t[j + 1];
+        const uint32_t wn = w + 64u * D;
+        t[D - 1] = (wn < R.Wp) ? __ldg(reinterpret_cast<const ulonglong2*>(R.top + wn)) : make_ulonglong2(0, 0);
+        uint64_t mx0 = 0, mx1 = 0;
+        if (do_mut && R.mc) row_mutations(P, M, R, w, mx0, mx1);
+        if (w < R.Wc) {
+            ulonglong2 fm = make_ulonglong2(0, 0);
+            if (w < R.Wp) fm = *reinterpret_cast<const ulonglong2*>(sfix + w);
+            const uint64_t x0 = (cur.x & ~fm.x) ^ mx0, x1 = (cur.y & ~fm.y) ^ mx1;
+            *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(x0, x1);
+            if (do_fs) fold_fs(sF, sV, w, x0, x1);
+        }
+    }
+}
+
+// Crossover rows.  MODE 0: switch mask from the warp's mask bitmap; MODE 1:
+// direct event compares (tape rows with more than kMaxEvDevice events).
+template <int MODE>
+__device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const RowArgs& R, const uint64_t* sfix,
+                                             uint64_t* mask, uint32_t* Q, bool inv, bool do_mut, bool gather,
+                                             bool do_fs, uint64_t* sF, uint64_t* sV, float (&d)[kMaxTraits]) {
+    const uint32_t lane = threadIdx.x & 31u;
+    constexpr bool xo = true;
+    const float4* eff4 = reinterpret_cast<const float4*>(P.eff);
+    uint32_t qh = 0, qt = 0;
+    ulonglong2 t_a, b_a, t_b, b_b;
+    load_pair(t_a, b_a, R, 2u * lane, xo);
+    load_pair(t_b, b_b, R, 2u * lane + 64u, xo);
+    for (uint32_t w0 = 0; w0 < R.Wc; w0 += 64u) {
+        const uint32_t w = w0 + 2u * lane;
+        ulonglong2 t_c, b_c;
+        load_pair(t_c, b_c, R, w + 128u, xo);
+        uint64_t mx0 = 0, mx1 = 0;
+        if (do_mut && R.mc) row_mutations(P, M, R, w, mx0, mx1);
+        const bool live = w < R.Wc;
+        ulonglong2 fm = make_ulonglong2(0, 0);
+        if (live && w < R.Wp) fm = *reinterpret_cast<const ulonglong2*>(sfix + w);
+        const uint64_t t0 = t_a.x & ~fm.x, t1 = t_a.y & ~fm.y;
+        uint64_t x0, x1;
+        {
+            const uint64_t b0 = b_a.x & ~fm.x, b1 = b_a.y & ~fm.y;
+            const uint64_t h0 = live ? (t0 ^ b0) : 0ull, h1 = live ? (t1 ^ b1) : 0ull;
+            uint64_t m0 = 0, m1 = 0;
+            if (MODE == 0) {
+                if (live) {
+                    ulonglong2* mw = reinterpret_cast<ulonglong2*>(mask + w);
+                    const ulonglong2 m = *mw;
+                    *mw = make_ulonglong2(0, 0);
+                    m0 = m.x;
+                    m1 = m.y;
+                }
+            } else {
+                m0 = sw_mask_events(h0, w * 64u, P.pos, R.evg, R.E);
+                m1 = sw_mask_events(h1, w * 64u + 64u, P.pos, R.evg, R.E);
+            }
+            const uint64_t sw0 = m0 & h0, sw1 = m1 & h1;
+            x0 = t0 ^ sw0;
+            x1 = t1 ^ sw1;
+            if (gather)
+                effq_push(inv ? (h0 ^ sw0) : sw0, inv ? (h1 ^ sw1) : sw1, inv ? t0 : b0, inv ? t1 : b1, w, Q, qh, qt,
+                          eff4, d);
+        }
+        if (live) {
+            x0 ^= mx0;
+            x1 ^= mx1;
+            *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(x0, x1);
+            if (do_fs) fold_fs(sF, sV, w, x0, x1);
+        }
+        t_a = t_b; b_a = b_b;
+        t_b = t_c; b_b = b_c;
+    }
+    if (gather && qt != qh) {
+        effq_round(Q, qh, qt - qh, eff4, d);
+        __syncwarp();
+    }
+}
+
+__device__ CLOTHO_COLD float4 row_body_events(const PopDev& P, uint32_t M, const RowArgs R, const uint64_t* sfix,
+                                               uint32_t* Q, bool do_mut, bool gather, bool do_fs, uint64_t* sF,
+                                               uint64_t* sV) {
+    float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
+    row_body_suf<1>(P, M, R, sfix, nullptr, Q, false, do_mut, gather, do_fs, sF, sV, d);
+    return make_float4(d[0], d[1], d[2], d[3]);
+}
+
+// Nearest suffix-table row b (a multiple of 64) of rank threshold r and the
+// ranks between them: [c0, c0 + n), n <= 32.
+__device__ __forceinline__ uint32_t table_row(uint32_t r, uint32_t A, uint32_t& c0, uint32_t& n) {
+    const uint32_t lo = r & ~63u;
+    const uint32_t b = (r - lo <= 32u) ? lo : lo + 64u;
+    c0 = min(r, b);
+    n = min(max(r, b), A) - c0;
+    return b;
+}
+
+// One offspring row, the whole warp (suffix-table classifier).
+__device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st, uint32_t g, const uint64_t* sfix,
+                                            uint64_t* mask, WarpSmem& ws, bool do_mut, bool do_ph, bool gather,
+                                            bool do_fs, uint64_t* sF, uint64_t* sV) {
+    const uint32_t lane = threadIdx.x & 31u;
+    RowArgs R;
+    float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
+    row_setup(P, st, g, do_mut, do_ph, gather, R, d);
+    prefetch_l2(R.top, R.Wp * 8u);
+    if (R.E > 0) prefetch_l2(R.bot, R.Wp * 8u);
+    const uint32_t E = R.E;
+    bool inv = false;
+    if (E > kMaxEvDevice) {
+        add4(d, row_body_events(P, st.M, R, sfix, ws.q, do_mut, gather, do_fs, sF, sV));
+    } else if (E > 0) {
+        const uint32_t A = st.A;
+        for (uint32_t k = lane; k < E; k += 32u) {
+            const uint32_t r = threshold_rank(P, row_event(P, st, R, g, k));
+            uint32_t c0, n;
+            ws.go[k] = (table_row(r, A, c0, n) >> 6) * P.Wcap;
+            ws.rr[k] = r;
+        }
+        __syncwarp();
+        // corrections: toggle the slots whose rank lies between threshold and table row
+        uint32_t* m32 = reinterpret_cast<uint32_t*>(mask);
+#pragma unroll 4
+        for (uint32_t k = 0; k < E; ++k) {
+            uint32_t c0, n;
+            table_row(ws.rr[k], A, c0, n);
+            if (lane < n) {
+                const uint32_t s = __ldg(P.inv + c0 + lane);
+                atomicXor(m32 + (s >> 5), 1u << (s & 31u));
+            }
+        }
+        // switched share of the rank space: the sorted thresholds pair into intervals
+        if (gather) {
+            int32_t len = 0;
+            for (uint32_t k = lane; k < E; k += 32u) {
+                const uint32_t rk = ws.rr[k];
+                uint32_t posn = 0;
+                for (uint32_t j = 0; j < E; ++j) {
+                    const uint32_t rj = ws.rr[j];
+                    posn += (rj < rk || (rj == rk && j < k)) ? 1u : 0u;
+                }
+                len += (posn & 1u) ? (int32_t)rk : -(int32_t)rk;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) len += __shfl_xor_sync(0xffffffffu, len, o);
+            if (E & 1u) len += (int32_t)A;
+            inv = 2 * (int64_t)len > (int64_t)A;
+            if (inv && lane < kMaxTraits)
+                R.zbase = P.zg[st.cur ^ 1u][(size_t)(R.topr ^ 1u) * 4u + lane] - P.st->fixsum[lane];
+        }
+        __syncwarp();
+        // XOR of the events' table rows, kTableInflight 16-byte loads per lane in flight
+        const uint64_t* __restrict__ suf = P.suf;
+        ulonglong2* m2 = reinterpret_cast<ulonglong2*>(mask);
+        for (uint32_t k = 0; k < E; ++k) {
+            const uint64_t* tk = suf + ws.go[k];
+            for (uint32_t wb = 0; wb < R.Wp; wb += 64u * kTableInflight) {
+                ulonglong2 v[kTableInflight];
+#pragma unroll
+                for (uint32_t j = 0; j < kTableInflight; ++j) {
+                    const uint32_t w = wb + 64u * j + 2u * lane;
+                    v[j] = (w < R.Wp) ? __ldg(reinterpret_cast<const ulonglong2*>(tk + w)) : make_ulonglong2(0, 0);
+                }
+#pragma unroll
+                for (uint32_t j = 0; j < kTableInflight; ++j) {
+                    const uint32_t w = wb + 64u * j + 2u * lane;
+                    if (w < R.Wp) {
+                        ulonglong2 x = m2[w >> 1];
+                        x.x ^= v[j].x;
+                        x.y ^= v[j].y;
+                        m2[w >> 1] = x;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    }
+    if (E == 0) row_body_copy(P, st.M, R, sfix, do_mut, do_fs, sF, sV);
+    else if (E <= kMaxEvDevice) row_body_suf<0>(P, st.M, R, sfix, mask, ws.q, inv, do_mut, gather, do_fs, sF, sV, d);
+    if (do_ph) row_phenotype(P, st, g, R, d);
+}
+
+// ---------------------------------------------------------------------------
+// Interval classifier (allele spaces beyond the suffix table).
+
+// Sorted breakpoint thresholds of one gamete as half-open rank intervals:
+// a het bit switches strand iff its slot rank lies in one of them.
+struct RowXo {
+    uint32_t a[kMaxIv];   // interval start (rank)
+    uint32_t l[kMaxIv];   // length; 0 = empty
+    const uint2* iv;      // the same intervals in shared memory (any count)
+    uint32_t niv;
+};
+
+template <int NI>
+__device__ __forceinline__ bool in_iv(uint32_t r, const RowXo& X) {
+    bool s = false;
+    if (NI > 0) {
+#pragma unroll
+        for (int k = 0; k < NI; ++k) s |= (r - X.a[k]) < X.l[k];
+    } else {
+        for (uint32_t k = 0; k < X.niv; ++k) s |= (r - X.iv[k].x) < X.iv[k].y;
+    }
+    return s;
+}
+
+// One branch-free step of a het-bit chain: classify the lowest bit of h.
+template <int NI>
+__device__ __forceinline__ void xo_step(uint32_t& h, uint32_t& m, uint32_t base, const uint32_t* __restrict__ grank,
+                                        const RowXo& X) {
+    const bool nz = h != 0u;
+    const uint32_t j = nz ? (uint32_t)(__ffs(h) - 1) : 0u;
+    h &= h - 1u;
+    const uint32_t r = __ldg(grank + base + j);
+    const bool s = nz && in_iv<NI>(r, X);
+    m |= (uint32_t)s << j;
+}
+
+// Switched-strand masks of the lane's two words: four interleaved 32-bit chains.
+template <int NI>
+__device__ __forceinline__ void classify(uint64_t h0, uint64_t h1, uint32_t s0, const uint32_t* __restrict__ grank,
+                                         const RowXo& X, uint64_t& m0, uint64_t& m1) {
+    uint32_t a = (uint32_t)h0, b = (uint32_t)(h0 >> 32), c = (uint32_t)h1, d = (uint32_t)(h1 >> 32);
+    uint32_t ma = 0, mb = 0, mc = 0, md = 0;
+    while (a | b | c | d) {
+        xo_step<NI>(a, ma, s0, grank, X);
+        xo_step<NI>(b, mb, s0 + 32u, grank, X);
+        xo_step<NI>(c, mc, s0 + 64u, grank, X);
+        xo_step<NI>(d, md, s0 + 96u, grank, X);
+    }
+    m0 = (uint64_t)ma | ((uint64_t)mb << 32);
+    m1 = (uint64_t)mc | ((uint64_t)md << 32);
+}
+
+// Warp-balanced classification of one 64-word chunk: the het bits of the
+// warp go through the queue, four per lane; switched bits are ORed into the
+// warp's chunk mask SM and their effects gathered.  H = total het bits (<= kQueueCap).
+template <int NI>
+__device__ __forceinline__ void classify_balanced(uint64_t h0, uint64_t h1, uint64_t b0, uint64_t b1, uint32_t w,
+                                                  uint32_t w0, uint32_t off, uint32_t H, uint32_t* Q,
+                                                  uint32_t* SM, const uint32_t* __restrict__ grank, const RowXo& X,
+                                                  const float4* __restrict__ eff4, bool gather,
+                                                  float (&d)[kMaxTraits], uint64_t& m0, uint64_t& m1) {
+    const uint32_t lane = threadIdx.x & 31u;
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) SM[4u * lane + k] = 0u;
+    uint32_t q = off;
+    const uint32_t hh[4] = {(uint32_t)h0, (uint32_t)(h0 >> 32), (uint32_t)h1, (uint32_t)(h1 >> 32)};
+    const uint32_t bb[4] = {(uint32_t)b0, (uint32_t)(b0 >> 32), (uint32_t)b1, (uint32_t)(b1 >> 32)};
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) {
+        const uint32_t base = w * 64u + 32u * k;
+        for (uint32_t x = hh[k]; x; x &= x - 1u) {
+            const uint32_t j = (uint32_t)(__ffs(x) - 1);
+            Q[q++] = (base + j) | (((bb[k] >> j) & 1u) << 31);
+        }
+    }
+    __syncwarp();
+    const uint32_t sbase = w0 * 64u;
+    for (uint32_t ib = 0; ib < H; ib += 128u) {
+        uint32_t e[4];
+        bool sw[4];
+#pragma unroll
+        for (uint32_t k = 0; k < 4; ++k) {
+            const uint32_t i = ib + lane + 32u * k;
+            e[k] = (i < H) ? Q[i] : 0u;
+            const uint32_t r = __ldg(grank + (e[k] & 0x7fffffffu));
+            sw[k] = (i < H) && in_iv<NI>(r, X);
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < 4; ++k) {
+            if (sw[k]) {
+                const uint32_t loc = (e[k] & 0x7fffffffu) - sbase;
+                atomicOr(&SM[loc >> 5], 1u << (loc & 31u));
+            }
+        }
+        if (gather) {
+            float4 ef[4];
+#pragma unroll
+            for (uint32_t k = 0; k < 4; ++k)
+                ef[k] = sw[k] ? __ldg(eff4 + (e[k] & 0x7fffffffu)) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (uint32_t k = 0; k < 4; ++k) {
+                const float g = sw[k] ? ((e[k] >> 31) ? 1.0f : -1.0f) : 0.0f;
+                d[0] = fmaf(g, ef[k].x, d[0]);
+                d[1] = fmaf(g, ef[k].y, d[1]);
+                d[2] = fmaf(g, ef[k].z, d[2]);
+                d[3] = fmaf(g, ef[k].w, d[3]);
+            }
+        }
+    }
+    __syncwarp();
+    m0 = (uint64_t)SM[4u * lane] | ((uint64_t)SM[4u * lane + 1u] << 32);
+    m1 = (uint64_t)SM[4u * lane + 2u] | ((uint64_t)SM[4u * lane + 3u] << 32);
+    __syncwarp();
+}
+
+// Per-row crossover mode of the interval classifier
+enum XoKind : int { kXoCopy = 0, kXoIv4 = 4, kXoIv8 = 8, kXoFar = -1, kXoEvents = -2 };
+
+template <int KIND>
+__device__ __forceinline__ void row_body_iv(const PopDev& P, const DevStatus& st, const RowArgs& R,
+                                            const uint64_t* sfix, const RowXo& X, uint32_t* Q, uint32_t* SM,
+                                            bool do_mut, bool gather, bool do_fs, uint64_t* sF, uint64_t* sV,
+                                            float (&d)[kMaxTraits]) {
+    const uint32_t lane = threadIdx.x & 31u;
+    constexpr bool xo = (KIND != kXoCopy);
+    const float4* eff4 = reinterpret_cast<const float4*>(P.eff);
+    ulonglong2 t_a, b_a, t_b, b_b;
+    load_pair(t_a, b_a, R, 2u * lane, xo);
+    load_pair(t_b, b_b, R, 2u * lane + 64u, xo);
+    for (uint32_t w0 = 0; w0 < R.Wc; w0 += 64u) {
+        const uint32_t w = w0 + 2u * lane;
+        ulonglong2 t_c, b_c;
+        load_pair(t_c, b_c, R, w + 128u, xo);
+        uint64_t mx0 = 0, mx1 = 0;
+        if (do_mut && R.mc) mutation_masks(P, st, R, w, mx0, mx1);
+        const bool live = w < R.Wc;
+        ulonglong2 fm = make_ulonglong2(0, 0);
+        if (live && w < R.Wp) fm = *reinterpret_cast<const ulonglong2*>(sfix + w);
+        const uint64_t t0 = t_a.x & ~fm.x, t1 = t_a.y & ~fm.y;
+        uint64_t x0 = t0, x1 = t1;
+        if (xo) {
+            const uint64_t b0 = b_a.x & ~fm.x, b1 = b_a.y & ~fm.y;
+            const uint64_t h0 = live ? (t0 ^ b0) : 0ull, h1 = live ? (t1 ^ b1) : 0ull;
+            uint64_t m0, m1;
+            if (KIND != kXoEvents) {
+                // warp prefix of het counts decides between the balanced queue and per-lane chains
+                const uint32_t c = (uint32_t)(__popcll(h0) + __popcll(h1));
+                uint32_t incl = c;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= (uint32_t)o) incl += y;
+                }
+                const uint32_t H = __shfl_sync(0xffffffffu, incl, 31);
+                if (H <= kQueueCap) {
+                    classify_balanced<(KIND > 0 ? KIND : 0)>(h0, h1, b0, b1, w, w0, incl - c, H, Q, SM, P.rank, X,
+                                                             eff4, gather, d, m0, m1);
+                } else {
+                    classify<(KIND > 0 ? KIND : 0)>(h0, h1, w * 64u, P.rank, X, m0, m1);
+                    if (gather) switched_effects(m0, m1, b0, b1, w * 64u, eff4, d);
+                }
+            } else {
+                m0 = sw_mask_events(h0, w * 64u, P.pos, R.evg, R.E);
+                m1 = sw_mask_events(h1, w * 64u + 64u, P.pos, R.evg, R.E);
+                if (gather) switched_effects(m0, m1, b0, b1, w * 64u, eff4, d);
+            }
+            x0 = (t0 & ~m0) | (b0 & m0);
+            x1 = (t1 & ~m1) | (b1 & m1);
+        }
+        if (live) {
+            x0 ^= mx0;
+            x1 ^= mx1;
+            *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(x0, x1);
+            if (do_fs) fold_fs(sF, sV, w, x0, x1);
+        }
+        t_a = t_b; b_a = b_b;
+        t_b = t_c; b_b = b_c;
+    }
+}
+
+// One offspring row, the whole warp (interval classifier).
+__device__ __forceinline__ void gen_row_iv(const PopDev& P, const DevStatus& st, uint32_t g, const uint64_t* sfix,
+                                           uint2* s_iv, uint32_t* s_thr, uint32_t* Q, uint32_t* SM, bool do_mut,
+                                           bool do_ph, bool gather, bool do_fs, uint64_t* sF, uint64_t* sV) {
+    const uint32_t lane = threadIdx.x & 31u;
+    RowArgs R;
+    float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
+    row_setup(P, st, g, do_mut, do_ph, gather, R, d);
+    const uint32_t E = R.E;
     // ---- breakpoints -> sorted rank thresholds -> intervals
     RowXo X;
 #pragma unroll
@@ -384,16 +820,7 @@ __device__ __forceinline__ void gen_row(const PopDev& P, const DevStatus& st, ui
     X.niv = 0;
     int kind = kXoCopy;
     if (E > 0 && E <= kMaxEvDevice) {
-        for (uint32_t k = lane; k < E; k += 32u) {
-            double e;
-            if (philox) {
-                const U4 a = philox4x32(g, 1u + (k >> 1), st.gen, kStreamGamete, P.seed);
-                e = (k & 1u) ? u01(a.z, a.w) : u01(a.x, a.y);
-            } else {
-                e = __ldg(evg + k);
-            }
-            s_thr[k] = threshold_rank(P, e);
-        }
+        for (uint32_t k = lane; k < E; k += 32u) s_thr[k] = threshold_rank(P, row_event(P, st, R, g, k));
         __syncwarp();
         // stable rank sort of the thresholds
         uint32_t mine[4], posn[4];
@@ -440,80 +867,42 @@ __device__ __forceinline__ void gen_row(const PopDev& P, const DevStatus& st, ui
     } else if (E > kMaxEvDevice) {
         kind = kXoEvents;  // tape rows with very long event lists
     }
-
-    // ---- new alleles of this row (slot indices), lanes hold up to 32
-    R.mo = 0;
-    R.mc = 0;
-    R.my_slot = 0xffffffffu;
-    float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
-    const float4* eff4 = reinterpret_cast<const float4*>(P.eff);
-    if (do_mut) {
-        R.mo = P.row_off[g];
-        R.mc = P.row_off[g + 1u] - R.mo;
-        if (lane < R.mc) {
-            const uint32_t i = R.mo + lane;
-            const uint32_t mi = philox ? i : P.row_mut[i];
-            R.my_slot = (mi < st.M) ? P.mut_slot[mi] : 0xffffffffu;
-            if (do_ph && R.my_slot != 0xffffffffu) {
-                const float4 e = __ldg(eff4 + R.my_slot);
-                d[0] += e.x; d[1] += e.y; d[2] += e.z; d[3] += e.w;
-            }
-        }
-        if (do_ph && R.mc > 32u && lane == 0) {
-            for (uint32_t j = 32; j < R.mc; ++j) {
-                const uint32_t mi = philox ? R.mo + j : P.row_mut[R.mo + j];
-                if (mi >= st.M) continue;
-                const uint32_t s = P.mut_slot[mi];
-                if (s == 0xffffffffu) continue;
-                const float4 e = __ldg(eff4 + s);
-                d[0] += e.x; d[1] += e.y; d[2] += e.z; d[3] += e.w;
-            }
-        }
-    }
-
     switch (kind) {
-        case kXoCopy: row_body<kXoCopy, SR>(P, st, R, srank, sfix, X, Q, SM, do_mut, do_ph, do_fs, sF, sV, d); break;
-        case kXoIv4: row_body<kXoIv4, SR>(P, st, R, srank, sfix, X, Q, SM, do_mut, do_ph, do_fs, sF, sV, d); break;
-        case kXoIv8: row_body<kXoIv8, SR>(P, st, R, srank, sfix, X, Q, SM, do_mut, do_ph, do_fs, sF, sV, d); break;
-        case kXoFar: row_body<kXoFar, SR>(P, st, R, srank, sfix, X, Q, SM, do_mut, do_ph, do_fs, sF, sV, d); break;
-        default: row_body<kXoEvents, SR>(P, st, R, srank, sfix, X, Q, SM, do_mut, do_ph, do_fs, sF, sV, d); break;
+        case kXoCopy: row_body_iv<kXoCopy>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, sF, sV, d); break;
+        case kXoIv4: row_body_iv<kXoIv4>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, sF, sV, d); break;
+        case kXoIv8: row_body_iv<kXoIv8>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, sF, sV, d); break;
+        case kXoFar: row_body_iv<kXoFar>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, sF, sV, d); break;
+        default: row_body_iv<kXoEvents>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, sF, sV, d); break;
     }
-    if (do_ph) {
-        double z[kMaxTraits];
-#pragma unroll
-        for (uint32_t t = 0; t < kMaxTraits; ++t) {
-            double v = (double)d[t];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            z[t] = v;
-        }
-        if (lane < kMaxTraits) {
-            const double zt = P.zg[st.cur ^ 1u][(size_t)topr * 4u + lane];
-            const double zz = lane == 0 ? z[0] : lane == 1 ? z[1] : lane == 2 ? z[2] : z[3];
-            P.zg[st.cur][(size_t)g * 4u + lane] = (zt - P.st->fixsum[lane]) + zz;
-        }
-    }
+    if (do_ph) row_phenotype(P, st, g, R, d);
 }
 
 }  // namespace
 
 // Dynamic shared memory: [AND acc: maxW][OR acc: maxW][fixed mask: maxW] u64,
-// then (SR) the slot ranks as u16 [maxR].
-template <bool SR>
+// then (SUF) the warps' mask bitmaps and one WarpSmem per warp.  With gacc set (rows
+// too wide for that layout) the AND/OR fold goes to the population's global
+// accumulators and the fixed mask is read from global memory.
+template <bool SUF>
 __global__ void __launch_bounds__(kGenThreads, 1)
 k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restrict__ ctl, uint32_t fuse,
-             int profile, uint32_t maxW, uint32_t maxR) {
+             int profile, uint32_t maxW, uint32_t gacc) {
     extern __shared__ __align__(16) uint64_t s_dyn[];
-    __shared__ uint2 s_iv[kWarps][kMaxIvSmem];
-    __shared__ uint32_t s_thr[kWarps][kMaxEvDevice];
-    __shared__ uint32_t s_q[kWarps][kQueueCap];
-    __shared__ uint32_t s_sm[kWarps][128];
+    constexpr uint32_t kIvWarps = SUF ? 1 : kWarps;  // interval-classifier state, unused by the suffix table
+    __shared__ uint2 s_iv[kIvWarps][kMaxIvSmem];
+    __shared__ uint32_t s_thr[kIvWarps][kMaxEvDevice];
+    __shared__ uint32_t s_q[kIvWarps][kQueueCap];
+    __shared__ uint32_t s_sm[kIvWarps][128];
     __shared__ uint32_t s_item, s_next;
     uint64_t* sF = s_dyn;
     uint64_t* sV = s_dyn + maxW;
     uint64_t* sfix = s_dyn + 2u * maxW;
-    uint16_t* srank = reinterpret_cast<uint16_t*>(s_dyn + 3u * maxW);
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    // SUF: per-warp mask bitmaps [kWarps][maxW] u64, then one WarpSmem per warp
+    uint64_t* mask = s_dyn + (3u + (SUF ? warp : 0u)) * maxW;
+    WarpSmem& ws = reinterpret_cast<WarpSmem*>(s_dyn + (3u + kWarps) * maxW)[SUF ? warp : 0u];
+    if (SUF)
+        for (uint32_t w = lane; w < maxW; w += 32u) mask[w] = 0ull;
     const bool do_mut = (fuse & kFuseMut) != 0, do_ph = (fuse & kFusePheno) != 0, do_fs = (fuse & kFuseFs) != 0;
     int cur_pop = -1;
     uint32_t cur_W = 0;
@@ -538,7 +927,12 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
         }
         const PopDev& P = pops[p];
         const DevStatus st = *P.st;
-        if ((int)p != cur_pop) {
+        if ((int)p != cur_pop && gacc) {
+            cur_pop = (int)p;
+            sF = P.accF;
+            sV = P.accV;
+            sfix = P.fixmask;
+        } else if ((int)p != cur_pop) {
             if (cur_pop >= 0 && do_fs) {
                 const PopDev& Q = pops[cur_pop];
                 for (uint32_t w = threadIdx.x; w < cur_W; w += blockDim.x) {
@@ -552,27 +946,35 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             if (do_fs)
                 for (uint32_t w = threadIdx.x; w < cur_W; w += blockDim.x) { sF[w] = ~0ull; sV[w] = 0ull; }
             for (uint32_t w = threadIdx.x; w < st.pW; w += blockDim.x) sfix[w] = P.fixmask[w];
-            if (SR)
-                for (uint32_t s = threadIdx.x; s < st.A && s < maxR; s += blockDim.x) srank[s] = (uint16_t)P.rank[s];
             __syncthreads();
         }
+        // all effects zero: the gathered sums are exactly zero, skip them
+        const bool gather = do_ph && st.nz_eff != 0;
         const uint32_t S = 2u * st.N;
         const uint32_t rpi = ctl->rows_per_item ? ctl->rows_per_item : kRowsPerItem;
         const uint32_t r0 = (item - ctl->item_base[p]) * rpi;
         const uint32_t r1 = min(S, r0 + rpi);
+        const uint32_t Se = (S + 1u) >> 1;
         for (;;) {
             uint32_t k = 0;
             if (lane == 0) k = atomicAdd(&s_next, 1u);
-            const uint32_t g = r0 + __shfl_sync(0xffffffffu, k, 0);
-            if (g >= r1) break;
-            gen_row<SR>(P, st, g, srank, sfix, s_iv[warp], s_thr[warp], s_q[warp], s_sm[warp], do_mut, do_ph, do_fs,
-                        sF, sV);
+            const uint32_t v = r0 + __shfl_sync(0xffffffffu, k, 0);
+            if (v >= r1) break;
+            // even gametes first, then odd ones: the second gamete of a mate pair
+            // is a copy row under the reference's crossover rule, so a CTA runs
+            // one kind of row at a time
+            const uint32_t g = v < Se ? 2u * v : 2u * (v - Se) + 1u;
+            if (SUF)
+                gen_row_suf(P, st, g, sfix, mask, ws, do_mut, do_ph, gather, do_fs, sF, sV);
+            else
+                gen_row_iv(P, st, g, sfix, s_iv[warp], s_thr[warp], s_q[warp], s_sm[warp], do_mut, do_ph, gather,
+                           do_fs, sF, sV);
             if (profile && lane == 0) { rows_done += 1; words_done += st.W; }
         }
         __syncthreads();
     }
     __syncthreads();
-    if (cur_pop >= 0 && do_fs) {
+    if (cur_pop >= 0 && do_fs && !gacc) {
         const PopDev& Q = pops[cur_pop];
         for (uint32_t w = threadIdx.x; w < cur_W; w += blockDim.x) {
             atomicAnd((unsigned long long*)&Q.accF[w], (unsigned long long)sF[w]);
@@ -585,31 +987,35 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     }
 }
 
-// Shared-memory rank table: u16 ranks are used when every population has
-// A <= 65,536 and the layout fits the opt-in shared-memory limit.
+// The suffix-table classifier runs when every population has a table
+// (capacity <= kSufMaxSlots slots, so maxW <= 1,024 words).
 void launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, WorkCtl* ctl, uint32_t maxW,
                        uint32_t maxA, uint32_t fuse, int profile) {
-    const size_t static_smem = sizeof(uint2) * kWarps * kMaxIvSmem + sizeof(uint32_t) * kWarps * kMaxEvDevice +
-                               sizeof(uint32_t) * kWarps * (kQueueCap + 128) + 64;
-    const size_t base = 3ull * maxW * sizeof(uint64_t);
-    uint32_t maxR = (maxA <= 65536u) ? ((maxA + 7u) & ~7u) : 0u;
-    if (base + 2ull * maxR + static_smem > 227u * 1024u) maxR = 0;
-    const size_t smem = base + 2ull * maxR;
+    const bool suf = maxA <= kSufMaxSlots;
+    // the interval classifier keeps 56 KB of static shared memory
+    const uint32_t gacc = (!suf && 3ull * maxW * sizeof(uint64_t) > 160u * 1024u) ? 1u : 0u;
+    const size_t smem =
+        gacc ? 0 : (3ull + (suf ? kWarps : 0u)) * maxW * sizeof(uint64_t) + (suf ? kWarps * sizeof(WarpSmem) : 0);
     static size_t configured[2] = {0, 0};
-    const int sr = maxR > 0 ? 1 : 0;
-    if (smem + static_smem > 48u * 1024u && smem > configured[sr]) {
-        if (sr) cudaFuncSetAttribute(k_generation<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int si = suf ? 1 : 0;
+    // static shared memory is above 48 KB on its own, so the opt-in attribute is always needed
+    if (smem > configured[si] || configured[si] == 0) {
+        if (suf) cudaFuncSetAttribute(k_generation<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         else cudaFuncSetAttribute(k_generation<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        configured[sr] = smem;
+        configured[si] = smem > 0 ? smem : 1;
     }
-    if (sr) k_generation<true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, maxR);
-    else k_generation<false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, 0u);
+    if (suf)
+        k_generation<true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, 0u);
+    else
+        k_generation<false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, gacc);
 }
 
 // ---------------------------------------------------------------------------
-// Position ranks for the crossover classifier, rebuilt every generation over
+// Position ranks for the crossover classifiers, rebuilt every generation over
 // the slots [0, A): counting sort of positions into NB buckets, then each
-// slot's rank = slots in lower buckets + smaller positions in its own bucket.
+// slot's rank = slots in lower buckets + slots of its own bucket with a
+// smaller position (or the same position and a lower slot index).  inv is the
+// inverse map (rank -> slot); suf is the suffix table of the classifier.
 __global__ void k_rank_count(const PopDev* __restrict__ pops, uint32_t npops) {
     for (uint32_t p = 0; p < npops; ++p) {
         const PopDev& P = pops[p];
@@ -625,8 +1031,9 @@ __global__ void k_rank_scatter(const PopDev* __restrict__ pops, uint32_t npops) 
         for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < A; s += gridDim.x * blockDim.x) {
             const double x = P.pos[s];
             const uint32_t b = pos_bucket(x, P.NB);
-            const uint32_t k = atomicAdd(&P.bcur[b], 1u);
-            P.bpos[P.boff[b] + k] = x;
+            const uint32_t k = P.boff[b] + atomicAdd(&P.bcur[b], 1u);
+            P.bpos[k] = x;
+            P.bslot[k] = s;
         }
     }
 }
@@ -639,17 +1046,53 @@ __global__ void k_rank_final(const PopDev* __restrict__ pops, uint32_t npops) {
             const uint32_t b = pos_bucket(x, P.NB);
             const uint32_t k0 = P.boff[b], k1 = P.boff[b + 1u];
             uint32_t r = k0;
-            for (uint32_t k = k0; k < k1; ++k) r += (P.bpos[k] < x) ? 1u : 0u;
+            for (uint32_t k = k0; k < k1; ++k) {
+                const double y = P.bpos[k];
+                r += (y < x || (y == x && P.bslot[k] < s)) ? 1u : 0u;
+            }
             P.rank[s] = r;
+            if (P.inv) P.inv[r] = s;
         }
     }
 }
-void launch_ranks(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxNB) {
+
+// suf[g * Wcap + w] = bits of word w whose slot has rank >= 64 g, for
+// g = 0 .. ceil(A/64) (the last row is empty).  A block covers 32 words.
+__global__ void __launch_bounds__(256) k_suf_build(const PopDev* __restrict__ pops, uint32_t npops) {
+    __shared__ uint32_t s_grp[32][65];  // (rank >> 6) + 1 per slot, 0 beyond A
+    const uint32_t tx = threadIdx.x & 31u, ty = threadIdx.x >> 5;
+    for (uint32_t p = 0; p < npops; ++p) {
+        const PopDev& P = pops[p];
+        if (!P.suf) continue;
+        const uint32_t A = P.st->A, W = P.st->W;
+        const uint32_t Gt = (A + 63u) >> 6;
+        for (uint32_t wb = blockIdx.x * 32u; wb < W; wb += gridDim.x * 32u) {
+            __syncthreads();
+            for (uint32_t i = threadIdx.x; i < 2048u; i += blockDim.x) {
+                const uint32_t s = wb * 64u + i;
+                s_grp[i >> 6][i & 63u] = (s < A) ? (P.rank[s] >> 6) + 1u : 0u;
+            }
+            __syncthreads();
+            const uint32_t w = wb + tx;
+            if (w >= W) continue;
+            for (uint32_t g = blockIdx.y * 8u + ty; g <= Gt; g += gridDim.y * 8u) {
+                uint64_t m = 0;
+#pragma unroll 16
+                for (uint32_t b = 0; b < 64u; ++b) m |= (uint64_t)(s_grp[tx][b] > g) << b;
+                P.suf[(size_t)g * P.Wcap + w] = m;
+            }
+        }
+    }
+}
+
+void launch_ranks(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxNB, uint32_t maxW,
+                  bool suf) {
     const int g = L.num_sms * 2;
     k_rank_count<<<g, 256, 0, L.stream>>>(pops, npops);
     launch_uscan_buckets(L, pops, npops, maxNB);
     k_rank_scatter<<<g, 256, 0, L.stream>>>(pops, npops);
     k_rank_final<<<g, 256, 0, L.stream>>>(pops, npops);
+    if (suf) k_suf_build<<<dim3((maxW + 31u) / 32u, 8), 256, 0, L.stream>>>(pops, npops);
 }
 
 // ---------------------------------------------------------------------------

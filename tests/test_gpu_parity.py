@@ -144,6 +144,19 @@ def test_many_events_beyond_register_set():
     run_parity(8, 100, 4096, mu=0.3, rho=24.0, p_neutral=1.0, q1=False)
 
 
+@pytest.mark.parametrize("A_cap", [70_000, 500_000])
+def test_wide_allele_space_interval_classifier(A_cap):
+    # capacities above 65,536 slots run the interval classifier over global
+    # ranks; at 500,000 the free-space fold also goes to global accumulators
+    run_parity(6, 60, A_cap, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.5, rho=3.0, p_neutral=0.5)
+
+
+def test_suffix_table_boundaries():
+    # many alleles with shared positions and breakpoints on and between the
+    # 64-rank table rows: corrections from both sides, ties broken by slot
+    run_parity(12, 120, 8192, mu=2.0, rho=12.0, p_neutral=1.0, q1=False)
+
+
 def test_staged_policies_equal_fused():
     orc, gpu = make_pair(180, 4096, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.2, rho=1.5, p_neutral=0.4)
     gpu2 = cg.Population(180, 4096, 2, fitness="gaussian_vs", fit_param=4.0, mu=0.2, rho=1.5, p_neutral=0.4,
