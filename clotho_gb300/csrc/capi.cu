@@ -64,6 +64,9 @@ std::vector<size_t> sizes_of(const Geometry& g) {
         (g.NB + 1ull) * 4 * 2, g.NB * 4ull, A * 8, A * 4, A * 4,  // bcnt+boff, bcur, bpos, bslot, rank
         A <= kSufMaxSlots ? A * 4 : 0,                            // inv
         A <= kSufMaxSlots ? (A / 64 + 1) * W * 8 : 0,             // suf
+        A <= kSufMaxSlots ? S * 16 : 0,                           // plan_row
+        A <= kSufMaxSlots ? g.EVcap * 4ull : 0,                   // plan_go
+        A <= kSufMaxSlots ? g.EVcap * 4ull : 0,                   // plan_cr
         sizeof(DevStatus),
         // two tape sets: pairs, swap, ev_off, ev_pos, mut_seq, mut_pos, mut_eff
         S * 4, S, (S + 1) * 4, g.EVcap * 8ull, g.Mcap * 4ull, g.Mcap * 8ull, g.Mcap * T * 4ull,
@@ -166,6 +169,7 @@ int alloc_pop(clotho_ctx* ctx, const clotho_desc& d, PopHost** out) {
     b.boff = b.bcnt + (g.NB + 1);
     b.bcur = (uint32_t*)ptr[k++]; b.bpos = (double*)ptr[k++]; b.bslot = (uint32_t*)ptr[k++];
     b.rank = (uint32_t*)ptr[k++]; b.inv = (uint32_t*)ptr[k++]; b.suf = (uint64_t*)ptr[k++];
+    b.plan_row = (uint4*)ptr[k++]; b.plan_go = (uint32_t*)ptr[k++]; b.plan_cr = (uint32_t*)ptr[k++];
     b.st = (DevStatus*)ptr[k++];
     b.Scap = g.Scap; b.Ncap = g.Ncap; b.Wcap = g.Wcap; b.Acap = g.Aslots; b.Mcap = g.Mcap;
     b.EVcap = g.EVcap; b.FXcap = g.FXcap; b.T = g.T; b.NB = g.NB;
@@ -259,6 +263,10 @@ int prof_collect(clotho_ctx* ctx) {
 }
 
 void launch_gen(clotho_ctx* ctx, const PopDev* pops, uint32_t npops, uint32_t fuse) {
+    if (ctx->maxA <= kSufMaxSlots) {  // per-row crossover plans of the suffix-table classifier
+        launch_plan(cfg(ctx), pops, npops, ctx->maxS);
+        ctx->launches += 1;
+    }
     prof_begin(ctx);
     launch_generation(cfg(ctx), pops, npops, ctx->d_ctl, ctx->maxW, ctx->maxA, fuse, ctx->profiling ? 1 : 0);
     prof_end(ctx);

@@ -45,7 +45,7 @@ struct DevStatus {
     uint32_t fit_const;    // every fitness value equal (selection is uniform)
     uint32_t all_neutral;  // phenotype took the constant path
     uint32_t last_M;
-    uint32_t pad0;
+    uint32_t ev_used;      // crossover-plan event entries allocated in the step in progress
     double   fit_total;    // sum of fitness of the current population
     double   fixsum[4];    // effect sums of the alleles fixed in this step's parent
 };
@@ -88,6 +88,9 @@ struct PopDev {
     uint32_t* rank;        // [Acap] rank of each slot (position, then slot index) among the A slots
     uint32_t* inv;         // [Acap] slot of each rank (Acap <= kSufMaxSlots, else null)
     uint64_t* suf;         // [(Acap/64 + 1) * Wcap] suffix table of the crossover classifier (or null)
+    uint4*    plan_row;    // [Scap] per-row crossover plan: top strand, events, event base, flags (with suf)
+    uint32_t* plan_go;     // [EVcap] table row offset per planned event (with suf)
+    uint32_t* plan_cr;     // [EVcap] correction ranks per planned event: first | count << 20 (with suf)
     DevStatus* st;
     uint32_t Scap, Ncap, Wcap, Acap, Mcap, EVcap, FXcap, T;
     uint32_t NB, pad2;     // position buckets (power of two)
@@ -209,6 +212,11 @@ void launch_seed_rows(const LaunchCfg&, const PopDev* pops, uint32_t npops, cons
 void launch_stats(const LaunchCfg&, const PopDev* pops, uint32_t p, uint32_t* counts, uint32_t A);
 void launch_ranks(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxNB, uint32_t maxW, bool suf);
 void launch_uscan_buckets(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxNB);
+
+void launch_plan(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
+
+// crossover-plan row flags
+constexpr uint32_t kPlanInv = 1u, kPlanLong = 2u;
 
 // fuse flags of k_generation
 constexpr uint32_t kFuseMut = 1u, kFusePheno = 2u, kFuseFs = 4u;

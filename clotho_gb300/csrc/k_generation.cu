@@ -175,8 +175,11 @@ __device__ __forceinline__ void mutation_masks(const PopDev& P, const DevStatus&
     }
 }
 
-// Parents, strand swap and breakpoint count of gamete g; the new alleles of
-// the row (lanes hold up to 32 slot indices) and their effects.
+__device__ __forceinline__ void row_mutation_setup(const PopDev& P, const DevStatus& st, uint32_t g, bool do_mut,
+                                                   bool gather, RowArgs& R, float (&d)[kMaxTraits]);
+
+// Parents, strand swap and breakpoint count of gamete g (interval classifier);
+// the new alleles of the row (lanes hold up to 32 slot indices) and their effects.
 __device__ __forceinline__ void row_setup(const PopDev& P, const DevStatus& st, uint32_t g, bool do_mut,
                                           bool do_ph, bool gather, RowArgs& R, float (&d)[kMaxTraits]) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -220,7 +223,14 @@ __device__ __forceinline__ void row_setup(const PopDev& P, const DevStatus& st, 
     R.zbase = 0.0;
     if (do_ph && lane < kMaxTraits)
         R.zbase = P.zg[st.cur ^ 1u][(size_t)topr * 4u + lane] - P.st->fixsum[lane];
+    row_mutation_setup(P, st, g, do_mut, gather, R, d);
+}
 
+// The new alleles of row g (lanes hold up to 32 slot indices) and their effects.
+__device__ __forceinline__ void row_mutation_setup(const PopDev& P, const DevStatus& st, uint32_t g, bool do_mut,
+                                                   bool gather, RowArgs& R, float (&d)[kMaxTraits]) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const bool philox = R.philox;
     R.mo = 0;
     R.mc = 0;
     R.my_slot = 0xffffffffu;
@@ -538,88 +548,85 @@ __device__ __forceinline__ uint32_t table_row(uint32_t r, uint32_t A, uint32_t& 
     return b;
 }
 
-// One offspring row, the whole warp (suffix-table classifier).
+// One offspring row, the whole warp (suffix-table classifier), from its plan
+// (k_row_plan): top strand, breakpoints, table rows and correction ranks.
 __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st, uint32_t g, const uint64_t* sfix,
                                             uint64_t* mask, WarpSmem& ws, bool do_mut, bool do_ph, bool gather,
                                             bool do_fs, uint64_t* sF, uint64_t* sV) {
     const uint32_t lane = threadIdx.x & 31u;
+    const uint4 pr = __ldg(P.plan_row + g);
+    const uint32_t E = pr.y, base = pr.z;
+    const bool inv = gather && (pr.w & kPlanInv) != 0;
+    const uint64_t* prow = P.rows[st.cur ^ 1u];
     RowArgs R;
-    float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
-    row_setup(P, st, g, do_mut, do_ph, gather, R, d);
+    R.topr = pr.x;
+    R.top = prow + (size_t)pr.x * P.Wcap;
+    R.bot = prow + (size_t)(pr.x ^ 1u) * P.Wcap;
+    R.out = P.rows[st.cur] + (size_t)g * P.Wcap;
+    R.Wc = st.W;
+    R.Wp = st.pW;
+    R.E = E;
+    R.philox = P.mode == kModePhilox;
+    R.evg = P.ev_pos + base;
     prefetch_l2(R.top, R.Wp * 8u);
-    if (R.E > 0) prefetch_l2(R.bot, R.Wp * 8u);
-    const uint32_t E = R.E;
-    bool inv = false;
-    if (E > kMaxEvDevice) {
+    if (E > 0) prefetch_l2(R.bot, R.Wp * 8u);
+    R.zbase = 0.0;
+    if (do_ph && lane < kMaxTraits)
+        R.zbase = P.zg[st.cur ^ 1u][(size_t)(inv ? pr.x ^ 1u : pr.x) * 4u + lane] - P.st->fixsum[lane];
+    float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
+    row_mutation_setup(P, st, g, do_mut, gather, R, d);
+    if (pr.w & kPlanLong) {
         add4(d, row_body_events(P, st.M, R, sfix, ws.q, do_mut, gather, do_fs, sF, sV));
-    } else if (E > 0) {
-        const uint32_t A = st.A;
-        for (uint32_t k = lane; k < E; k += 32u) {
-            const uint32_t r = threshold_rank(P, row_event(P, st, R, g, k));
-            uint32_t c0, n;
-            ws.go[k] = (table_row(r, A, c0, n) >> 6) * P.Wcap;
-            ws.rr[k] = r;
-        }
-        __syncwarp();
+    } else if (E == 0) {
+        row_body_copy(P, st.M, R, sfix, do_mut, do_fs, sF, sV);
+    } else {
         // corrections: toggle the slots whose rank lies between threshold and table row
         uint32_t* m32 = reinterpret_cast<uint32_t*>(mask);
+        for (uint32_t k0 = 0; k0 < E; k0 += 32u) {
+            const uint32_t my_cr = (k0 + lane < E) ? __ldg(P.plan_cr + base + k0 + lane) : 0u;
+            const uint32_t ke = min(32u, E - k0);
 #pragma unroll 4
-        for (uint32_t k = 0; k < E; ++k) {
-            uint32_t c0, n;
-            table_row(ws.rr[k], A, c0, n);
-            if (lane < n) {
-                const uint32_t s = __ldg(P.inv + c0 + lane);
-                atomicXor(m32 + (s >> 5), 1u << (s & 31u));
-            }
-        }
-        // switched share of the rank space: the sorted thresholds pair into intervals
-        if (gather) {
-            int32_t len = 0;
-            for (uint32_t k = lane; k < E; k += 32u) {
-                const uint32_t rk = ws.rr[k];
-                uint32_t posn = 0;
-                for (uint32_t j = 0; j < E; ++j) {
-                    const uint32_t rj = ws.rr[j];
-                    posn += (rj < rk || (rj == rk && j < k)) ? 1u : 0u;
+            for (uint32_t k = 0; k < ke; ++k) {
+                const uint32_t pc = __shfl_sync(0xffffffffu, my_cr, k);
+                if (lane < (pc >> 20)) {
+                    const uint32_t s = __ldg(P.inv + (pc & 0xfffffu) + lane);
+                    atomicXor(m32 + (s >> 5), 1u << (s & 31u));
                 }
-                len += (posn & 1u) ? (int32_t)rk : -(int32_t)rk;
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) len += __shfl_xor_sync(0xffffffffu, len, o);
-            if (E & 1u) len += (int32_t)A;
-            inv = 2 * (int64_t)len > (int64_t)A;
-            if (inv && lane < kMaxTraits)
-                R.zbase = P.zg[st.cur ^ 1u][(size_t)(R.topr ^ 1u) * 4u + lane] - P.st->fixsum[lane];
         }
         __syncwarp();
         // XOR of the events' table rows, kTableInflight 16-byte loads per lane in flight
         const uint64_t* __restrict__ suf = P.suf;
         ulonglong2* m2 = reinterpret_cast<ulonglong2*>(mask);
-        for (uint32_t k = 0; k < E; ++k) {
-            const uint64_t* tk = suf + ws.go[k];
-            for (uint32_t wb = 0; wb < R.Wp; wb += 64u * kTableInflight) {
-                ulonglong2 v[kTableInflight];
+        for (uint32_t k0 = 0; k0 < E; k0 += 32u) {
+            const uint32_t my_go = (k0 + lane < E) ? __ldg(P.plan_go + base + k0 + lane) : 0u;
+            const uint32_t ke = min(32u, E - k0);
+            for (uint32_t k = 0; k < ke; ++k) {
+                const uint64_t* tk = suf + __shfl_sync(0xffffffffu, my_go, k);
+                for (uint32_t wb = 0; wb < R.Wp; wb += 64u * kTableInflight) {
+                    ulonglong2 v[kTableInflight];
 #pragma unroll
-                for (uint32_t j = 0; j < kTableInflight; ++j) {
-                    const uint32_t w = wb + 64u * j + 2u * lane;
-                    v[j] = (w < R.Wp) ? __ldg(reinterpret_cast<const ulonglong2*>(tk + w)) : make_ulonglong2(0, 0);
-                }
+                    for (uint32_t j = 0; j < kTableInflight; ++j) {
+                        const uint32_t w = wb + 64u * j + 2u * lane;
+                        v[j] = (w < R.Wp) ? __ldg(reinterpret_cast<const ulonglong2*>(tk + w))
+                                          : make_ulonglong2(0, 0);
+                    }
 #pragma unroll
-                for (uint32_t j = 0; j < kTableInflight; ++j) {
-                    const uint32_t w = wb + 64u * j + 2u * lane;
-                    if (w < R.Wp) {
-                        ulonglong2 x = m2[w >> 1];
-                        x.x ^= v[j].x;
-                        x.y ^= v[j].y;
-                        m2[w >> 1] = x;
+                    for (uint32_t j = 0; j < kTableInflight; ++j) {
+                        const uint32_t w = wb + 64u * j + 2u * lane;
+                        if (w < R.Wp) {
+                            ulonglong2 x = m2[w >> 1];
+                            x.x ^= v[j].x;
+                            x.y ^= v[j].y;
+                            m2[w >> 1] = x;
+                        }
                     }
                 }
             }
         }
         __syncwarp();
+        row_body_suf<0>(P, st.M, R, sfix, mask, ws.q, inv, do_mut, gather, do_fs, sF, sV, d);
     }
-    if (E == 0) row_body_copy(P, st.M, R, sfix, do_mut, do_fs, sF, sV);
-    else if (E <= kMaxEvDevice) row_body_suf<0>(P, st.M, R, sfix, mask, ws.q, inv, do_mut, gather, do_fs, sF, sV, d);
     if (do_ph) row_phenotype(P, st, g, R, d);
 }
 
@@ -1008,6 +1015,123 @@ void launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, W
         k_generation<true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, 0u);
     else
         k_generation<false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, gacc);
+}
+
+// ---------------------------------------------------------------------------
+// Per-row crossover plans for the suffix-table classifier, one thread per row:
+// the top strand (parent individual and strand swap), the breakpoint count,
+// and for every breakpoint its nearest table row and correction ranks; plus
+// the direction of the phenotype gather.  Device-drawn breakpoints get their
+// plan entries from a block-aggregated counter; tape rows use the tape's own
+// event offsets.
+__global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pops, uint32_t npops) {
+    __shared__ uint32_t s_w[8];
+    __shared__ uint32_t s_base;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for (uint32_t p = 0; p < npops; ++p) {
+        const PopDev& P = pops[p];
+        if (!P.plan_row) continue;
+        const DevStatus st = *P.st;
+        const uint32_t S = 2u * st.N, A = st.A;
+        const bool philox = P.mode == kModePhilox;
+        const bool q1 = (P.flags & 1u) != 0;
+        for (uint32_t g0 = blockIdx.x * blockDim.x; g0 < S; g0 += gridDim.x * blockDim.x) {
+            const uint32_t g = g0 + threadIdx.x;
+            const bool live = g < S;
+            uint32_t pind = 0, E = 0, base = 0, flags = 0;
+            bool swap = false;
+            if (live) {
+                pind = P.pairs[g];
+                if (pind >= st.pN) {
+                    atomicOr(&P.st->err, kErrParent);
+                    pind = 0;
+                }
+                if (philox) {
+                    const U4 x = philox4x32(g, 0u, st.gen, kStreamGamete, P.seed);
+                    E = poisson_inv(u01(x.x, x.y), P.rho, P.exp_neg_rho);
+                    swap = u01(x.z, x.w) < P.bias;
+                    if (q1 && (g & 1u)) E = 0;
+                    if (E > kMaxEvDevice) {
+                        atomicOr(&P.st->err, kErrEvents);
+                        E = kMaxEvDevice;
+                    }
+                } else {
+                    swap = P.swap[g] != 0;
+                    base = P.ev_off[g];
+                    E = (q1 && (g & 1u)) ? 0u : P.ev_off[g + 1u] - base;
+                }
+            }
+            if (philox) {  // block-aggregated allocation of the plan entries
+                uint32_t incl = E;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= (uint32_t)o) incl += y;
+                }
+                if (lane == 31u) s_w[warp] = incl;
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    uint32_t t = 0;
+                    for (uint32_t i = 0; i < blockDim.x / 32u; ++i) {
+                        const uint32_t c = s_w[i];
+                        s_w[i] = t;
+                        t += c;
+                    }
+                    s_base = t ? atomicAdd(&P.st->ev_used, t) : 0u;
+                }
+                __syncthreads();
+                base = s_base + s_w[warp] + incl - E;
+                __syncthreads();
+                if (E && base + E > P.EVcap) {
+                    atomicOr(&P.st->err, kErrEvents);
+                    E = 0;
+                }
+            }
+            if (!live) continue;
+            if (E > kMaxEvDevice) {
+                flags = kPlanLong;  // tape rows with very long event lists: direct compares
+            } else if (E > 0) {
+                uint32_t* cr = P.plan_cr + base;
+                for (uint32_t k = 0; k < E; k += 2u) {
+                    double e0, e1 = 0.0;
+                    if (philox) {
+                        const U4 a = philox4x32(g, 1u + (k >> 1), st.gen, kStreamGamete, P.seed);
+                        e0 = u01(a.x, a.y);
+                        e1 = u01(a.z, a.w);
+                    } else {
+                        e0 = __ldg(P.ev_pos + base + k);
+                        if (k + 1u < E) e1 = __ldg(P.ev_pos + base + k + 1u);
+                    }
+                    cr[k] = threshold_rank(P, e0);
+                    if (k + 1u < E) cr[k + 1u] = threshold_rank(P, e1);
+                }
+                // share of the rank space the breakpoints switch: sorted thresholds pair into intervals
+                int64_t len = (E & 1u) ? (int64_t)A : 0;
+                for (uint32_t k = 0; k < E; ++k) {
+                    const uint32_t rk = cr[k];
+                    uint32_t posn = 0;
+                    for (uint32_t j = 0; j < E; ++j) {
+                        const uint32_t rj = cr[j];
+                        posn += (rj < rk || (rj == rk && j < k)) ? 1u : 0u;
+                    }
+                    len += (posn & 1u) ? (int64_t)rk : -(int64_t)rk;
+                }
+                if (2 * len > (int64_t)A) flags |= kPlanInv;
+                for (uint32_t k = 0; k < E; ++k) {
+                    uint32_t c0, n;
+                    const uint32_t b = table_row(cr[k], A, c0, n);
+                    P.plan_go[base + k] = (b >> 6) * P.Wcap;
+                    cr[k] = c0 | (n << 20);
+                }
+            }
+            P.plan_row[g] = make_uint4(2u * pind + (swap ? 1u : 0u), E, base, flags);
+        }
+    }
+}
+
+void launch_plan(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
+    const uint32_t blocks = max(1u, min((maxS + 255u) / 256u, (uint32_t)L.num_sms * 8u));
+    k_row_plan<<<blocks, 256, 0, L.stream>>>(pops, npops);
 }
 
 // ---------------------------------------------------------------------------

@@ -52,6 +52,7 @@ __global__ void k_begin(const PopDev* __restrict__ pops, uint32_t npops, const u
         st->pW = st->W;
         st->N = N;
         st->M = M;
+        st->ev_used = 0;
         st->cur ^= 1u;
         const uint32_t rpi = ctl->rows_per_item ? ctl->rows_per_item : kRowsPerItem;
         s_items[p] = (2u * N + rpi - 1u) / rpi;
