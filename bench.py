@@ -351,8 +351,11 @@ def main():
     achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     traffic = ncu_traffic()
+    # DRAM bytes per (row, live word) from one ncu capture of this kernel on a smaller
+    # population of the same workload (profiles/), scaled to this launch's rows x words
+    per_word = (traffic or {}).get("dram_bytes_per_row_word")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": (traffic or {}).get("bytes_per_launch") if traffic else None,
+                "traffic": per_word * words_done / max(nl, 1) if per_word else None,
                 "peak_kind": f"of {peak_kind}", "kernel": "k_generation", "kernel_ms": avg_ms,
                 "algorithmic_bytes_per_launch": bytes_per_launch, "W_live": w_live,
                 "step_share": (avg_ms * args.steps) / ms if ms else None}

@@ -307,8 +307,6 @@ __device__ __forceinline__ void row_phenotype(const PopDev& P, const DevStatus& 
 
 struct WarpSmem {
     uint32_t q[kQueueCap];            // effect queue: slot | sign << 31
-    uint32_t go[kMaxEvDevice];        // table row offset per event
-    uint32_t rr[kMaxEvDevice];        // rank threshold per event
 };
 
 __device__ __forceinline__ void add4(float (&d)[kMaxTraits], const float4& e) {
@@ -326,7 +324,7 @@ __device__ CLOTHO_COLD float4 effects_direct(uint64_t m0, uint64_t m1, uint64_t 
 }
 
 #ifndef CLOTHO_ROUND_LANE
-#define CLOTHO_ROUND_LANE 4
+#define CLOTHO_ROUND_LANE 2
 #endif
 #ifndef CLOTHO_TABLE_INFLIGHT
 #define CLOTHO_TABLE_INFLIGHT 16
@@ -335,36 +333,49 @@ constexpr uint32_t kRoundLane = CLOTHO_ROUND_LANE;   // queue entries gathered p
 constexpr uint32_t kRound = 32u * kRoundLane;
 constexpr uint32_t kTableInflight = CLOTHO_TABLE_INFLIGHT;
 
-// Effects of queue entries [head, head + n), n <= kRound, kRoundLane per lane.
-__device__ __forceinline__ void effq_round(const uint32_t* Q, uint32_t head, uint32_t n,
-                                           const float4* __restrict__ eff4, float (&d)[kMaxTraits]) {
+// A gather round in flight: its effects are loaded when the round is issued
+// and folded into the sums one round later, so the loads have a chunk of work
+// to land behind.
+struct EffRound {
+    float4 ef[kRoundLane];
+    float sg[kRoundLane];  // +1 / -1, 0 for an empty entry
+};
+
+__device__ __forceinline__ void effq_issue(const uint32_t* Q, uint32_t head, uint32_t n,
+                                           const float4* __restrict__ eff4, EffRound& r) {
     const uint32_t lane = threadIdx.x & 31u;
-    uint32_t e[kRoundLane];
-    bool ok[kRoundLane];
 #pragma unroll
     for (uint32_t k = 0; k < kRoundLane; ++k) {
         const uint32_t i = lane + 32u * k;
-        ok[k] = i < n;
-        e[k] = ok[k] ? Q[(head + i) & (kQueueCap - 1u)] : 0u;
+        const bool ok = i < n;
+        const uint32_t e = ok ? Q[(head + i) & (kQueueCap - 1u)] : 0u;
+        r.sg[k] = ok ? ((e >> 31) ? 1.0f : -1.0f) : 0.0f;
+        r.ef[k] = ok ? __ldg(eff4 + (e & 0x7fffffffu)) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    float4 ef[kRoundLane];
-#pragma unroll
-    for (uint32_t k = 0; k < kRoundLane; ++k)
-        ef[k] = ok[k] ? __ldg(eff4 + (e[k] & 0x7fffffffu)) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__device__ __forceinline__ void effq_complete(const EffRound& r, float (&d)[kMaxTraits]) {
 #pragma unroll
     for (uint32_t k = 0; k < kRoundLane; ++k) {
-        const float s = ok[k] ? ((e[k] >> 31) ? 1.0f : -1.0f) : 0.0f;
-        d[0] = fmaf(s, ef[k].x, d[0]);
-        d[1] = fmaf(s, ef[k].y, d[1]);
-        d[2] = fmaf(s, ef[k].z, d[2]);
-        d[3] = fmaf(s, ef[k].w, d[3]);
+        d[0] = fmaf(r.sg[k], r.ef[k].x, d[0]);
+        d[1] = fmaf(r.sg[k], r.ef[k].y, d[1]);
+        d[2] = fmaf(r.sg[k], r.ef[k].z, d[2]);
+        d[3] = fmaf(r.sg[k], r.ef[k].w, d[3]);
+    }
+}
+
+__device__ __forceinline__ void effq_clear(EffRound& r) {
+#pragma unroll
+    for (uint32_t k = 0; k < kRoundLane; ++k) {
+        r.sg[k] = 0.0f;
+        r.ef[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
 
 // Queue the gathered bits (g0, g1) of the lane's words w, w+1 (sign +1 where
-// s0/s1 has the bit) and gather every complete round.
+// s0/s1 has the bit); every complete round is issued, the previous one folded in.
 __device__ __forceinline__ void effq_push(uint64_t g0, uint64_t g1, uint64_t s0, uint64_t s1, uint32_t w,
-                                          uint32_t* Q, uint32_t& head, uint32_t& tail,
+                                          uint32_t* Q, uint32_t& head, uint32_t& tail, EffRound& pend,
                                           const float4* __restrict__ eff4, float (&d)[kMaxTraits]) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t c = (uint32_t)(__popcll(g0) + __popcll(g1));
@@ -395,7 +406,8 @@ __device__ __forceinline__ void effq_push(uint64_t g0, uint64_t g1, uint64_t s0,
     tail += H;
     __syncwarp();
     while (tail - head >= kRound) {
-        effq_round(Q, head, kRound, eff4, d);
+        effq_complete(pend, d);
+        effq_issue(Q, head, kRound, eff4, pend);
         head += kRound;
     }
     __syncwarp();
@@ -478,6 +490,8 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
     constexpr bool xo = true;
     const float4* eff4 = reinterpret_cast<const float4*>(P.eff);
     uint32_t qh = 0, qt = 0;
+    EffRound pend;
+    effq_clear(pend);
     ulonglong2 t_a, b_a, t_b, b_b;
     load_pair(t_a, b_a, R, 2u * lane, xo);
     load_pair(t_b, b_b, R, 2u * lane + 64u, xo);
@@ -513,7 +527,7 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
             x1 = t1 ^ sw1;
             if (gather)
                 effq_push(inv ? (h0 ^ sw0) : sw0, inv ? (h1 ^ sw1) : sw1, inv ? t0 : b0, inv ? t1 : b1, w, Q, qh, qt,
-                          eff4, d);
+                          pend, eff4, d);
         }
         if (live) {
             x0 ^= mx0;
@@ -524,9 +538,13 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
         t_a = t_b; b_a = b_b;
         t_b = t_c; b_b = b_c;
     }
-    if (gather && qt != qh) {
-        effq_round(Q, qh, qt - qh, eff4, d);
-        __syncwarp();
+    if (gather) {
+        effq_complete(pend, d);
+        if (qt != qh) {
+            effq_issue(Q, qh, qt - qh, eff4, pend);
+            effq_complete(pend, d);
+            __syncwarp();
+        }
     }
 }
 
