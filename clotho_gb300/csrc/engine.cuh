@@ -191,6 +191,21 @@ struct LaunchCfg {
     cudaStream_t stream;
     int num_sms;
 };
+
+// Population-parallel launches: blockIdx.z walks the populations, so small
+// populations of a batch run side by side; blockIdx.x (and .y) stride inside
+// one population.  per_pop bounds the useful blocks of one population.
+inline dim3 pop_grid(uint32_t npops, uint32_t per_pop, int num_sms, uint32_t per_sm = 4) {
+    const uint32_t gz = npops < 1u ? 1u : (npops > 65535u ? 65535u : npops);
+    uint32_t gx = (uint32_t)num_sms * per_sm / gz;
+    if (gx > per_pop) gx = per_pop;
+    if (gx < 1u) gx = 1u;
+    return dim3(gx, 1u, gz);
+}
+inline uint32_t blocks_for(uint64_t n, uint32_t per_block) {
+    const uint64_t b = (n + per_block - 1) / per_block;
+    return b < 1 ? 1u : (b > 0x7fffffffull ? 0x7fffffffu : (uint32_t)b);
+}
 // which: 0 = current child rows, 1 = parent rows of the step in progress
 void launch_fs_reduce(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxW, uint32_t which);
 void launch_fs_finalize(const LaunchCfg&, const PopDev* pops, uint32_t npops);

@@ -20,7 +20,7 @@ namespace clotho {
 // which == 0: the current child rows; which == 1: the parent of the step in progress.
 __global__ void __launch_bounds__(256) k_fs_reduce(const PopDev* __restrict__ pops, uint32_t npops,
                                                    uint32_t which) {
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         const DevStatus st = *P.st;
         const uint32_t S = 2u * (which ? st.pN : st.N);
@@ -49,7 +49,9 @@ __global__ void __launch_bounds__(256) k_fs_reduce(const PopDev* __restrict__ po
 }
 
 void launch_fs_reduce(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxW, uint32_t which) {
-    dim3 grid(max(1u, min(16u, (maxW + 511u) / 512u)), max(1, L.num_sms * 4 / max(1u, min(16u, (maxW + 511u) / 512u))));
+    const dim3 pg = pop_grid(npops, 0x7fffffffu, L.num_sms, 4);  // blocks per population in pg.x
+    const uint32_t gx = max(1u, min(16u, (maxW + 511u) / 512u));
+    const dim3 grid(gx, max(1u, pg.x / gx), pg.z);
     k_fs_reduce<<<grid, 256, 0, L.stream>>>(pops, npops, which);
 }
 

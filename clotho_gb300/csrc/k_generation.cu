@@ -1046,7 +1046,7 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
     __shared__ uint32_t s_w[8];
     __shared__ uint32_t s_base;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         if (!P.plan_row) continue;
         const DevStatus st = *P.st;
@@ -1148,8 +1148,7 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
 }
 
 void launch_plan(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
-    const uint32_t blocks = max(1u, min((maxS + 255u) / 256u, (uint32_t)L.num_sms * 8u));
-    k_row_plan<<<blocks, 256, 0, L.stream>>>(pops, npops);
+    k_row_plan<<<pop_grid(npops, blocks_for(maxS, 256), L.num_sms, 8), 256, 0, L.stream>>>(pops, npops);
 }
 
 // ---------------------------------------------------------------------------
@@ -1159,7 +1158,7 @@ void launch_plan(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_
 // smaller position (or the same position and a lower slot index).  inv is the
 // inverse map (rank -> slot); suf is the suffix table of the classifier.
 __global__ void k_rank_count(const PopDev* __restrict__ pops, uint32_t npops) {
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         const uint32_t A = P.st->A;
         for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < A; s += gridDim.x * blockDim.x)
@@ -1167,7 +1166,7 @@ __global__ void k_rank_count(const PopDev* __restrict__ pops, uint32_t npops) {
     }
 }
 __global__ void k_rank_scatter(const PopDev* __restrict__ pops, uint32_t npops) {
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         const uint32_t A = P.st->A;
         for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < A; s += gridDim.x * blockDim.x) {
@@ -1180,7 +1179,7 @@ __global__ void k_rank_scatter(const PopDev* __restrict__ pops, uint32_t npops) 
     }
 }
 __global__ void k_rank_final(const PopDev* __restrict__ pops, uint32_t npops) {
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         const uint32_t A = P.st->A;
         for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < A; s += gridDim.x * blockDim.x) {
@@ -1203,7 +1202,7 @@ __global__ void k_rank_final(const PopDev* __restrict__ pops, uint32_t npops) {
 __global__ void __launch_bounds__(256) k_suf_build(const PopDev* __restrict__ pops, uint32_t npops) {
     __shared__ uint32_t s_grp[32][65];  // (rank >> 6) + 1 per slot, 0 beyond A
     const uint32_t tx = threadIdx.x & 31u, ty = threadIdx.x >> 5;
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         if (!P.suf) continue;
         const uint32_t A = P.st->A, W = P.st->W;
@@ -1229,12 +1228,16 @@ __global__ void __launch_bounds__(256) k_suf_build(const PopDev* __restrict__ po
 
 void launch_ranks(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxNB, uint32_t maxW,
                   bool suf) {
-    const int g = L.num_sms * 2;
+    const dim3 g = pop_grid(npops, L.num_sms * 2u, L.num_sms, 2);
     k_rank_count<<<g, 256, 0, L.stream>>>(pops, npops);
     launch_uscan_buckets(L, pops, npops, maxNB);
     k_rank_scatter<<<g, 256, 0, L.stream>>>(pops, npops);
     k_rank_final<<<g, 256, 0, L.stream>>>(pops, npops);
-    if (suf) k_suf_build<<<dim3((maxW + 31u) / 32u, 8), 256, 0, L.stream>>>(pops, npops);
+    if (suf) {
+        const dim3 pg = pop_grid(npops, 0x7fffffffu, L.num_sms, 4);
+        const uint32_t gx = (maxW + 31u) / 32u;
+        k_suf_build<<<dim3(gx, max(1u, min(8u, pg.x / max(1u, gx))), pg.z), 256, 0, L.stream>>>(pops, npops);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1245,7 +1248,7 @@ void launch_ranks(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32
 __global__ void __launch_bounds__(256) k_phenotype(const PopDev* __restrict__ pops, uint32_t npops) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         const DevStatus st = *P.st;
         const uint32_t S = 2u * st.N, W = st.W;
@@ -1270,7 +1273,7 @@ __global__ void __launch_bounds__(256) k_phenotype(const PopDev* __restrict__ po
     }
 }
 void launch_phenotype(const LaunchCfg& L, const PopDev* pops, uint32_t npops) {
-    k_phenotype<<<L.num_sms * 8, 256, 0, L.stream>>>(pops, npops);
+    k_phenotype<<<pop_grid(npops, L.num_sms * 8u, L.num_sms, 8), 256, 0, L.stream>>>(pops, npops);
 }
 
 }  // namespace clotho

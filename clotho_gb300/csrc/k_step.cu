@@ -105,7 +105,7 @@ __device__ inline ScanSel scan_sel(const PopDev& P, int which) {
 
 __global__ void __launch_bounds__(1024) k_uscan_a(const PopDev* __restrict__ pops, uint32_t npops, int which) {
     __shared__ uint32_t s_w[32];
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         const ScanSel Z = scan_sel(P, which);
         const uint32_t L = Z.L;
@@ -144,7 +144,7 @@ __global__ void k_uscan_b(const PopDev* __restrict__ pops, uint32_t npops, int w
 __global__ void __launch_bounds__(1024) k_uscan_c(const PopDev* __restrict__ pops, uint32_t npops, int which,
                                                   int set_M) {
     __shared__ uint32_t s_w[32];
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         const ScanSel Z = scan_sel(P, which);
         const uint32_t S = Z.ncur, L = Z.L;
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(1024) k_uscan_c(const PopDev* __restrict__ pop
 static void launch_uscan(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxLen, int which,
                          int set_M) {
     const uint32_t nch = (maxLen + 1 + kScanChunk - 1) / kScanChunk;
-    const uint32_t g = max(1u, min(nch, (uint32_t)L.num_sms * 2u));
+    const dim3 g = pop_grid(npops, nch, L.num_sms, 2);
     k_uscan_a<<<g, 1024, 0, L.stream>>>(pops, npops, which);
     k_uscan_b<<<npops, 32, 0, L.stream>>>(pops, npops, which);
     k_uscan_c<<<g, 1024, 0, L.stream>>>(pops, npops, which, set_M);
@@ -197,7 +197,7 @@ void launch_uscan_buckets(const LaunchCfg& L, const PopDev* pops, uint32_t npops
 // Tape mutations grouped by target row (device counting sort; the in-row order
 // does not affect any result).
 __global__ void k_csr_count(const PopDev* __restrict__ pops, uint32_t npops) {
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         DevStatus* st = P.st;
         const uint32_t M = st->M, S = 2u * st->N;
@@ -209,7 +209,7 @@ __global__ void k_csr_count(const PopDev* __restrict__ pops, uint32_t npops) {
     }
 }
 __global__ void k_csr_scatter(const PopDev* __restrict__ pops, uint32_t npops) {
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         const uint32_t M = P.st->M, S = 2u * P.st->N;
         for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
@@ -221,7 +221,7 @@ __global__ void k_csr_scatter(const PopDev* __restrict__ pops, uint32_t npops) {
     }
 }
 void launch_mut_csr_tape(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
-    const int g = L.num_sms * 2;
+    const dim3 g = pop_grid(npops, L.num_sms * 2u, L.num_sms, 2);
     k_csr_count<<<g, 256, 0, L.stream>>>(pops, npops);
     launch_uscan(L, pops, npops, maxS, 0, 0);
     k_csr_scatter<<<g, 256, 0, L.stream>>>(pops, npops);
@@ -232,7 +232,7 @@ void launch_mut_csr_tape(const LaunchCfg& L, const PopDev* pops, uint32_t npops,
 // same law as M ~ Poisson(mu * 2N) with uniform target rows
 // (mutation_allocator.hpp:41-47, batch_mutation_task_population_space_row.hpp:77).
 __global__ void k_philox_rowcnt(const PopDev* __restrict__ pops, uint32_t npops) {
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         if (P.mode != kModePhilox) continue;
         const DevStatus* st = P.st;
@@ -244,7 +244,7 @@ __global__ void k_philox_rowcnt(const PopDev* __restrict__ pops, uint32_t npops)
     }
 }
 void launch_mut_counts_philox(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
-    k_philox_rowcnt<<<L.num_sms * 4, 256, 0, L.stream>>>(pops, npops);
+    k_philox_rowcnt<<<pop_grid(npops, blocks_for(maxS, 256), L.num_sms, 4), 256, 0, L.stream>>>(pops, npops);
     launch_uscan(L, pops, npops, maxS, 0, 1);
 }
 
@@ -254,7 +254,7 @@ void launch_mut_counts_philox(const LaunchCfg& L, const PopDev* pops, uint32_t n
 // the allele table (AlleleGenerator, allele_generator_vector.hpp:76-83) and
 // the trait table (TraitSpaceGenerator2, trait_space_generator.hpp:118-129).
 __global__ void k_mut_resolve(const PopDev* __restrict__ pops, uint32_t npops) {
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         DevStatus* st = P.st;
         const uint32_t M = st->M, fr = st->free_cnt, pA = st->pA, gen = st->gen, T = P.T;
@@ -298,13 +298,13 @@ __global__ void k_mut_resolve(const PopDev* __restrict__ pops, uint32_t npops) {
     }
 }
 void launch_mut_resolve(const LaunchCfg& L, const PopDev* pops, uint32_t npops) {
-    k_mut_resolve<<<L.num_sms * 2, 256, 0, L.stream>>>(pops, npops);
+    k_mut_resolve<<<pop_grid(npops, L.num_sms * 2u, L.num_sms, 2), 256, 0, L.stream>>>(pops, npops);
 }
 
 // Standalone mutation scatter (staged API): child->mutate(seq, slot) is a
 // single-bit XOR (population_space_row_block.hpp:111-125).
 __global__ void k_mut_scatter(const PopDev* __restrict__ pops, uint32_t npops) {
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         const DevStatus* st = P.st;
         const uint32_t M = st->M, S = 2u * st->N;
@@ -317,7 +317,7 @@ __global__ void k_mut_scatter(const PopDev* __restrict__ pops, uint32_t npops) {
     }
 }
 void launch_mut_scatter(const LaunchCfg& L, const PopDev* pops, uint32_t npops) {
-    k_mut_scatter<<<L.num_sms * 2, 256, 0, L.stream>>>(pops, npops);
+    k_mut_scatter<<<pop_grid(npops, L.num_sms * 2u, L.num_sms, 2), 256, 0, L.stream>>>(pops, npops);
 }
 
 // ---------------------------------------------------------------------------
@@ -325,7 +325,7 @@ void launch_mut_scatter(const LaunchCfg& L, const PopDev* pops, uint32_t npops) 
 // general_fitness_selection_generator.hpp:45-69): uniform when every fitness
 // is equal, else the FP64 inclusive prefix sum and an upper_bound per draw.
 __global__ void k_select_philox(const PopDev* __restrict__ pops, uint32_t npops) {
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         const DevStatus* st = P.st;
         const uint32_t N = st->N, Np = st->pN, gen = st->gen;
@@ -355,7 +355,7 @@ __global__ void k_select_philox(const PopDev* __restrict__ pops, uint32_t npops)
     }
 }
 void launch_select_philox(const LaunchCfg& L, const PopDev* pops, uint32_t npops) {
-    k_select_philox<<<L.num_sms * 2, 256, 0, L.stream>>>(pops, npops);
+    k_select_philox<<<pop_grid(npops, L.num_sms * 2u, L.num_sms, 2), 256, 0, L.stream>>>(pops, npops);
 }
 
 // ---------------------------------------------------------------------------
@@ -363,7 +363,7 @@ void launch_select_philox(const LaunchCfg& L, const PopDev* pops, uint32_t npops
 // or the constant 1.0 when every trait weight is zero (engine_batched_task.hpp:207-211);
 // then the fitness metric (GeneralFitness::operator(), general_fitness.hpp:101-119).
 __global__ void k_individuals(const PopDev* __restrict__ pops, uint32_t npops) {
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         DevStatus* st = P.st;
         const uint32_t N = st->N, T = P.T;
@@ -403,7 +403,7 @@ __global__ void k_individuals(const PopDev* __restrict__ pops, uint32_t npops) {
     }
 }
 void launch_individuals(const LaunchCfg& L, const PopDev* pops, uint32_t npops) {
-    k_individuals<<<L.num_sms * 2, 256, 0, L.stream>>>(pops, npops);
+    k_individuals<<<pop_grid(npops, L.num_sms * 2u, L.num_sms, 2), 256, 0, L.stream>>>(pops, npops);
 }
 
 // ---------------------------------------------------------------------------
@@ -411,7 +411,7 @@ void launch_individuals(const LaunchCfg& L, const PopDev* pops, uint32_t npops) 
 // fixed association order), plus the total and the all-equal check.
 __global__ void __launch_bounds__(1024) k_fscan_a(const PopDev* __restrict__ pops, uint32_t npops) {
     __shared__ double s_w[32];
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         DevStatus* st = P.st;
         const uint32_t N = st->N;
@@ -451,7 +451,7 @@ __global__ void k_fscan_b(const PopDev* __restrict__ pops, uint32_t npops) {
 }
 __global__ void __launch_bounds__(1024) k_fscan_c(const PopDev* __restrict__ pops, uint32_t npops) {
     __shared__ double s_w[32];
-    for (uint32_t p = 0; p < npops; ++p) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         DevStatus* st = P.st;
         const uint32_t N = st->N;
@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(1024) k_fscan_c(const PopDev* __restrict__ pop
 }
 void launch_cdf(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxN) {
     const uint32_t nch = (maxN + kScanChunk - 1) / kScanChunk;
-    const uint32_t g = max(1u, min(nch, (uint32_t)L.num_sms * 2u));
+    const dim3 g = pop_grid(npops, nch, L.num_sms, 2);
     k_fscan_a<<<g, 1024, 0, L.stream>>>(pops, npops);
     k_fscan_b<<<npops, 32, 0, L.stream>>>(pops, npops);
     k_fscan_c<<<g, 1024, 0, L.stream>>>(pops, npops);
