@@ -65,6 +65,9 @@ std::vector<size_t> sizes_of(const Geometry& g) {
         A <= kSufMaxSlots ? A * 4 : 0,                            // inv
         A <= kSufMaxSlots ? (A / 64 + 1) * W * 8 : 0,             // suf
         A <= kSufMaxSlots ? S * 16 : 0,                           // plan_row
+        A <= kSufMaxSlots ? (S + 1) * 4 * 2 : 0,                  // ord_cnt + ord_off
+        A <= kSufMaxSlots ? S * 4 : 0,                            // ord_cur
+        A <= kSufMaxSlots ? S * 4 : 0,                            // ord_pos
         A <= kSufMaxSlots ? g.EVcap * 4ull : 0,                   // plan_go
         A <= kSufMaxSlots ? g.EVcap * 4ull : 0,                   // plan_cr
         sizeof(DevStatus),
@@ -169,7 +172,11 @@ int alloc_pop(clotho_ctx* ctx, const clotho_desc& d, PopHost** out) {
     b.boff = b.bcnt + (g.NB + 1);
     b.bcur = (uint32_t*)ptr[k++]; b.bpos = (double*)ptr[k++]; b.bslot = (uint32_t*)ptr[k++];
     b.rank = (uint32_t*)ptr[k++]; b.inv = (uint32_t*)ptr[k++]; b.suf = (uint64_t*)ptr[k++];
-    b.plan_row = (uint4*)ptr[k++]; b.plan_go = (uint32_t*)ptr[k++]; b.plan_cr = (uint32_t*)ptr[k++];
+    b.plan_row = (uint4*)ptr[k++];
+    b.ord_cnt = (uint32_t*)ptr[k++];
+    b.ord_off = b.ord_cnt ? b.ord_cnt + (g.Scap + 1) : nullptr;
+    b.ord_cur = (uint32_t*)ptr[k++]; b.ord_pos = (uint32_t*)ptr[k++];
+    b.plan_go = (uint32_t*)ptr[k++]; b.plan_cr = (uint32_t*)ptr[k++];
     b.st = (DevStatus*)ptr[k++];
     b.Scap = g.Scap; b.Ncap = g.Ncap; b.Wcap = g.Wcap; b.Acap = g.Aslots; b.Mcap = g.Mcap;
     b.EVcap = g.EVcap; b.FXcap = g.FXcap; b.T = g.T; b.NB = g.NB;

@@ -12,7 +12,10 @@
 namespace clotho {
 
 constexpr uint32_t kMaxTraits = 4;
-constexpr uint32_t kGenThreads = 512;      // 16 warps per CTA, one CTA per SM, in the generation kernel
+#ifndef CLOTHO_GEN_THREADS
+#define CLOTHO_GEN_THREADS 512
+#endif
+constexpr uint32_t kGenThreads = CLOTHO_GEN_THREADS;  // one CTA per SM in the generation kernel
 constexpr uint32_t kRowsPerItem = 512;     // default child rows per scheduling item (tunable)
 constexpr uint32_t kMaxEvReg = 16;         // events held in registers
 constexpr uint32_t kMaxEvDevice = 128;     // device-drawn events per gamete
@@ -88,7 +91,11 @@ struct PopDev {
     uint32_t* rank;        // [Acap] rank of each slot (position, then slot index) among the A slots
     uint32_t* inv;         // [Acap] slot of each rank (Acap <= kSufMaxSlots, else null)
     uint64_t* suf;         // [(Acap/64 + 1) * Wcap] suffix table of the crossover classifier (or null)
-    uint4*    plan_row;    // [Scap] per-row crossover plan: top strand, events, event base, flags (with suf)
+    uint4*    plan_row;    // [Scap] crossover plans in processing order: row, top strand, event base, events | flags << 30
+    uint32_t* ord_cnt;     // [Scap + 1] rows per ordering key (zero between steps)
+    uint32_t* ord_off;     // [Scap + 1] exclusive prefix of ord_cnt
+    uint32_t* ord_cur;     // [Scap] scatter cursors (zero between steps)
+    uint32_t* ord_pos;     // [Scap] processing position of each row
     uint32_t* plan_go;     // [EVcap] table row offset per planned event (with suf)
     uint32_t* plan_cr;     // [EVcap] correction ranks per planned event: first | count << 20 (with suf)
     DevStatus* st;
@@ -227,11 +234,13 @@ void launch_seed_rows(const LaunchCfg&, const PopDev* pops, uint32_t npops, cons
 void launch_stats(const LaunchCfg&, const PopDev* pops, uint32_t p, uint32_t* counts, uint32_t A);
 void launch_ranks(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxNB, uint32_t maxW, bool suf);
 void launch_uscan_buckets(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxNB);
+void launch_uscan_order(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
 
 void launch_plan(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
 
 // crossover-plan row flags
-constexpr uint32_t kPlanInv = 1u, kPlanLong = 2u;
+constexpr uint32_t kPlanInv = 1u, kPlanLong = 2u, kPlanFlagShift = 30u;
+constexpr uint32_t kPlanMaxEvents = (1u << kPlanFlagShift) - 1u;
 
 // fuse flags of k_generation
 constexpr uint32_t kFuseMut = 1u, kFusePheno = 2u, kFuseFs = 4u;

@@ -566,20 +566,22 @@ __device__ __forceinline__ uint32_t table_row(uint32_t r, uint32_t A, uint32_t& 
     return b;
 }
 
-// One offspring row, the whole warp (suffix-table classifier), from its plan
-// (k_row_plan): top strand, breakpoints, table rows and correction ranks.
-__device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st, uint32_t g, const uint64_t* sfix,
+// One offspring row, the whole warp (suffix-table classifier), from the plan
+// at processing position v (k_row_plan): row, top strand, breakpoints, table
+// rows and correction ranks.
+__device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st, uint32_t v, const uint64_t* sfix,
                                             uint64_t* mask, WarpSmem& ws, bool do_mut, bool do_ph, bool gather,
                                             bool do_fs, uint64_t* sF, uint64_t* sV) {
     const uint32_t lane = threadIdx.x & 31u;
-    const uint4 pr = __ldg(P.plan_row + g);
-    const uint32_t E = pr.y, base = pr.z;
-    const bool inv = gather && (pr.w & kPlanInv) != 0;
+    const uint4 pr = __ldg(P.plan_row + v);
+    const uint32_t g = pr.x, topr = pr.y, base = pr.z;
+    const uint32_t E = pr.w & kPlanMaxEvents, flags = pr.w >> kPlanFlagShift;
+    const bool inv = gather && (flags & kPlanInv) != 0;
     const uint64_t* prow = P.rows[st.cur ^ 1u];
     RowArgs R;
-    R.topr = pr.x;
-    R.top = prow + (size_t)pr.x * P.Wcap;
-    R.bot = prow + (size_t)(pr.x ^ 1u) * P.Wcap;
+    R.topr = topr;
+    R.top = prow + (size_t)topr * P.Wcap;
+    R.bot = prow + (size_t)(topr ^ 1u) * P.Wcap;
     R.out = P.rows[st.cur] + (size_t)g * P.Wcap;
     R.Wc = st.W;
     R.Wp = st.pW;
@@ -590,10 +592,10 @@ __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st
     if (E > 0) prefetch_l2(R.bot, R.Wp * 8u);
     R.zbase = 0.0;
     if (do_ph && lane < kMaxTraits)
-        R.zbase = P.zg[st.cur ^ 1u][(size_t)(inv ? pr.x ^ 1u : pr.x) * 4u + lane] - P.st->fixsum[lane];
+        R.zbase = P.zg[st.cur ^ 1u][(size_t)(inv ? topr ^ 1u : topr) * 4u + lane] - P.st->fixsum[lane];
     float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
     row_mutation_setup(P, st, g, do_mut, gather, R, d);
-    if (pr.w & kPlanLong) {
+    if (flags & kPlanLong) {
         add4(d, row_body_events(P, st.M, R, sfix, ws.q, do_mut, gather, do_fs, sF, sV));
     } else if (E == 0) {
         row_body_copy(P, st.M, R, sfix, do_mut, do_fs, sF, sV);
@@ -985,12 +987,13 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             if (lane == 0) k = atomicAdd(&s_next, 1u);
             const uint32_t v = r0 + __shfl_sync(0xffffffffu, k, 0);
             if (v >= r1) break;
-            // even gametes first, then odd ones: the second gamete of a mate pair
-            // is a copy row under the reference's crossover rule, so a CTA runs
-            // one kind of row at a time
+            // interval classifier: even gametes first, then odd ones (the second
+            // gamete of a mate pair is a copy row under the reference's crossover
+            // rule), so a CTA runs one kind of row at a time; the suffix-table
+            // path takes its rows in plan order
             const uint32_t g = v < Se ? 2u * v : 2u * (v - Se) + 1u;
             if (SUF)
-                gen_row_suf(P, st, g, sfix, mask, ws, do_mut, do_ph, gather, do_fs, sF, sV);
+                gen_row_suf(P, st, v, sfix, mask, ws, do_mut, do_ph, gather, do_fs, sF, sV);
             else
                 gen_row_iv(P, st, g, sfix, s_iv[warp], s_thr[warp], s_q[warp], s_sm[warp], do_mut, do_ph, gather,
                            do_fs, sF, sV);
@@ -1017,8 +1020,8 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
 void launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, WorkCtl* ctl, uint32_t maxW,
                        uint32_t maxA, uint32_t fuse, int profile) {
     const bool suf = maxA <= kSufMaxSlots;
-    // the interval classifier keeps 56 KB of static shared memory
-    const uint32_t gacc = (!suf && 3ull * maxW * sizeof(uint64_t) > 160u * 1024u) ? 1u : 0u;
+    // the interval classifier keeps 3.5 KB of static shared memory per warp
+    const uint32_t gacc = (!suf && 3ull * maxW * sizeof(uint64_t) + kWarps * 3584u > 220u * 1024u) ? 1u : 0u;
     const size_t smem =
         gacc ? 0 : (3ull + (suf ? kWarps : 0u)) * maxW * sizeof(uint64_t) + (suf ? kWarps * sizeof(WarpSmem) : 0);
     static size_t configured[2] = {0, 0};
@@ -1033,6 +1036,49 @@ void launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, W
         k_generation<true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, 0u);
     else
         k_generation<false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, gacc);
+}
+
+// ---------------------------------------------------------------------------
+// Processing order of the offspring rows (parent-major): rows are sorted by
+// parent individual, so rows reading the same parent strands run side by side
+// and the second read of a strand is an L2 hit.  Counting sort by key; the
+// order inside one key does not matter (rows are independent).  Keys 0 and 2
+// (by gamete parity first) are kept for measurement.
+#ifndef CLOTHO_ORDER_KEY
+#define CLOTHO_ORDER_KEY 1
+#endif
+__device__ __forceinline__ uint32_t order_key(const PopDev& P, uint32_t g, uint32_t N, uint32_t pN) {
+    uint32_t pind = P.pairs[g];
+    if (pind >= pN) pind = 0;
+#if CLOTHO_ORDER_KEY == 1
+    return pind;                                  // parent only
+#elif CLOTHO_ORDER_KEY == 2
+    return (g & 1u) * N + (g >> 1);               // even rows, then odd rows
+#else
+    return (g & 1u) * N + pind;                   // parity, then parent
+#endif
+}
+
+__global__ void k_ord_count(const PopDev* __restrict__ pops, uint32_t npops) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
+        const PopDev& P = pops[p];
+        if (!P.plan_row) continue;
+        const uint32_t N = P.st->N, pN = P.st->pN, S = 2u * N;
+        for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < S; g += gridDim.x * blockDim.x)
+            atomicAdd(&P.ord_cnt[order_key(P, g, N, pN)], 1u);
+    }
+}
+
+__global__ void k_ord_scatter(const PopDev* __restrict__ pops, uint32_t npops) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
+        const PopDev& P = pops[p];
+        if (!P.plan_row) continue;
+        const uint32_t N = P.st->N, pN = P.st->pN, S = 2u * N;
+        for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < S; g += gridDim.x * blockDim.x) {
+            const uint32_t key = order_key(P, g, N, pN);
+            P.ord_pos[g] = P.ord_off[key] + atomicAdd(&P.ord_cur[key], 1u);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1142,13 +1188,22 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
                     cr[k] = c0 | (n << 20);
                 }
             }
-            P.plan_row[g] = make_uint4(2u * pind + (swap ? 1u : 0u), E, base, flags);
+            if (E > kPlanMaxEvents) {
+                atomicOr(&P.st->err, kErrEvents);
+                E = 0;
+                flags = 0;
+            }
+            P.plan_row[P.ord_pos[g]] = make_uint4(g, 2u * pind + (swap ? 1u : 0u), base, E | (flags << kPlanFlagShift));
         }
     }
 }
 
 void launch_plan(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
-    k_row_plan<<<pop_grid(npops, blocks_for(maxS, 256), L.num_sms, 8), 256, 0, L.stream>>>(pops, npops);
+    const dim3 g = pop_grid(npops, blocks_for(maxS, 256), L.num_sms, 8);
+    k_ord_count<<<g, 256, 0, L.stream>>>(pops, npops);
+    launch_uscan_order(L, pops, npops, maxS);
+    k_ord_scatter<<<g, 256, 0, L.stream>>>(pops, npops);
+    k_row_plan<<<g, 256, 0, L.stream>>>(pops, npops);
 }
 
 // ---------------------------------------------------------------------------

@@ -97,9 +97,10 @@ struct ScanSel {
     uint32_t L;      // elements (counts) to scan; off gets L entries
     uint32_t ncur;   // cursors to zero
 };
-// which == 0: per-row mutation counts; which == 1: position buckets
+// which == 0: per-row mutation counts; 1: position buckets; 2: rows per ordering key
 __device__ inline ScanSel scan_sel(const PopDev& P, int which) {
     if (which == 0) return ScanSel{P.row_cnt, P.row_off, P.row_cur, 2u * P.st->N + 1u, 2u * P.st->N};
+    if (which == 2) return ScanSel{P.ord_cnt, P.ord_off, P.ord_cur, 2u * P.st->N + 1u, 2u * P.st->N};
     return ScanSel{P.bcnt, P.boff, P.bcur, P.NB + 1u, P.NB};
 }
 
@@ -191,6 +192,9 @@ static void launch_uscan(const LaunchCfg& L, const PopDev* pops, uint32_t npops,
 
 void launch_uscan_buckets(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxNB) {
     launch_uscan(L, pops, npops, maxNB, 1, 0);
+}
+void launch_uscan_order(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
+    launch_uscan(L, pops, npops, maxS, 2, 0);
 }
 
 // ---------------------------------------------------------------------------
