@@ -248,6 +248,42 @@ class Population:
         self._ck(self.L.clotho_get_pairs(self.h, _ptr(out)), "get_pairs")
         return out
 
+    def margins(self):
+        """(col_counts[A], row_counts[2N]): sequences per allele slot, alleles per sequence."""
+        i = self.info()
+        col = np.zeros(max(1, i["A"]), np.uint32)
+        row = np.zeros(max(1, 2 * i["N"]), np.uint32)
+        self._ck(self.L.clotho_margins(self.h, _ptr(col), _ptr(row)), "margins")
+        return col[: i["A"]], row[: 2 * i["N"]]
+
+    def allele_frequency_log(self) -> dict:
+        """The reference's `allele_frequency` log entry for the whole population."""
+        from . import logs
+        col, row = self.margins()
+        return logs.allele_frequency(col, row, 2 * self.info()["N"])
+
+    # ---- checkpoint / resume (between generations)
+    def snapshot(self) -> bytes:
+        n = int(self.L.clotho_snapshot_size(self.h))
+        if n == 0:
+            msg = self.L.clotho_last_error(self.h)
+            raise ClothoError("snapshot: " + (msg.decode() if msg else "no snapshot can be taken now"))
+        buf = np.empty(n, np.uint8)
+        self._ck(self.L.clotho_snapshot(self.h, _ptr(buf), n), "snapshot")
+        return buf.tobytes()
+
+    def restore(self, data: bytes):
+        buf = np.frombuffer(data, np.uint8).copy()
+        self._ck(self.L.clotho_restore(self.h, _ptr(buf), buf.size), "restore")
+
+    def save(self, path: str):
+        with open(path, "wb") as f:
+            f.write(self.snapshot())
+
+    def load(self, path: str):
+        with open(path, "rb") as f:
+            self.restore(f.read())
+
     def stats(self, sfs_len: int = 0):
         st = capi.Stats()
         sfs = np.zeros(sfs_len, np.uint32) if sfs_len else None
@@ -400,6 +436,14 @@ class Batch:
         if sfs is not None:
             d["sfs"] = sfs
         return d
+
+    def margins(self, i: int):
+        """(col_counts[A], row_counts[2N]) of population i."""
+        inf = self.info(i)
+        col = np.zeros(max(1, inf["A"]), np.uint32)
+        row = np.zeros(max(1, 2 * inf["N"]), np.uint32)
+        self._ck(self.L.clotho_pop_margins(self.h, i, _ptr(col), _ptr(row)), "pop_margins")
+        return col[: inf["A"]], row[: 2 * inf["N"]]
 
     @property
     def footprint(self) -> int:

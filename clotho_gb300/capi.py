@@ -77,6 +77,11 @@ SIGNATURES = {
     "clotho_get_fitness": (C.c_int, [vp, vp]),
     "clotho_get_pairs": (C.c_int, [vp, vp]),
     "clotho_stats_compute": (C.c_int, [vp, C.POINTER(Stats), vp, u32]),
+    "clotho_margins": (C.c_int, [vp, vp, vp]),
+    "clotho_pop_margins": (C.c_int, [vp, u32, vp, vp]),
+    "clotho_snapshot_size": (C.c_size_t, [vp]),
+    "clotho_snapshot": (C.c_int, [vp, vp, C.c_size_t]),
+    "clotho_restore": (C.c_int, [vp, vp, C.c_size_t]),
     "clotho_profile": (C.c_int, [vp, C.c_int]),
     "clotho_kernel_time": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(u32), C.POINTER(u64), C.POINTER(u64)]),
     "clotho_timer_begin": (C.c_int, [vp]),

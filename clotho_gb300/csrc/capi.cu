@@ -99,6 +99,7 @@ struct clotho_ctx {
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     uint64_t launches = 0;
     cudaGraphExec_t graph = nullptr;
+    uint64_t graph_launches = 0;  // kernels per replay of graph
     std::vector<uint32_t> graph_key;
     bool in_step = false;
     uint32_t maxW = 0, maxS = 0, maxN = 0, maxNB = 0, maxA = 0;
@@ -272,7 +273,7 @@ int prof_collect(clotho_ctx* ctx) {
 void launch_gen(clotho_ctx* ctx, const PopDev* pops, uint32_t npops, uint32_t fuse) {
     if (ctx->maxA <= kSufMaxSlots) {  // per-row crossover plans of the suffix-table classifier
         launch_plan(cfg(ctx), pops, npops, ctx->maxS);
-        ctx->launches += 1;
+        ctx->launches += 6;  // order count, 3-kernel scan, order scatter, plan
     }
     prof_begin(ctx);
     launch_generation(cfg(ctx), pops, npops, ctx->d_ctl, ctx->maxW, ctx->maxA, fuse, ctx->profiling ? 1 : 0);
@@ -346,7 +347,9 @@ void enqueue_fused_step(clotho_ctx* ctx, uint32_t set, bool philox) {
     launch_individuals(L, pops, n);
     launch_cdf(L, pops, n, ctx->maxN);
     launch_end(L, pops, n);
-    ctx->launches += philox ? 20 : 21;
+    // begin, mutation counts or CSR (4 or 5), finalize, resolve, ranks (6, + suffix table), selection (device
+    // draws), individuals, 3-kernel prefix sum, end; launch_gen and ensure_parent_acc count their own
+    ctx->launches += 19u + (ctx->maxA <= kSufMaxSlots ? 1u : 0u);
     for (PopHost* p : ctx->pops) p->acc_valid = true;
 }
 
@@ -638,7 +641,10 @@ int clotho_run_philox(clotho_ctx* ctx, uint32_t N, uint32_t G) {
         cudaGraph_t gr;
         CK(cudaStreamSynchronize(ctx->stream));
         CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        const uint64_t l0 = ctx->launches;
         enqueue_fused_step(ctx, 2, true);
+        ctx->graph_launches = ctx->launches - l0;
+        ctx->launches = l0;
         CK(cudaStreamEndCapture(ctx->stream, &gr));
         CK(cudaGraphInstantiate(&ctx->graph, gr, 0));
         cudaGraphDestroy(gr);
@@ -646,7 +652,7 @@ int clotho_run_philox(clotho_ctx* ctx, uint32_t N, uint32_t G) {
     }
     for (uint32_t g = 1; g < G; ++g) {
         CK(cudaGraphLaunch(ctx->graph, ctx->stream));
-        ctx->launches += 20;
+        ctx->launches += ctx->graph_launches;
     }
     return 0;
 }
@@ -730,7 +736,7 @@ int clotho_crossover(clotho_ctx* ctx, const uint8_t* swap, const uint32_t* ev_of
     if ((rc = h2d(ctx, D.ev_pos, ev_pos, (size_t)ev_total, ctx->stream))) return rc;
     // item prefix is already set by begin; ranks over the current positions
     launch_ranks(cfg(ctx), ctx->d_pops[0], 1, ctx->maxNB, ctx->maxW, ctx->maxA <= kSufMaxSlots);
-    ctx->launches += 6;
+    ctx->launches += 6u + (ctx->maxA <= kSufMaxSlots ? 1u : 0u);
     launch_gen(ctx, ctx->d_pops[0], 1, 0u);
     if ((rc = check_launch(ctx, "crossover"))) return rc;
     CK(cudaStreamSynchronize(ctx->stream));
@@ -965,6 +971,189 @@ int clotho_stats_compute(clotho_ctx* ctx, clotho_stats* out, uint32_t* sfs, uint
     return stats_of(ctx, 0, out, sfs, sfs_len);
 }
 
+static int margins_of(clotho_ctx* ctx, uint32_t idx, uint32_t* col, uint32_t* row) {
+    if (!ctx || idx >= ctx->pops.size()) return fail(ctx, CLOTHO_E_ARG, "no such population");
+    int rc;
+    PopHost* p = ctx->pops[idx];
+    const DevStatus s = read_status(ctx, p, &rc);
+    if (rc) return rc;
+    const uint32_t S = 2 * s.N;
+    const size_t ncol = std::max<size_t>(1, (size_t)s.W * 64), nrow = std::max<uint32_t>(1, S);
+    uint32_t* d = nullptr;
+    CK(cudaMalloc(&d, (ncol + nrow) * 4));
+    CK(cudaMemsetAsync(d, 0, (ncol + nrow) * 4, ctx->stream));
+    if (col && S && s.W) launch_stats(cfg(ctx), ctx->d_pops[0], idx, d, s.W);
+    if (row && S) launch_row_counts(cfg(ctx), ctx->d_pops[0], idx, d + ncol, S);
+    if (col && s.A) CK(cudaMemcpyAsync(col, d, (size_t)s.A * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (row && S) CK(cudaMemcpyAsync(row, d + ncol, (size_t)S * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(d);
+    ctx->launches += (col ? 1 : 0) + (row ? 1 : 0);
+    return check_launch(ctx, "margins");
+}
+
+int clotho_margins(clotho_ctx* ctx, uint32_t* col, uint32_t* row) { return margins_of(ctx, 0, col, row); }
+int clotho_pop_margins(clotho_ctx* ctx, uint32_t index, uint32_t* col, uint32_t* row) {
+    return margins_of(ctx, index, col, row);
+}
+
+// ---- checkpoint / resume ---------------------------------------------------
+namespace {
+constexpr char kSnapMagic[8] = {'C', 'L', 'O', 'T', 'H', 'O', 'S', '1'};
+
+struct SnapHeader {
+    char magic[8];
+    uint32_t version, header_bytes;
+    clotho_desc desc;
+    DevStatus st;
+    uint64_t total_bytes;
+};
+
+struct SnapLayout {
+    size_t rows, pos, age, eff, fx_pos, fx_age, fx_eff, free_list, zg, zi, fit, cdf, total;
+};
+
+// Byte offsets of the sections after the header, each 8-byte aligned.
+SnapLayout snap_layout(const DevStatus& st, uint32_t T) {
+    SnapLayout L{};
+    const size_t S = 2ull * st.N, N = st.N, A = st.A, F = st.fixed_total;
+    size_t o = sizeof(SnapHeader);
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o += (bytes + 7) & ~(size_t)7;
+        return at;
+    };
+    L.rows = take(S * st.W * 8);
+    L.pos = take(A * 8);
+    L.age = take(A * 4);
+    L.eff = take(A * 16);
+    L.fx_pos = take(F * 8);
+    L.fx_age = take(F * 4);
+    L.fx_eff = take(F * T * 4);
+    L.free_list = take((size_t)st.free_cnt * 4);
+    L.zg = take(S * 32);
+    L.zi = take(N * 32);
+    L.fit = take(N * 8);
+    L.cdf = take(N * 8);
+    L.total = o;
+    return L;
+}
+
+bool same_parameters(const clotho_desc& a, const clotho_desc& b) {
+    return a.traits == b.traits && a.fitness == b.fitness && a.flags == b.flags && a.fit_param == b.fit_param &&
+           a.mu == b.mu && a.rho == b.rho && a.bias == b.bias && a.p_neutral == b.p_neutral &&
+           a.eff_mean == b.eff_mean && a.eff_sigma == b.eff_sigma && a.seed == b.seed;
+}
+}  // namespace
+
+size_t clotho_snapshot_size(clotho_ctx* ctx) {
+    if (!ctx || ctx->pops.size() != 1 || ctx->in_step || !ctx->pops[0]->ready) return 0;
+    int rc;
+    const DevStatus st = read_status(ctx, ctx->pops[0], &rc);
+    return rc ? 0 : snap_layout(st, ctx->pops[0]->dev[0].T).total;
+}
+
+int clotho_snapshot(clotho_ctx* ctx, void* dst, size_t len) {
+    if (!ctx || !dst) return CLOTHO_E_ARG;
+    if (ctx->pops.size() != 1) return fail(ctx, CLOTHO_E_ARG, "snapshot takes a single-population context");
+    if (ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "snapshot between generations only");
+    PopHost* p = ctx->pops[0];
+    if (!p->ready) return fail(ctx, CLOTHO_E_STATE, "population not initialised");
+    int rc;
+    const DevStatus st = read_status(ctx, p, &rc);
+    if (rc) return rc;
+    const PopDev& D = p->dev[0];
+    const SnapLayout L = snap_layout(st, D.T);
+    if (len < L.total) return fail(ctx, CLOTHO_E_CAPACITY, "snapshot buffer too small");
+    char* b = static_cast<char*>(dst);
+    SnapHeader h{};
+    std::memcpy(h.magic, kSnapMagic, 8);
+    h.version = 1;
+    h.header_bytes = sizeof(SnapHeader);
+    h.desc = p->desc;
+    h.st = st;
+    h.total_bytes = L.total;
+    std::memcpy(b, &h, sizeof(h));
+    const size_t S = 2ull * st.N, F = st.fixed_total;
+    cudaStream_t s = ctx->stream;
+    if (S * st.W)
+        CK(cudaMemcpy2DAsync(b + L.rows, (size_t)st.W * 8, D.rows[st.cur], (size_t)D.Wcap * 8, (size_t)st.W * 8, S,
+                             cudaMemcpyDeviceToHost, s));
+    if (st.A) {
+        CK(cudaMemcpyAsync(b + L.pos, D.pos, (size_t)st.A * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(b + L.age, D.age, (size_t)st.A * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(b + L.eff, D.eff, (size_t)st.A * 16, cudaMemcpyDeviceToHost, s));
+    }
+    if (F) {
+        CK(cudaMemcpyAsync(b + L.fx_pos, D.fx_pos, F * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(b + L.fx_age, D.fx_age, F * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(b + L.fx_eff, D.fx_eff, F * D.T * 4, cudaMemcpyDeviceToHost, s));
+    }
+    if (st.free_cnt)
+        CK(cudaMemcpyAsync(b + L.free_list, D.free_list, (size_t)st.free_cnt * 4, cudaMemcpyDeviceToHost, s));
+    if (S) CK(cudaMemcpyAsync(b + L.zg, D.zg[st.cur], S * 32, cudaMemcpyDeviceToHost, s));
+    if (st.N) {
+        CK(cudaMemcpyAsync(b + L.zi, D.zi, (size_t)st.N * 32, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(b + L.fit, D.fit, (size_t)st.N * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(b + L.cdf, D.cdf, (size_t)st.N * 8, cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    return 0;
+}
+
+int clotho_restore(clotho_ctx* ctx, const void* src, size_t len) {
+    if (!ctx || !src) return CLOTHO_E_ARG;
+    if (ctx->pops.size() != 1) return fail(ctx, CLOTHO_E_ARG, "restore takes a single-population context");
+    if (ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "restore between generations only");
+    if (len < sizeof(SnapHeader)) return fail(ctx, CLOTHO_E_ARG, "not a snapshot (too short)");
+    SnapHeader h;
+    std::memcpy(&h, src, sizeof(h));
+    if (std::memcmp(h.magic, kSnapMagic, 8) != 0 || h.version != 1 || h.header_bytes != sizeof(SnapHeader))
+        return fail(ctx, CLOTHO_E_ARG, "not a snapshot of this library version");
+    PopHost* p = ctx->pops[0];
+    const PopDev& D = p->dev[0];
+    const DevStatus st = h.st;
+    if (st.cur > 1u || st.W != ref_width(st.A)) return fail(ctx, CLOTHO_E_ARG, "snapshot status is inconsistent");
+    const SnapLayout L = snap_layout(st, D.T);
+    if (h.total_bytes != L.total || len < L.total) return fail(ctx, CLOTHO_E_ARG, "snapshot truncated");
+    if (!same_parameters(h.desc, p->desc))
+        return fail(ctx, CLOTHO_E_ARG, "snapshot parameters differ from the context's");
+    if (st.N > D.Ncap || st.A > D.Acap || st.W > D.Wcap || st.fixed_total > D.FXcap || st.free_cnt > D.Acap)
+        return fail(ctx, CLOTHO_E_CAPACITY, "snapshot does not fit the context's capacities");
+    int rc = init_pop(ctx, 0, st.N);  // zeroed tables and counters
+    if (rc) return rc;
+    const char* b = static_cast<const char*>(src);
+    const size_t S = 2ull * st.N, F = st.fixed_total;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(D.st, &st, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
+    if (S * st.W)
+        CK(cudaMemcpy2DAsync(D.rows[st.cur], (size_t)D.Wcap * 8, b + L.rows, (size_t)st.W * 8, (size_t)st.W * 8, S,
+                             cudaMemcpyHostToDevice, s));
+    if (st.A) {
+        CK(cudaMemcpyAsync(D.pos, b + L.pos, (size_t)st.A * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(D.age, b + L.age, (size_t)st.A * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(D.eff, b + L.eff, (size_t)st.A * 16, cudaMemcpyHostToDevice, s));
+    }
+    if (F) {
+        CK(cudaMemcpyAsync(D.fx_pos, b + L.fx_pos, F * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(D.fx_age, b + L.fx_age, F * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(D.fx_eff, b + L.fx_eff, F * D.T * 4, cudaMemcpyHostToDevice, s));
+    }
+    if (st.free_cnt)
+        CK(cudaMemcpyAsync(D.free_list, b + L.free_list, (size_t)st.free_cnt * 4, cudaMemcpyHostToDevice, s));
+    if (S) CK(cudaMemcpyAsync(D.zg[st.cur], b + L.zg, S * 32, cudaMemcpyHostToDevice, s));
+    if (st.N) {
+        CK(cudaMemcpyAsync(D.zi, b + L.zi, (size_t)st.N * 32, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(D.fit, b + L.fit, (size_t)st.N * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(D.cdf, b + L.cdf, (size_t)st.N * 8, cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    p->acc_valid = false;  // the next step reduces the restored rows again
+    p->hostN = st.N;
+    if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+    return 0;
+}
+
 // ---- timing --------------------------------------------------------------
 int clotho_profile(clotho_ctx* ctx, int enable) {
     if (!ctx) return CLOTHO_E_ARG;
@@ -1130,7 +1319,10 @@ int clotho_batch_run_philox(clotho_ctx* ctx, const uint32_t* N, uint32_t G) {
         cudaGraph_t gr;
         CK(cudaStreamSynchronize(ctx->stream));
         CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        const uint64_t l0 = ctx->launches;
         enqueue_fused_step(ctx, 2, true);
+        ctx->graph_launches = ctx->launches - l0;
+        ctx->launches = l0;
         CK(cudaStreamEndCapture(ctx->stream, &gr));
         CK(cudaGraphInstantiate(&ctx->graph, gr, 0));
         cudaGraphDestroy(gr);
@@ -1138,7 +1330,7 @@ int clotho_batch_run_philox(clotho_ctx* ctx, const uint32_t* N, uint32_t G) {
     }
     for (uint32_t g = 1; g < G; ++g) {
         CK(cudaGraphLaunch(ctx->graph, ctx->stream));
-        ctx->launches += 20;
+        ctx->launches += ctx->graph_launches;
     }
     return 0;
 }

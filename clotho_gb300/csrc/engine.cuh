@@ -232,6 +232,7 @@ void launch_end(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_seed_rows(const LaunchCfg&, const PopDev* pops, uint32_t npops, const uint32_t* thr,
                       uint64_t seed, uint32_t A);
 void launch_stats(const LaunchCfg&, const PopDev* pops, uint32_t p, uint32_t* counts, uint32_t A);
+void launch_row_counts(const LaunchCfg&, const PopDev* pops, uint32_t p, uint32_t* counts, uint32_t S);
 void launch_ranks(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxNB, uint32_t maxW, bool suf);
 void launch_uscan_buckets(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxNB);
 void launch_uscan_order(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);

@@ -545,4 +545,25 @@ void launch_stats(const LaunchCfg& L, const PopDev* pops, uint32_t p, uint32_t* 
     k_col_counts<<<grid, 64, 0, L.stream>>>(pops, p, counts, W * 64u);
 }
 
+// Row margins: alleles carried by each sequence (the row margin of
+// population_space_row_frequency_evaluator.hpp:37-62), one warp per row.
+__global__ void __launch_bounds__(256) k_row_counts(const PopDev* __restrict__ pops, uint32_t p,
+                                                    uint32_t* __restrict__ counts) {
+    const PopDev& P = pops[p];
+    const DevStatus* st = P.st;
+    const uint32_t S = 2u * st->N, W = st->W;
+    const uint64_t* rows = P.rows[st->cur];
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < S; r += (gridDim.x * blockDim.x) >> 5) {
+        uint32_t c = 0;
+        for (uint32_t w = lane; w < W; w += 32u) c += (uint32_t)__popcll(rows[(size_t)r * P.Wcap + w]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if (lane == 0) counts[r] = c;
+    }
+}
+void launch_row_counts(const LaunchCfg& L, const PopDev* pops, uint32_t p, uint32_t* counts, uint32_t S) {
+    k_row_counts<<<max(1u, min(blocks_for(S, 8), (uint32_t)L.num_sms * 8u)), 256, 0, L.stream>>>(pops, p, counts);
+}
+
 }  // namespace clotho

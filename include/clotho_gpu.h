@@ -146,6 +146,23 @@ int  clotho_seed_population(clotho_ctx *ctx, uint32_t N, uint32_t A, const doubl
 int  clotho_load_population(clotho_ctx *ctx, uint32_t N, uint32_t A, const uint64_t *rows,
                             const double *pos, const float *eff);
 
+/* ---- checkpoint / resume --------------------------------------------------
+ * The reference keeps its state in host objects and writes logs only
+ * (engine_batched_task.hpp:233-242); these calls save and restore one
+ * population between generations so that a run can be resumed.  A snapshot
+ * holds the description, the status word (generation, sizes, counts), the
+ * current rows, the allele and fixed-allele tables, the last free list,
+ * per-genome trait sums,
+ * phenotypes, fitness and its prefix sum.  Device-drawn generations are keyed
+ * by (seed, generation), so a restored population continues bit for bit as
+ * the uninterrupted one.  Restore needs a single-population context whose
+ * parameters (traits, fitness, flags, fit_param, mu, rho, bias, p_neutral,
+ * eff_mean, eff_sigma, seed) equal the snapshot's and whose capacities hold
+ * it; clotho_snapshot_size returns 0 when no snapshot can be taken. */
+size_t clotho_snapshot_size(clotho_ctx *ctx);
+int  clotho_snapshot(clotho_ctx *ctx, void *dst, size_t len);
+int  clotho_restore(clotho_ctx *ctx, const void *src, size_t len);
+
 /* ---- fused generation (the hot path) ------------------------------------ */
 /* Engine::simulate() (engine_batched_task.hpp:163-223) with the tape standing
  * in for the RNG draws: free space + fixed removal (FreeSpaceAnalyzerMT,
@@ -214,6 +231,10 @@ typedef struct clotho_stats {
 /* sfs may be NULL; else sfs[k] for k in [0, sfs_len) counts slots carried by
  * exactly k rows (k = 2N folded into the last bin when sfs_len <= 2N). */
 int  clotho_stats_compute(clotho_ctx *ctx, clotho_stats *out, uint32_t *sfs, uint32_t sfs_len);
+/* Margins of the current rows (population_space_row_frequency_evaluator.hpp:37-62,
+ * margin_details.hpp:50-98): col_counts[A] = sequences carrying each allele
+ * slot, row_counts[2N] = alleles carried by each sequence.  Either may be NULL. */
+int  clotho_margins(clotho_ctx *ctx, uint32_t *col_counts, uint32_t *row_counts);
 
 /* ---- timing ------------------------------------------------------------- */
 /* CUDA events on the context stream around the fused generation kernel.
@@ -251,6 +272,7 @@ int  clotho_pop_init(clotho_ctx *ctx, uint32_t index, uint32_t N0);
 int  clotho_pop_info(clotho_ctx *ctx, uint32_t index, clotho_info *out);
 int  clotho_pop_rows(clotho_ctx *ctx, uint32_t index, uint64_t *dst, size_t dst_words);
 int  clotho_pop_stats(clotho_ctx *ctx, uint32_t index, clotho_stats *out, uint32_t *sfs, uint32_t sfs_len);
+int  clotho_pop_margins(clotho_ctx *ctx, uint32_t index, uint32_t *col_counts, uint32_t *row_counts);
 /* One device-drawn generation of every population (N[i] offspring). */
 int  clotho_batch_generation_philox(clotho_ctx *ctx, const uint32_t *N);
 /* G such generations, replayed from one captured CUDA graph. */

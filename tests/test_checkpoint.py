@@ -1,0 +1,130 @@
+"""Checkpoint / resume and population margins through the C-ABI.
+
+A population saved between generations and restored into a fresh context
+continues exactly as the uninterrupted run: device-drawn generations are keyed
+by (seed, generation), so rows, phenotypes and fitness are bit-identical, and a
+tape-driven run stays bit-exact against the oracle after the restore.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from tests.conftest import gpu_available
+
+pytestmark = pytest.mark.gpu
+
+if not gpu_available():  # collected on CPU machines, skipped there
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+import clotho_gb300 as cg  # noqa: E402
+from tests.test_gpu_parity import compare_state, make_pair  # noqa: E402
+
+KW = dict(fitness="gaussian_vs", fit_param=3.0, mu=0.05, rho=2.0, p_neutral=0.3, seed=77,
+          max_events=1 << 15, max_mutations=1 << 13, max_fixed=1 << 14)
+
+
+def _state(pop):
+    i = pop.info()
+    return pop.rows(), pop.phenotypes(), pop.fitness(), pop.alleles(), pop.fixed(), i
+
+
+def _same(a, b):
+    ra, pa, fa, (posa, agea, effa), (fpa, faa, fea), ia = a
+    rb, pb, fb, (posb, ageb, effb), (fpb, fab, feb), ib = b
+    assert ia == ib
+    assert np.array_equal(ra, rb)
+    assert np.array_equal(pa, pb) and np.array_equal(fa, fb)
+    assert np.array_equal(posa, posb) and np.array_equal(agea, ageb) and np.array_equal(effa, effb)
+    assert np.array_equal(fpa, fpb) and np.array_equal(faa, fab) and np.array_equal(fea, feb)
+
+
+def test_resume_device_drawn_run_is_bit_identical(tmp_path):
+    N = 1500
+    a = cg.Population(N, 1 << 13, 2, **KW)
+    a.init(N)
+    for _ in range(6):
+        a.simulate_philox(N)
+    snap = a.snapshot()
+    a.save(str(tmp_path / "pop.ckpt"))
+    a.run_philox(N, 5)
+    a.check()
+    ref = _state(a)
+
+    b = cg.Population(N, 1 << 13, 2, **KW)  # fresh context, same parameters
+    b.restore(snap)
+    assert b.info()["generation"] == 7
+    b.run_philox(N, 5)
+    b.check()
+    _same(ref, _state(b))
+
+    c = cg.Population(2 * N, 1 << 14, 2, **KW)  # larger capacities hold it too; restored from the file
+    c.load(str(tmp_path / "pop.ckpt"))
+    for _ in range(5):
+        c.simulate_philox(N)
+    _same(ref, _state(c))
+    for p in (a, b, c):
+        p.close()
+
+
+def test_resume_tape_run_stays_bit_exact_against_the_oracle():
+    N = 200
+    orc, gpu = make_pair(N, 8192, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.2, rho=1.5, p_neutral=0.4)
+    orc.init(N)
+    gpu.init(N)
+    for g in range(6):
+        gpu.simulate(orc.step_record(N))
+    snap = gpu.snapshot()
+    gpu.close()
+    _, fresh = make_pair(N, 8192, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.2, rho=1.5, p_neutral=0.4)
+    fresh.restore(snap)
+    compare_state(orc, fresh, 5, kind="gaussian_vs", fit_param=4.0)
+    for g in range(6, 12):
+        fresh.simulate(orc.step_record(N))
+        compare_state(orc, fresh, g, kind="gaussian_vs", fit_param=4.0)
+    fresh.close()
+
+
+def test_restore_rejects_other_parameters_and_damaged_snapshots():
+    N = 300
+    a = cg.Population(N, 4096, 2, **KW)
+    a.init(N)
+    a.run_philox(N, 3)
+    snap = a.snapshot()
+    other = cg.Population(N, 4096, 2, **dict(KW, rho=2.5))
+    with pytest.raises(cg.ClothoError):
+        other.restore(snap)
+    small = cg.Population(N // 2, 4096, 2, **KW)
+    with pytest.raises(cg.ClothoError):
+        small.restore(snap)
+    same = cg.Population(N, 4096, 2, **KW)
+    with pytest.raises(cg.ClothoError):
+        same.restore(snap[: len(snap) // 2])
+    with pytest.raises(cg.ClothoError):
+        same.restore(b"\0" * len(snap))
+    same.restore(snap)  # the intact snapshot still works after the refusals
+    assert same.info()["generation"] == a.info()["generation"]
+    for p in (a, other, small, same):
+        p.close()
+
+
+def test_margins_and_allele_frequency_log_match_the_rows():
+    N = 800
+    pop = cg.Population(N, 1 << 13, 1, **dict(KW, mu=0.3))
+    pop.init(N)
+    pop.run_philox(N, 15)
+    i = pop.info()
+    rows = pop.rows()
+    bits = np.unpackbits(rows.view(np.uint8).reshape(rows.shape[0], -1), axis=1, bitorder="little")
+    col, row = pop.margins()
+    assert np.array_equal(col, bits[:, : i["A"]].sum(axis=0))
+    assert np.array_equal(row, bits.sum(axis=1))
+    log = pop.allele_frequency_log()
+    assert log["distribution"] == [int(x) for x in col]
+    freq = log["frequency_distribution"]
+    assert len(freq) == 2 * N + 1 and sum(freq) == i["A"]
+    st = pop.stats(sfs_len=2 * N + 1)
+    assert np.array_equal(np.asarray(freq), st["sfs"])
+    assert st["segregating"] == int(((col > 0) & (col < 2 * N)).sum())
+    assert log["stats"]["alleles_per_sequence"]["total"] == 2 * N
+    assert log["stats"]["sequences_per_allele"]["max"] == int(col.max())
+    pop.close()
