@@ -262,6 +262,34 @@ class Population:
         col, row = self.margins()
         return logs.allele_frequency(col, row, 2 * self.info()["N"])
 
+    def pairwise_difference(self, sample=None, n: int | None = None, distances: bool = False) -> dict:
+        """Pairwise differences over sampled rows (all pairs i < j): the
+        reference's min / max / mean / median / variance plus count and total.
+        sample: row indices (default rows 0..n-1, n default 2N).  The median
+        needs the distances, so it is reported when distances=True."""
+        if sample is not None:
+            sample = np.ascontiguousarray(sample, np.uint32)
+            n = sample.size
+        elif n is None:
+            n = 2 * self.info()["N"]
+        pw = capi.Pairwise()
+        d = np.zeros(max(1, n * (n - 1) // 2), np.uint32) if distances else None
+        self._ck(self.L.clotho_pairwise_difference(self.h, _ptr(sample), n, _ptr(d) if distances else None,
+                                                    C.byref(pw)), "pairwise_difference")
+        out = {"min": pw.min, "max": pw.max, "mean": pw.mean, "variance": pw.variance, "count": pw.count,
+               "total": pw.total}
+        if distances:
+            d = d[: n * (n - 1) // 2]
+            out["median"] = float(np.median(d)) if d.size else 0.0
+            out["distances"] = d
+        return out
+
+    def write_ms(self, fp, sample=None, seeds=(0, 0, 0)):
+        """Write the sampled rows (default: all) in Hudson's ms format; returns the slots written."""
+        from . import ms
+        pos, _, _ = self.alleles()
+        return ms.write_ms(fp, self.rows(), pos, sample=sample, seeds=seeds)
+
     # ---- checkpoint / resume (between generations)
     def snapshot(self) -> bytes:
         n = int(self.L.clotho_snapshot_size(self.h))

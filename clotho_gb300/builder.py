@@ -19,7 +19,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(OUT_DIR, "libclotho_gpu.so")
 DRIVER_PATH = os.path.join(OUT_DIR, "qtlsim_gb300")
 CPP_DIR = os.path.join(HERE, "cpp")
-SOURCES = ["capi.cu", "k_freespace.cu", "k_step.cu", "k_generation.cu", "k_noalloc.cu"]
+SOURCES = ["capi.cu", "k_freespace.cu", "k_step.cu", "k_generation.cu", "k_noalloc.cu", "k_analysis.cu"]
 HEADERS = ["engine.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",

@@ -39,6 +39,11 @@ class Info(C.Structure):
         "fixed_total", "last_M", "all_neutral", "device_error")] + [("mean_fitness", C.c_double)]
 
 
+class Pairwise(C.Structure):
+    _fields_ = [("count", C.c_uint64), ("total", C.c_uint64), ("min", u32), ("max", u32),
+                ("mean", C.c_double), ("variance", C.c_double)]
+
+
 class Stats(C.Structure):
     _fields_ = [("segregating", u32), ("fixed_now", u32), ("mean_fitness", C.c_double),
                 ("mean_phenotype", C.c_double * 4), ("heterozygosity", C.c_double)]
@@ -78,6 +83,8 @@ SIGNATURES = {
     "clotho_get_pairs": (C.c_int, [vp, vp]),
     "clotho_stats_compute": (C.c_int, [vp, C.POINTER(Stats), vp, u32]),
     "clotho_margins": (C.c_int, [vp, vp, vp]),
+    "clotho_pairwise_difference": (C.c_int, [vp, vp, u32, vp, C.POINTER(Pairwise)]),
+    "clotho_pop_pairwise_difference": (C.c_int, [vp, u32, vp, u32, vp, C.POINTER(Pairwise)]),
     "clotho_pop_margins": (C.c_int, [vp, u32, vp, vp]),
     "clotho_snapshot_size": (C.c_size_t, [vp]),
     "clotho_snapshot": (C.c_int, [vp, vp, C.c_size_t]),

@@ -997,6 +997,63 @@ int clotho_pop_margins(clotho_ctx* ctx, uint32_t index, uint32_t* col, uint32_t*
     return margins_of(ctx, index, col, row);
 }
 
+static int pairwise_of(clotho_ctx* ctx, uint32_t idx, const uint32_t* sample, uint32_t n, uint32_t* dist,
+                       clotho_pairwise* out) {
+    if (!ctx || !out || idx >= ctx->pops.size()) return fail(ctx, CLOTHO_E_ARG, "no such population");
+    if (n > 65536u) return fail(ctx, CLOTHO_E_CAPACITY, "pairwise difference: sample of more than 65,536 rows");
+    if (dist && n > 16384u) return fail(ctx, CLOTHO_E_CAPACITY, "pairwise distances: sample of more than 16,384 rows");
+    int rc;
+    PopHost* p = ctx->pops[idx];
+    const DevStatus s = read_status(ctx, p, &rc);
+    if (rc) return rc;
+    const uint32_t S = 2 * s.N;
+    std::vector<uint32_t> smp(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        smp[i] = sample ? sample[i] : i;
+        if (smp[i] >= S) return fail(ctx, CLOTHO_E_ARG, "pairwise difference: sample row out of range");
+    }
+    *out = clotho_pairwise{};
+    const uint64_t pairs = n > 1 ? (uint64_t)n * (n - 1) / 2 : 0;
+    if (!pairs) return 0;
+    uint32_t* d_smp = nullptr;
+    uint32_t* d_dist = nullptr;
+    PairwiseOut* d_out = nullptr;
+    CK(cudaMalloc(&d_smp, (size_t)n * 4));
+    CK(cudaMalloc(&d_out, sizeof(PairwiseOut)));
+    if (dist) CK(cudaMalloc(&d_dist, pairs * 4));
+    PairwiseOut h{};
+    h.min = 0xffffffffu;
+    CK(cudaMemcpyAsync(d_smp, smp.data(), (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(d_out, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream));
+    launch_pairwise(cfg(ctx), ctx->d_pops[0], idx, d_smp, n, d_dist, d_out);
+    rc = check_launch(ctx, "pairwise difference");
+    CK(cudaMemcpyAsync(&h, d_out, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    if (dist) CK(cudaMemcpyAsync(dist, d_dist, pairs * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(d_smp);
+    cudaFree(d_out);
+    if (d_dist) cudaFree(d_dist);
+    ctx->launches += 1;
+    if (rc) return rc;
+    out->count = h.count;
+    out->total = h.total;
+    out->min = h.count ? h.min : 0;
+    out->max = h.max;
+    out->mean = h.count ? (double)h.total / (double)h.count : 0.0;
+    out->variance = h.count ? (double)h.sumsq / (double)h.count - out->mean * out->mean : 0.0;
+    if (out->variance < 0.0) out->variance = 0.0;
+    return 0;
+}
+
+int clotho_pairwise_difference(clotho_ctx* ctx, const uint32_t* sample, uint32_t n, uint32_t* dist,
+                               clotho_pairwise* out) {
+    return pairwise_of(ctx, 0, sample, n, dist, out);
+}
+int clotho_pop_pairwise_difference(clotho_ctx* ctx, uint32_t index, const uint32_t* sample, uint32_t n,
+                                   uint32_t* dist, clotho_pairwise* out) {
+    return pairwise_of(ctx, index, sample, n, dist, out);
+}
+
 // ---- checkpoint / resume ---------------------------------------------------
 namespace {
 constexpr char kSnapMagic[8] = {'C', 'L', 'O', 'T', 'H', 'O', 'S', '1'};

@@ -233,6 +233,13 @@ void launch_seed_rows(const LaunchCfg&, const PopDev* pops, uint32_t npops, cons
                       uint64_t seed, uint32_t A);
 void launch_stats(const LaunchCfg&, const PopDev* pops, uint32_t p, uint32_t* counts, uint32_t A);
 void launch_row_counts(const LaunchCfg&, const PopDev* pops, uint32_t p, uint32_t* counts, uint32_t S);
+// device accumulators of the pairwise-difference kernel
+struct PairwiseOut {
+    unsigned long long count, total, sumsq;
+    unsigned int min, max;
+};
+void launch_pairwise(const LaunchCfg&, const PopDev* pops, uint32_t p, const uint32_t* sample, uint32_t n,
+                     uint32_t* dist, PairwiseOut* out);
 void launch_ranks(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxNB, uint32_t maxW, bool suf);
 void launch_uscan_buckets(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxNB);
 void launch_uscan_order(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);

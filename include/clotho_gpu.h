@@ -236,6 +236,21 @@ int  clotho_stats_compute(clotho_ctx *ctx, clotho_stats *out, uint32_t *sfs, uin
  * slot, row_counts[2N] = alleles carried by each sequence.  Either may be NULL. */
 int  clotho_margins(clotho_ctx *ctx, uint32_t *col_counts, uint32_t *row_counts);
 
+/* Pairwise differences (association_matrix_pairwise_difference.hpp:75-120,
+ * cuda/analysis/pairwise_difference_kernel.hpp:56-339): for every pair i < j
+ * of the n sampled rows, the number of allele slots where they differ.
+ * sample[n] are row indices (< 2N; NULL = rows 0..n-1), n <= 65,536.  dist,
+ * if not NULL, receives the n(n-1)/2 distances in row-major upper-triangle
+ * order (pair (i,j) at i*n - i(i+1)/2 + j-i-1); it needs n <= 16,384. */
+typedef struct clotho_pairwise {
+    uint64_t count;           /* pairs                                          */
+    uint64_t total;           /* sum of the distances                           */
+    uint32_t min, max;
+    double   mean, variance;  /* variance divided by the count (Boost.Accumulators) */
+} clotho_pairwise;
+int  clotho_pairwise_difference(clotho_ctx *ctx, const uint32_t *sample, uint32_t n, uint32_t *dist,
+                                clotho_pairwise *out);
+
 /* ---- timing ------------------------------------------------------------- */
 /* CUDA events on the context stream around the fused generation kernel.
  * After enabling, clotho_kernel_time returns total ms and launch count of the
@@ -273,6 +288,8 @@ int  clotho_pop_info(clotho_ctx *ctx, uint32_t index, clotho_info *out);
 int  clotho_pop_rows(clotho_ctx *ctx, uint32_t index, uint64_t *dst, size_t dst_words);
 int  clotho_pop_stats(clotho_ctx *ctx, uint32_t index, clotho_stats *out, uint32_t *sfs, uint32_t sfs_len);
 int  clotho_pop_margins(clotho_ctx *ctx, uint32_t index, uint32_t *col_counts, uint32_t *row_counts);
+int  clotho_pop_pairwise_difference(clotho_ctx *ctx, uint32_t index, const uint32_t *sample, uint32_t n,
+                                    uint32_t *dist, clotho_pairwise *out);
 /* One device-drawn generation of every population (N[i] offspring). */
 int  clotho_batch_generation_philox(clotho_ctx *ctx, const uint32_t *N);
 /* G such generations, replayed from one captured CUDA graph. */

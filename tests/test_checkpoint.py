@@ -128,3 +128,31 @@ def test_margins_and_allele_frequency_log_match_the_rows():
     assert log["stats"]["alleles_per_sequence"]["total"] == 2 * N
     assert log["stats"]["sequences_per_allele"]["max"] == int(col.max())
     pop.close()
+
+
+def test_pairwise_difference_matches_numpy():
+    N = 700
+    pop = cg.Population(N, 1 << 13, 1, **dict(KW, mu=0.3))
+    pop.init(N)
+    pop.run_philox(N, 12)
+    rows = pop.rows()
+    bits = np.unpackbits(rows.view(np.uint8).reshape(rows.shape[0], -1), axis=1, bitorder="little").astype(np.int32)
+    rng = np.random.default_rng(9)
+    for sample in (rng.choice(2 * N, 150, replace=False), np.arange(65), np.arange(2 * N)):
+        sub = bits[sample]
+        d = (sub[:, None, :] != sub[None, :, :]).sum(axis=2) if len(sample) <= 200 else None
+        got = pop.pairwise_difference(sample=sample, distances=len(sample) <= 200)
+        n = len(sample)
+        assert got["count"] == n * (n - 1) // 2
+        if d is not None:
+            iu = np.triu_indices(n, 1)
+            ref = d[iu]
+            assert np.array_equal(got["distances"], ref)     # row-major upper triangle
+            assert got["total"] == ref.sum() and got["min"] == ref.min() and got["max"] == ref.max()
+            assert abs(got["mean"] - ref.mean()) < 1e-9 and abs(got["variance"] - ref.var()) < 1e-6
+            assert got["median"] == float(np.median(ref))
+        else:
+            # totals from per-site counts: sum over pairs = sum over sites of c (n - c)
+            c = sub.sum(axis=0).astype(np.int64)
+            assert got["total"] == int((c * (n - c)).sum())
+    pop.close()
