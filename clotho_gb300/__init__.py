@@ -134,6 +134,21 @@ class Population:
     def run_philox(self, N: int, G: int):
         self._ck(self.L.clotho_run_philox(self.h, N, G), "run_philox")
 
+    def run_philox_schedule(self, sizes):
+        """Device-drawn generations with N = sizes[g] offspring individuals in
+        generation g (population growth), replayed from one CUDA graph."""
+        n = np.ascontiguousarray(sizes, np.uint32)
+        if n.size:
+            self._ck(self.L.clotho_run_philox_schedule(self.h, _ptr(n), n.size), "run_philox_schedule")
+
+    def run_growth(self, growth, G: int):
+        """G generations whose sizes follow a growth model (clotho_gb300.growth)."""
+        from . import growth as gr
+        i = self.info()
+        sizes = gr.schedule(growth, i["N"], i["generation"], G)
+        self.run_philox_schedule(sizes)
+        return sizes
+
     # ---- staged policies
     def begin_generation(self, N: int, M: int):
         self._ck(self.L.clotho_begin_generation(self.h, N, M), "begin_generation")
@@ -437,6 +452,14 @@ class Batch:
             return
         n = np.ascontiguousarray(self.N, np.uint32)
         self._ck(self.L.clotho_batch_run_philox(self.h, _ptr(n), G), "batch_run_philox")
+
+    def run_schedule(self, sizes):
+        """sizes[g][i]: offspring individuals of population i in generation g."""
+        n = np.ascontiguousarray(sizes, np.uint32)
+        if n.size:
+            assert n.ndim == 2 and n.shape[1] == len(self.N)
+            self._ck(self.L.clotho_run_philox_schedule(self.h, _ptr(n), n.shape[0]), "run_philox_schedule")
+            self.N = [int(x) for x in n[-1]]
 
     def set_rows_per_item(self, rows: int):
         self._ck(self.L.clotho_set_rows_per_item(self.h, rows), "set_rows_per_item")

@@ -14,6 +14,9 @@
 #include <chrono>
 #include <cmath>
 #include <cstdint>
+#include <functional>
+#include <map>
+#include <memory>
 #include <random>
 #include <stdexcept>
 #include <string>
@@ -277,6 +280,73 @@ public:
     }
 };
 
+// ---- population growth: the reference's runtime plugins and their registry
+// (population_growth_toolkit.hpp:27-53).  A model maps (current N, generation)
+// to the next N; the engine asks once at set-up with (0, 0) and before every
+// generation with (previous N, generation) (engine_batched_task.hpp:143-170).
+struct PopulationGrowth {
+    virtual ~PopulationGrowth() = default;
+    virtual unsigned operator()(unsigned N, unsigned generation) const = 0;
+    virtual std::string name() const = 0;
+};
+
+// N' = (unsigned)(A N + B) (linear_population_growth.cpp:23-25); A = 1, B = 0 by default
+struct LinearGrowth : PopulationGrowth {
+    double A = 1.0, B = 0.0;
+    LinearGrowth(double a = 1.0, double b = 0.0) : A(a), B(b) {}
+    unsigned operator()(unsigned N, unsigned) const override {
+        const double v = A * N + B;
+        return v > 0.0 ? (unsigned)v : 0u;
+    }
+    std::string name() const override { return "linear"; }
+};
+
+// N' = sizes[g % size] (predefined_population_growth.cpp:26-28); default {10000}
+struct PredefinedGrowth : PopulationGrowth {
+    std::vector<unsigned> sizes;
+    explicit PredefinedGrowth(std::vector<unsigned> s = {10000u}) : sizes(s.empty() ? std::vector<unsigned>{10000u} : s) {}
+    unsigned operator()(unsigned, unsigned generation) const override { return sizes[generation % sizes.size()]; }
+    std::string name() const override { return "predefined"; }
+};
+
+// String-keyed registry: name -> factory taking numeric parameters
+// ("A", "B" for linear; "sizes" for predefined).
+class GrowthToolkit {
+public:
+    using Params = std::map<std::string, std::vector<double>>;
+    using Factory = std::function<std::shared_ptr<PopulationGrowth>(const Params&)>;
+
+    static GrowthToolkit& instance() {
+        static GrowthToolkit tk;
+        return tk;
+    }
+    void register_tool(const std::string& name, Factory f) { tools_[name] = std::move(f); }
+    std::shared_ptr<PopulationGrowth> get_tool(const std::string& name, const Params& p = {}) const {
+        auto it = tools_.find(name);
+        if (it == tools_.end()) throw Error("unknown population growth model: " + name);
+        return it->second(p);
+    }
+
+private:
+    GrowthToolkit() {
+        auto first = [](const Params& p, const char* k, double d) {
+            auto it = p.find(k);
+            return (it == p.end() || it->second.empty()) ? d : it->second[0];
+        };
+        register_tool("linear", [first](const Params& p) {
+            return std::make_shared<LinearGrowth>(first(p, "A", 1.0), first(p, "B", 0.0));
+        });
+        register_tool("predefined", [](const Params& p) {
+            std::vector<unsigned> s;
+            auto it = p.find("sizes");
+            if (it != p.end())
+                for (double v : it->second) s.push_back((unsigned)v);
+            return std::make_shared<PredefinedGrowth>(s);
+        });
+    }
+    std::map<std::string, Factory> tools_;
+};
+
 // ---- Engine<...> restated on the device (engine_batched_task.hpp:110-223).
 // staged = true drives the policies one by one; false uses the fused call.
 template <class RNG = std::mt19937_64>
@@ -288,8 +358,23 @@ public:
         check(clotho_init(pop_.get(), N_), pop_.get(), "clotho_init");
     }
 
+    // With a growth model the initial size is growth(0, 0) (Engine::init,
+    // engine_batched_task.hpp:143-161) and every generation's size follows it.
+    EngineGB300(RNG* rng, const Parameters& p, std::shared_ptr<PopulationGrowth> growth)
+        : rng_(rng), pop_(p), sel_(rng), xover_(rng, p.rho, p.bias), mut_(rng, p), N_(p.max_individuals),
+          growth_(std::move(growth)) {
+        if (growth_) N_ = (*growth_)(0u, 0u);
+        if (N_ > p.max_individuals) throw Error("growth: initial size exceeds max_individuals");
+        fit_.assign(N_, 1.0);
+        check(clotho_init(pop_.get(), N_), pop_.get(), "clotho_init");
+    }
+
     void simulate(bool staged = false) {
         const auto t0 = std::chrono::steady_clock::now();
+        if (growth_) {  // size of this generation from the current one (engine_batched_task.hpp:167-170)
+            N_ = (*growth_)(N_, pop_.info().generation);
+            if (N_ > pop_.params().max_individuals) throw Error("growth: size exceeds max_individuals");
+        }
         const unsigned N = N_;
         const uint32_t M = mut_.generateNewMutation(2 * N);
         if (staged) {
@@ -364,6 +449,7 @@ private:
     PhenotypeGPU pheno_;
     FitnessGPU fitness_;
     unsigned N_;
+    std::shared_ptr<PopulationGrowth> growth_;
     std::vector<double> fit_;
     std::vector<double> sim_times_;
     std::vector<uint32_t> free_sizes_, var_sizes_, fixed_sizes_;

@@ -2,10 +2,15 @@
 // over the C++ policy adapters: G generations of a population on the GPU,
 // per-generation status on stdout, the reference's performance JSON at the end.
 //
-//   qtlsim_gb300 [N] [generations] [mu] [rho] [traits] [staged(0|1)] [seed]
+//   qtlsim_gb300 [N] [generations] [mu] [rho] [traits] [staged(0|1)] [seed] [growth]
+//
+// growth: "linear:A:B" or "predefined:n0,n1,..." (the population_growth
+// toolkit's models); N is then the capacity and the sizes follow the model.
 #include <cstdio>
 #include <cstdlib>
 #include <random>
+#include <sstream>
+#include <string>
 
 #include "clotho_gb300.hpp"
 
@@ -22,7 +27,28 @@ int main(int argc, char** argv) {
     p.fitness = CLOTHO_FIT_GAUSSIAN;
     std::mt19937_64 rng(p.seed);
     try {
-        clotho::gb300::EngineGB300<std::mt19937_64> engine(&rng, p);
+        std::shared_ptr<clotho::gb300::PopulationGrowth> growth;
+        if (argc > 8) {  // "name:v0:v1" or "name:v0,v1,..."
+            std::string spec(argv[8]);
+            const size_t c = spec.find(':');
+            const std::string name = spec.substr(0, c);
+            std::vector<double> vals;
+            std::string rest = c == std::string::npos ? "" : spec.substr(c + 1);
+            for (char& ch : rest)
+                if (ch == ':' ) ch = ',';
+            std::stringstream ss(rest);
+            for (std::string tok; std::getline(ss, tok, ',');)
+                if (!tok.empty()) vals.push_back(std::atof(tok.c_str()));
+            clotho::gb300::GrowthToolkit::Params prm;
+            if (name == "linear") {
+                if (vals.size() > 0) prm["A"] = {vals[0]};
+                if (vals.size() > 1) prm["B"] = {vals[1]};
+            } else {
+                prm["sizes"] = vals;
+            }
+            growth = clotho::gb300::GrowthToolkit::instance().get_tool(name, prm);
+        }
+        clotho::gb300::EngineGB300<std::mt19937_64> engine(&rng, p, growth);
         for (unsigned g = 0; g < G; ++g) {
             engine.simulate(staged);
             if ((g + 1) % 10 == 0 || g + 1 == G) {

@@ -87,7 +87,12 @@ struct clotho_ctx {
     PopDev* d_pops[3] = {nullptr, nullptr, nullptr};  // per set: npops contiguous PopDev
     WorkCtl* d_ctl = nullptr;
     uint32_t* d_hdr[3] = {nullptr, nullptr, nullptr}; // per set: [2*npops]
-    uint32_t* h_hdr = nullptr;                          // pinned staging [2*npops]
+    // step headers (N, M per population) are staged in a ring of pinned slots:
+    // a slot is reused only after the copy that read it has completed
+    uint32_t* h_ring = nullptr;                         // [kHdrRing][2 * kMaxPops]
+    cudaEvent_t ring_ev[64]{};
+    bool ring_used[64]{};
+    uint32_t ring_next = 0;
     uint32_t set = 0;                                    // next tape set
     cudaEvent_t copy_done[2]{}, kern_done[2]{};
     std::string err;
@@ -107,6 +112,9 @@ struct clotho_ctx {
 
 namespace {
 
+constexpr uint32_t kHdrRing = 64;
+static_assert(sizeof(((clotho_ctx*)nullptr)->ring_ev) / sizeof(cudaEvent_t) == kHdrRing, "header ring size");
+
 int fail(clotho_ctx* c, int code, const std::string& m) {
     if (c) c->err = m;
     return code;
@@ -120,6 +128,31 @@ int fail(clotho_ctx* c, int code, const std::string& m) {
     } while (0)
 
 LaunchCfg cfg(clotho_ctx* ctx) { return LaunchCfg{ctx->stream, ctx->num_sms}; }
+
+// A pinned slot for one step header; nullptr if pinned memory is unavailable.
+uint32_t* hdr_stage(clotho_ctx* ctx, uint32_t* slot) {
+    if (!ctx->h_ring) {
+        if (cudaMallocHost(&ctx->h_ring, sizeof(uint32_t) * 2 * kMaxPops * kHdrRing) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->h_ring = nullptr;
+            return nullptr;
+        }
+        for (uint32_t k = 0; k < kHdrRing; ++k) cudaEventCreateWithFlags(&ctx->ring_ev[k], cudaEventDisableTiming);
+    }
+    const uint32_t k = ctx->ring_next;
+    ctx->ring_next = (k + 1) % kHdrRing;
+    if (ctx->ring_used[k]) cudaEventSynchronize(ctx->ring_ev[k]);
+    *slot = k;
+    return ctx->h_ring + (size_t)k * 2 * kMaxPops;
+}
+
+// Copy n headers from slot into dst on stream s and mark the slot busy until then.
+int hdr_copy(clotho_ctx* ctx, uint32_t slot, uint32_t* dst, uint32_t n, cudaStream_t s) {
+    CK(cudaMemcpyAsync(dst, ctx->h_ring + (size_t)slot * 2 * kMaxPops, 8ull * n, cudaMemcpyHostToDevice, s));
+    CK(cudaEventRecord(ctx->ring_ev[slot], s));
+    ctx->ring_used[slot] = true;
+    return 0;
+}
 
 int check_launch(clotho_ctx* ctx, const char* what) {
     cudaError_t e = cudaGetLastError();
@@ -216,9 +249,6 @@ int sync_pop_arrays(clotho_ctx* ctx) {
         for (uint32_t i = 0; i < n; ++i) h[i] = ctx->pops[i]->dev[s];
         CK(cudaMemcpyAsync(ctx->d_pops[s], h.data(), sizeof(PopDev) * n, cudaMemcpyHostToDevice, ctx->stream));
     }
-    if (ctx->h_hdr) cudaFreeHost(ctx->h_hdr);
-    ctx->h_hdr = nullptr;
-    if (n) CK(cudaMallocHost(&ctx->h_hdr, sizeof(uint32_t) * 2 * n));
     ctx->maxW = ctx->maxS = ctx->maxN = 0;
     for (PopHost* p : ctx->pops) {
         ctx->maxW = std::max(ctx->maxW, p->dev[0].Wcap);
@@ -425,7 +455,9 @@ int clotho_destroy(clotho_ctx* ctx) {
         if (ctx->d_pops[s]) cudaFree(ctx->d_pops[s]);
         if (ctx->d_hdr[s]) cudaFree(ctx->d_hdr[s]);
     }
-    if (ctx->h_hdr) cudaFreeHost(ctx->h_hdr);
+    if (ctx->h_ring) cudaFreeHost(ctx->h_ring);
+    for (uint32_t k = 0; k < kHdrRing; ++k)
+        if (ctx->ring_ev[k]) cudaEventDestroy(ctx->ring_ev[k]);
     if (ctx->d_ctl) cudaFree(ctx->d_ctl);
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
@@ -591,9 +623,12 @@ int clotho_generation_tape(clotho_ctx* ctx, const clotho_gen_tape* tape) {
     // the tape set s was last read by the kernels of two steps ago
     CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->kern_done[s], 0));
     if ((rc = upload_tape(ctx, ctx->pops[0], s, tape))) return rc;
-    ctx->h_hdr[0] = tape->N;
-    ctx->h_hdr[1] = tape->M;
-    CK(cudaMemcpyAsync(ctx->d_hdr[s], ctx->h_hdr, 8, cudaMemcpyHostToDevice, ctx->copy_stream));
+    uint32_t slot;
+    uint32_t* h = hdr_stage(ctx, &slot);
+    if (!h) return fail(ctx, CLOTHO_E_NOMEM, "pinned host memory refused");
+    h[0] = tape->N;
+    h[1] = tape->M;
+    if ((rc = hdr_copy(ctx, slot, ctx->d_hdr[s], 1, ctx->copy_stream))) return rc;
     CK(cudaEventRecord(ctx->copy_done[s], ctx->copy_stream));
     CK(cudaStreamWaitEvent(ctx->stream, ctx->copy_done[s], 0));
     enqueue_fused_step(ctx, s, false);
@@ -610,12 +645,16 @@ int clotho_generation_philox(clotho_ctx* ctx, uint32_t N) {
     int rc = require_ready(ctx);
     if (rc) return rc;
     if (ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "a staged generation is in progress");
-    for (size_t i = 0; i < ctx->pops.size(); ++i) {
+    for (size_t i = 0; i < ctx->pops.size(); ++i)
         if (N > ctx->pops[i]->dev[2].Ncap) return fail(ctx, CLOTHO_E_CAPACITY, "N exceeds max_individuals");
-        ctx->h_hdr[2 * i] = N;
-        ctx->h_hdr[2 * i + 1] = 0;
+    uint32_t slot;
+    uint32_t* h = hdr_stage(ctx, &slot);
+    if (!h) return fail(ctx, CLOTHO_E_NOMEM, "pinned host memory refused");
+    for (size_t i = 0; i < ctx->pops.size(); ++i) {
+        h[2 * i] = N;
+        h[2 * i + 1] = 0;
     }
-    CK(cudaMemcpyAsync(ctx->d_hdr[2], ctx->h_hdr, 8 * ctx->pops.size(), cudaMemcpyHostToDevice, ctx->stream));
+    if ((rc = hdr_copy(ctx, slot, ctx->d_hdr[2], (uint32_t)ctx->pops.size(), ctx->stream))) return rc;
     enqueue_fused_step(ctx, 2, true);
     if ((rc = check_launch(ctx, "generation_philox"))) return rc;
     for (PopHost* p : ctx->pops) p->hostN = N;
@@ -666,9 +705,12 @@ int clotho_begin_generation(clotho_ctx* ctx, uint32_t N, uint32_t M) {
     if (N > p->dev[0].Ncap) return fail(ctx, CLOTHO_E_CAPACITY, "N exceeds max_individuals");
     if (M > p->dev[0].Mcap) return fail(ctx, CLOTHO_E_CAPACITY, "M exceeds max_mutations");
     CK(cudaStreamSynchronize(ctx->copy_stream));
-    ctx->h_hdr[0] = N;
-    ctx->h_hdr[1] = M;
-    CK(cudaMemcpyAsync(ctx->d_hdr[0], ctx->h_hdr, 8, cudaMemcpyHostToDevice, ctx->stream));
+    uint32_t slot;
+    uint32_t* h = hdr_stage(ctx, &slot);
+    if (!h) return fail(ctx, CLOTHO_E_NOMEM, "pinned host memory refused");
+    h[0] = N;
+    h[1] = M;
+    if ((rc = hdr_copy(ctx, slot, ctx->d_hdr[0], 1, ctx->stream))) return rc;
     launch_begin(cfg(ctx), ctx->d_pops[0], 1, ctx->d_hdr[0], ctx->d_ctl);
     ctx->launches += 1;
     ctx->in_step = true;
@@ -1347,12 +1389,16 @@ int clotho_batch_generation_philox(clotho_ctx* ctx, const uint32_t* N) {
     if (!N) return fail(ctx, CLOTHO_E_ARG, "null N");
     if (ctx->pops.empty()) return 0;
     if (ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "a staged generation is in progress");
-    for (size_t i = 0; i < ctx->pops.size(); ++i) {
+    for (size_t i = 0; i < ctx->pops.size(); ++i)
         if (N[i] > ctx->pops[i]->dev[2].Ncap) return fail(ctx, CLOTHO_E_CAPACITY, "N exceeds max_individuals");
-        ctx->h_hdr[2 * i] = N[i];
-        ctx->h_hdr[2 * i + 1] = 0;
+    uint32_t slot;
+    uint32_t* h = hdr_stage(ctx, &slot);
+    if (!h) return fail(ctx, CLOTHO_E_NOMEM, "pinned host memory refused");
+    for (size_t i = 0; i < ctx->pops.size(); ++i) {
+        h[2 * i] = N[i];
+        h[2 * i + 1] = 0;
     }
-    CK(cudaMemcpyAsync(ctx->d_hdr[2], ctx->h_hdr, 8 * ctx->pops.size(), cudaMemcpyHostToDevice, ctx->stream));
+    if ((rc = hdr_copy(ctx, slot, ctx->d_hdr[2], (uint32_t)ctx->pops.size(), ctx->stream))) return rc;
     enqueue_fused_step(ctx, 2, true);
     if ((rc = check_launch(ctx, "batch_generation_philox"))) return rc;
     for (size_t i = 0; i < ctx->pops.size(); ++i) ctx->pops[i]->hostN = N[i];
@@ -1389,6 +1435,65 @@ int clotho_batch_run_philox(clotho_ctx* ctx, const uint32_t* N, uint32_t G) {
         CK(cudaGraphLaunch(ctx->graph, ctx->stream));
         ctx->launches += ctx->graph_launches;
     }
+    return 0;
+}
+
+int clotho_run_philox_schedule(clotho_ctx* ctx, const uint32_t* N, uint32_t G) {
+    int rc = require_ready(ctx);
+    if (rc) return rc;
+    if (!N) return fail(ctx, CLOTHO_E_ARG, "null schedule");
+    if (ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "a staged generation is in progress");
+    const uint32_t n = (uint32_t)ctx->pops.size();
+    if (G == 0 || n == 0) return 0;
+    std::vector<uint32_t> hdr(2ull * n * G, 0u);
+    for (uint32_t g = 0; g < G; ++g)
+        for (uint32_t i = 0; i < n; ++i) {
+            const uint32_t v = N[(size_t)g * n + i];
+            if (v > ctx->pops[i]->dev[2].Ncap)
+                return fail(ctx, CLOTHO_E_CAPACITY, "schedule N exceeds max_individuals");
+            hdr[2ull * ((size_t)g * n + i)] = v;
+        }
+    if (ctx->profiling) {  // per-launch events are taken from eager launches
+        for (uint32_t g = 0; g < G; ++g)
+            if ((rc = clotho_batch_generation_philox(ctx, N + (size_t)g * n))) return rc;
+        return 0;
+    }
+    uint32_t* d_sched = nullptr;
+    CK(cudaMalloc(&d_sched, hdr.size() * 4));
+    CK(cudaMemcpy(d_sched, hdr.data(), hdr.size() * 4, cudaMemcpyHostToDevice));
+    // the first generation runs eagerly (it may need the parent reduction)
+    CK(cudaMemcpyAsync(ctx->d_hdr[2], d_sched, 8ull * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    enqueue_fused_step(ctx, 2, true);
+    rc = check_launch(ctx, "run_philox_schedule");
+    if (!rc && G > 1) {
+        // every size of a step is read from the device status word, so one graph
+        // serves all generations; only the step header changes between replays
+        const std::vector<uint32_t> key{0xffffffffu, n};
+        if (!ctx->graph || ctx->graph_key != key) {
+            if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+            cudaGraph_t gr;
+            CK(cudaStreamSynchronize(ctx->stream));
+            CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            const uint64_t l0 = ctx->launches;
+            enqueue_fused_step(ctx, 2, true);
+            ctx->graph_launches = ctx->launches - l0;
+            ctx->launches = l0;
+            CK(cudaStreamEndCapture(ctx->stream, &gr));
+            CK(cudaGraphInstantiate(&ctx->graph, gr, 0));
+            cudaGraphDestroy(gr);
+            ctx->graph_key = key;
+        }
+        for (uint32_t g = 1; g < G; ++g) {
+            CK(cudaMemcpyAsync(ctx->d_hdr[2], d_sched + 2ull * n * g, 8ull * n, cudaMemcpyDeviceToDevice,
+                               ctx->stream));
+            CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+            ctx->launches += ctx->graph_launches;
+        }
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(d_sched);
+    if (rc) return rc;
+    for (uint32_t i = 0; i < n; ++i) ctx->pops[i]->hostN = N[(size_t)(G - 1) * n + i];
     return 0;
 }
 

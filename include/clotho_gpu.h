@@ -294,6 +294,13 @@ int  clotho_pop_pairwise_difference(clotho_ctx *ctx, uint32_t index, const uint3
 int  clotho_batch_generation_philox(clotho_ctx *ctx, const uint32_t *N);
 /* G such generations, replayed from one captured CUDA graph. */
 int  clotho_batch_run_philox(clotho_ctx *ctx, const uint32_t *N, uint32_t G);
+/* G device-drawn generations with a size schedule: N[g * npops + i] offspring
+ * individuals of population i in generation g (population growth,
+ * predefined_population_growth.cpp:26-28, linear_population_growth.cpp:23-25).
+ * One captured CUDA graph serves every generation; the sizes are copied to
+ * the device once and each replay reads its own.  Works on single-population
+ * and batched contexts. */
+int  clotho_run_philox_schedule(clotho_ctx *ctx, const uint32_t *N, uint32_t G);
 /* Rows per scheduling item of the generation kernel (autotuner knob). */
 int  clotho_set_rows_per_item(clotho_ctx *ctx, uint32_t rows);
 /* Free and total device memory (admission control). */

@@ -156,3 +156,30 @@ def test_pairwise_difference_matches_numpy():
             c = sub.sum(axis=0).astype(np.int64)
             assert got["total"] == int((c * (n - c)).sum())
     pop.close()
+
+
+def test_growth_schedule_in_one_graph_equals_generation_by_generation():
+    from clotho_gb300 import growth
+    sizes = growth.schedule(growth.LinearGrowth(1.2, 7.0), 300, 1, 8)
+    kw = dict(KW, max_events=1 << 16, max_mutations=1 << 13)
+    a = cg.Population(2000, 1 << 13, 2, **kw)
+    b = cg.Population(2000, 1 << 13, 2, **kw)
+    for p in (a, b):
+        p.init(300)
+    a.run_philox_schedule(sizes)
+    for n in sizes:
+        b.simulate_philox(n)
+    a.check()
+    assert a.info()["N"] == sizes[-1]
+    _same(_state(a), _state(b))
+    # a predefined schedule on a batch of two populations
+    bt = cg.Batch([a.desc, a.desc])
+    bt.N = [200, 200]
+    bt.init()
+    sched = [[100 + 10 * g, 400 - 20 * g] for g in range(6)]
+    bt.run_schedule(sched)
+    assert [bt.info(i)["N"] for i in range(2)] == sched[-1]
+    assert all(bt.info(i)["device_error"] == 0 for i in range(2))
+    for p in (a, b):
+        p.close()
+    bt.close()

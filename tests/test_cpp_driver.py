@@ -37,3 +37,18 @@ def test_driver_runs_generations(staged):
     assert status[-1]["alleles"] > 0
     perf = lines[-1]
     assert len(perf["performance"]["simulate"]) == 30 and len(perf["memory"]["free_count"]) == 30
+
+
+@pytest.mark.gpu
+def test_driver_follows_a_growth_model():
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+    from clotho_gb300 import builder
+    builder.build()
+    # predefined sizes (population_growth toolkit): generation k has sizes[k % 3] individuals
+    r = subprocess.run([builder.DRIVER_PATH, "600", "20", "0.1", "1.0", "1", "0", "5", "predefined:300,500,400"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    status = [json.loads(x) for x in r.stdout.strip().splitlines() if '"generation"' in x]
+    assert [(s["generation"], s["N"]) for s in status] == [(10, [300, 500, 400][10 % 3]), (20, [300, 500, 400][20 % 3])]
+    assert all(s["device_error"] == 0 for s in status)
