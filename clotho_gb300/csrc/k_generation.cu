@@ -392,16 +392,17 @@ __device__ __forceinline__ void effq_push(uint64_t g0, uint64_t g1, uint64_t s0,
         return;
     }
     uint32_t i = tail + incl - c;
-    uint64_t x0 = g0, x1 = g1;
-    while (x0 | x1) {
-        const bool lo = x0 != 0ull;
-        const uint64_t x = lo ? x0 : x1;
-        const uint32_t j = (uint32_t)(__ffsll((long long)x) - 1);
-        const uint32_t sb = (uint32_t)(((lo ? s0 : s1) >> j) & 1ull);
-        Q[i & (kQueueCap - 1u)] = (w * 64u + (lo ? 0u : 64u) + j) | (sb << 31);
-        ++i;
-        const uint64_t xc = x & (x - 1ull);
-        if (lo) x0 = xc; else x1 = xc;
+    // the lane's four 32-bit mask words one after another: 32-bit bit scans
+    const uint32_t gg[4] = {(uint32_t)g0, (uint32_t)(g0 >> 32), (uint32_t)g1, (uint32_t)(g1 >> 32)};
+    const uint32_t ss[4] = {(uint32_t)s0, (uint32_t)(s0 >> 32), (uint32_t)s1, (uint32_t)(s1 >> 32)};
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) {
+        const uint32_t base = w * 64u + 32u * k;
+        for (uint32_t x = gg[k]; x; x &= x - 1u) {
+            const uint32_t j = (uint32_t)(__ffs(x) - 1);
+            Q[i & (kQueueCap - 1u)] = (base + j) | ((ss[k] >> j) << 31);
+            ++i;
+        }
     }
     tail += H;
     __syncwarp();
