@@ -405,6 +405,11 @@ int clotho_create(const clotho_desc* desc, clotho_ctx** out) {
         return CLOTHO_E_CUDA;
     }
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (init_recip_step() || init_recip_gen()) {  // constant tables of this device
+        cudaGetLastError();
+        delete ctx;
+        return CLOTHO_E_CUDA;
+    }
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete ctx;

@@ -167,6 +167,19 @@ __device__ inline double u01(uint32_t hi, uint32_t lo) {
     return (double)v * 0x1.0p-53;
 }
 
+// 1/k for the Poisson inversion (k = 1..kRecip-1); multiplying by it avoids
+// FP64 divisions, which are slow on this part.  Every translation unit that
+// draws Poisson numbers has its own copy (no relocatable device code), filled
+// on the current device by that unit's init_recip_* function.
+constexpr uint32_t kRecip = 256;
+static __constant__ double c_recip[kRecip];
+static inline int fill_recip_table() {
+    double h[kRecip];
+    h[0] = 0.0;
+    for (uint32_t k = 1; k < kRecip; ++k) h[k] = 1.0 / (double)k;
+    return cudaMemcpyToSymbol(c_recip, h, sizeof(h)) == cudaSuccess ? 0 : -1;
+}
+
 // Poisson draw by sequential inversion of the CDF; e = exp(-lambda) from the
 // host.  Used only for small means (per-gamete events, per-row mutations).
 __device__ inline uint32_t poisson_inv(double u, double lambda, double e) {
@@ -174,7 +187,7 @@ __device__ inline uint32_t poisson_inv(double u, double lambda, double e) {
     uint32_t k = 0;
     while (u > F && k < 4096u) {
         ++k;
-        p *= lambda / (double)k;
+        p *= lambda * (k < kRecip ? c_recip[k] : 1.0 / (double)k);
         F += p;
     }
     return k;
@@ -245,6 +258,8 @@ void launch_uscan_buckets(const LaunchCfg&, const PopDev* pops, uint32_t npops, 
 void launch_uscan_order(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
 
 void launch_plan(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
+int init_recip_step();  // k_step.cu's copy of the reciprocal table
+int init_recip_gen();   // k_generation.cu's copy
 
 // crossover-plan row flags
 constexpr uint32_t kPlanInv = 1u, kPlanLong = 2u, kPlanFlagShift = 30u;

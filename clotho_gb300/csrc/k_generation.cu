@@ -1090,19 +1090,21 @@ __global__ void k_ord_scatter(const PopDev* __restrict__ pops, uint32_t npops) {
 // plan entries from a block-aggregated counter; tape rows use the tape's own
 // event offsets.
 __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pops, uint32_t npops) {
-    __shared__ uint32_t s_w[8];
-    __shared__ uint32_t s_base;
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t lane = threadIdx.x & 31u;
     for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         if (!P.plan_row) continue;
         const DevStatus st = *P.st;
-        const uint32_t S = 2u * st.N, A = st.A;
+        const uint32_t S = 2u * st.N, A = st.A, Se = (S + 1u) >> 1;
         const bool philox = P.mode == kModePhilox;
         const bool q1 = (P.flags & 1u) != 0;
-        for (uint32_t g0 = blockIdx.x * blockDim.x; g0 < S; g0 += gridDim.x * blockDim.x) {
-            const uint32_t g = g0 + threadIdx.x;
-            const bool live = g < S;
+        for (uint32_t v0 = blockIdx.x * blockDim.x; v0 < S; v0 += gridDim.x * blockDim.x) {
+            const uint32_t v = v0 + threadIdx.x;
+            const bool live = v < S;
+            // even gametes on the first half of the threads, odd ones on the second:
+            // under the reference's crossover rule odd gametes are copy rows, so a
+            // warp holds one kind of row
+            const uint32_t g = v < Se ? 2u * v : 2u * (v - Se) + 1u;
             uint32_t pind = 0, E = 0, base = 0, flags = 0;
             bool swap = false;
             if (live) {
@@ -1113,9 +1115,8 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
                 }
                 if (philox) {
                     const U4 x = philox4x32(g, 0u, st.gen, kStreamGamete, P.seed);
-                    E = poisson_inv(u01(x.x, x.y), P.rho, P.exp_neg_rho);
+                    E = (q1 && (g & 1u)) ? 0u : poisson_inv(u01(x.x, x.y), P.rho, P.exp_neg_rho);
                     swap = u01(x.z, x.w) < P.bias;
-                    if (q1 && (g & 1u)) E = 0;
                     if (E > kMaxEvDevice) {
                         atomicOr(&P.st->err, kErrEvents);
                         E = kMaxEvDevice;
@@ -1126,27 +1127,17 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
                     E = (q1 && (g & 1u)) ? 0u : P.ev_off[g + 1u] - base;
                 }
             }
-            if (philox) {  // block-aggregated allocation of the plan entries
+            if (philox) {  // warp-aggregated allocation of the plan entries
                 uint32_t incl = E;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
                     if (lane >= (uint32_t)o) incl += y;
                 }
-                if (lane == 31u) s_w[warp] = incl;
-                __syncthreads();
-                if (threadIdx.x == 0) {
-                    uint32_t t = 0;
-                    for (uint32_t i = 0; i < blockDim.x / 32u; ++i) {
-                        const uint32_t c = s_w[i];
-                        s_w[i] = t;
-                        t += c;
-                    }
-                    s_base = t ? atomicAdd(&P.st->ev_used, t) : 0u;
-                }
-                __syncthreads();
-                base = s_base + s_w[warp] + incl - E;
-                __syncthreads();
+                const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+                uint32_t b0 = 0;
+                if (lane == 0 && tot) b0 = atomicAdd(&P.st->ev_used, tot);
+                base = __shfl_sync(0xffffffffu, b0, 0) + incl - E;
                 if (E && base + E > P.EVcap) {
                     atomicOr(&P.st->err, kErrEvents);
                     E = 0;
@@ -1198,6 +1189,8 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
         }
     }
 }
+
+int init_recip_gen() { return fill_recip_table(); }
 
 void launch_plan(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
     const dim3 g = pop_grid(npops, blocks_for(maxS, 256), L.num_sms, 8);

@@ -10,6 +10,8 @@
 
 namespace clotho {
 
+int init_recip_step() { return fill_recip_table(); }
+
 namespace {
 constexpr uint32_t kScanChunk = 4096;  // elements per scan chunk (1024 threads x 4)
 
