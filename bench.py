@@ -17,8 +17,8 @@ generation (free space, selection, crossover, mutation, phenotype, fitness).
   cpu_baseline  the CPU oracle (restatement of the reference's path) on the
            host cores, on a bounded sample of the same workload.
 
---impl reference times that CPU restatement alone (the reference itself needs
-Boost, which is absent).
+--impl reference times that CPU restatement alone: the reference's own engine
+needs Boost (every hot-path header includes it), which this image lacks.
 """
 from __future__ import annotations
 

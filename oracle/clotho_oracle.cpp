@@ -611,7 +611,8 @@ struct Engine {
         return 0;
     }
 
-    // Draws one generation in the reference's order:
+    // Draws one generation in the reference's draw order
+    // (engine_batched_task.hpp:175-202):
     // M (mutation_allocator.hpp:41-47); selection pairs
     // (general_fitness_selection_generator.hpp:45-69,104-113); per gamete E then
     // E positions (batch_crossover_mtwe.hpp:117-133); all bias bits (:135-145);
