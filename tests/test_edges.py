@@ -1,0 +1,107 @@
+"""Edge cases through the C-ABI: very long breakpoint lists, tapes with
+out-of-range indices, allele-capacity overflow, all-zero fitness and a
+one-individual population.  Invalid tape entries are bounds-checked on the
+device: they are skipped and reported as sticky error bits
+(CLOTHO_DEVERR_*), and the population stays usable."""
+import numpy as np
+import pytest
+
+import oracle
+from tests.conftest import gpu_available
+
+pytestmark = pytest.mark.gpu
+
+if not gpu_available():  # collected on CPU machines, skipped there
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+import clotho_gb300 as cg  # noqa: E402
+from tests.test_gpu_parity import compare_state, make_pair  # noqa: E402
+
+
+
+def _tape(N, pairs, mut_seq, mut_pos=None, rng=None):
+    S = 2 * N
+    M = len(mut_seq)
+    rng = rng or np.random.default_rng(0)
+    return oracle.Tape(N, M, np.asarray(pairs, np.uint32), np.zeros(S, np.uint8), np.zeros(S + 1, np.uint32),
+                       np.zeros(0), np.asarray(mut_seq, np.uint32),
+                       rng.random(M) if mut_pos is None else mut_pos, np.zeros(M, np.float32))
+
+
+def test_rows_with_more_than_128_breakpoints_match_the_oracle():
+    # rho = 150: most gametes carry more breakpoints than the device draws per
+    # gamete (128), so tape rows take the direct event-compare path
+    N = 40
+    orc, gpu = make_pair(N, 8192, mu=1.0, rho=150.0, p_neutral=1.0, q1=False)
+    orc.init(N)
+    gpu.init(N)
+    for g in range(6):
+        tape = orc.step_record(N)
+        assert (np.diff(tape.ev_off) > 128).any()
+        gpu.simulate(tape)
+        compare_state(orc, gpu, g)
+
+
+def test_out_of_range_tape_indices_are_flagged_and_skipped():
+    N = 30
+    gpu = cg.Population(N, 4096, 1, mu=0.0, rho=0.0, p_neutral=1.0, max_events=64, max_mutations=64)
+    gpu.init(N)
+    rng = np.random.default_rng(1)
+    gpu.simulate(_tape(N, rng.integers(0, N, 2 * N), [0, 5, 7], rng=rng))   # three alleles
+    assert gpu.info()["device_error"] == 0 and gpu.info()["A"] == 3
+    pairs = rng.integers(0, N, 2 * N)
+    pairs[3] = N + 5                                   # no such parent
+    gpu.simulate(_tape(N, pairs, [1, 2 * N + 9], rng=rng))   # second mutation: no such row
+    err = gpu.info()["device_error"]
+    assert err & 8 and err & 16                        # CLOTHO_DEVERR_PARENT, CLOTHO_DEVERR_SEQ
+    with pytest.raises(cg.ClothoError):
+        gpu.check()
+    rows = gpu.rows()
+    assert rows.shape[0] == 2 * N
+    gpu.simulate(_tape(N, rng.integers(0, N, 2 * N), [], rng=rng))          # still usable afterwards
+    assert gpu.info()["generation"] == 4
+    gpu.close()
+
+
+def test_allele_capacity_overflow_is_flagged_and_capped():
+    N = 20
+    gpu = cg.Population(N, 4096, 1, mu=0.0, rho=0.0, p_neutral=1.0, max_events=64, max_mutations=8192)
+    gpu.init(N)
+    rng = np.random.default_rng(2)
+    gpu.simulate(_tape(N, rng.integers(0, N, 2 * N), rng.integers(0, 2 * N, 5000), rng=rng))
+    i = gpu.info()
+    assert i["device_error"] & 1                       # CLOTHO_DEVERR_ALLELES
+    assert i["A"] == 4096 and i["W"] == 64
+    rows = gpu.rows()
+    bits = np.unpackbits(rows.view(np.uint8).reshape(rows.shape[0], -1), axis=1, bitorder="little")
+    assert bits.sum() <= 4096                          # mutations past the capacity were dropped
+    gpu.simulate(_tape(N, rng.integers(0, N, 2 * N), [], rng=rng))
+    assert gpu.info()["A"] <= 4096
+    gpu.close()
+
+
+def test_all_zero_fitness_falls_back_to_uniform_selection():
+    # every individual carries large effects; quadratic fitness with a tiny scale is zero for all
+    N, A = 100, 40
+    gpu = cg.Population(N, 4096, 1, fitness="quadratic", fit_param=1e-3, mu=0.01, rho=0.5, p_neutral=0.0,
+                        max_events=4096, max_mutations=1024)
+    gpu.seed_population(N, np.linspace(0.01, 0.99, A), np.full(A, 10.0, np.float32),
+                        np.full(A, 2 ** 31, np.uint32), 7)   # each allele in about half the rows
+    gpu.simulate_philox(N)
+    gpu.simulate_philox(N)
+    i = gpu.info()
+    assert i["device_error"] & 64                      # CLOTHO_DEVERR_FITNESS
+    assert i["N"] == N and i["generation"] == 3
+    gpu.close()
+
+
+def test_one_individual_population():
+    gpu = cg.Population(1, 4096, 2, fitness="gaussian_vs", fit_param=2.0, mu=0.5, rho=2.0, p_neutral=0.2,
+                        max_events=256, max_mutations=256)
+    gpu.init(1)
+    gpu.run_philox(1, 25)
+    gpu.check()
+    i = gpu.info()
+    assert i["N"] == 1 and gpu.rows().shape[0] == 2
+    assert np.isfinite(gpu.phenotypes()).all()
+    gpu.close()
