@@ -280,3 +280,27 @@ def test_crossover_fixture_on_gpu(q1):
     assert np.array_equal(child, orc.rows())
     for a, want in ((77, True), (33, False), (88, True), (99, False), (22, True), (15, True)):
         assert bit(child, kid, a) == want, a
+
+
+def test_c2_shaped_phenotype_error_stays_within_fp32_bound(capsys):
+    # QTL + selection shape: T=1, N(0,1) effects on every new allele, exp(-z^2/2),
+    # fitness-proportional parents; 100 generations of carried FP32 sums against
+    # the oracle's FP64 re-sums.  Prints the max / mean absolute error.
+    N, G = 1000, 100
+    orc, gpu = make_pair(N, 1 << 14, T=1, fitness="gaussian_vs", fit_param=1.0, mu=0.1, rho=1.0, p_neutral=0.0)
+    orc.init(N)
+    gpu.init(N)
+    worst, means, scale = 0.0, [], 0.0
+    for g in range(G):
+        gpu.simulate(orc.step_record(N))
+        zo, zg = orc.phenotypes(), gpu.phenotypes()
+        err = np.abs(zo - zg)
+        bound = pheno_bound(gpu.rows(), gpu.alleles()[2], g + 1)
+        assert np.all(err <= bound), f"gen {g}: {err.max()} > bound"
+        worst = max(worst, float(err.max()))
+        means.append(float(err.mean()))
+        scale = max(scale, float(np.abs(zo).max()))
+    assert np.array_equal(orc.rows(), gpu.rows())
+    with capsys.disabled():
+        print(f"\nC2-shaped N={N} G={G}: phenotype |FP32 carried - FP64| max {worst:.3e}, mean {np.mean(means):.3e}"
+              f" (|z| up to {scale:.2f}, alleles {gpu.info()['A']})")
