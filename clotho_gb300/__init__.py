@@ -25,7 +25,7 @@ FLAG_Q1 = 1
 DEVICE_ERRORS = {1: "allele capacity exceeded", 2: "fixed table capacity exceeded",
                  4: "more than 128 device-drawn events in a gamete", 8: "tape parent index out of range",
                  16: "tape mutation row out of range", 32: "mutation capacity exceeded",
-                 64: "all fitness values zero"}
+                 64: "all fitness values zero", 128: "asynchronous copy wait expired"}
 
 
 class ClothoError(RuntimeError):

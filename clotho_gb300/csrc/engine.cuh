@@ -25,7 +25,7 @@ constexpr uint32_t kSufMaxSlots = 65536;   // allele capacity up to which the su
 
 // sticky device error bits (CLOTHO_DEVERR_* in clotho_gpu.h)
 constexpr uint32_t kErrAlleles = 1u, kErrFixed = 2u, kErrEvents = 4u, kErrParent = 8u,
-                   kErrSeq = 16u, kErrMut = 32u, kErrFitness = 64u;
+                   kErrSeq = 16u, kErrMut = 32u, kErrFitness = 64u, kErrStall = 128u;
 
 enum Mode : uint32_t { kModeTape = 0, kModePhilox = 1 };
 

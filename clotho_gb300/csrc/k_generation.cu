@@ -307,7 +307,55 @@ __device__ __forceinline__ void row_phenotype(const PopDev& P, const DevStatus& 
 
 struct WarpSmem {
     uint32_t q[kQueueCap];            // effect queue: slot | sign << 31
+    unsigned long long mbar;          // completion barrier of the warp's bulk copies
+    unsigned long long pad;
 };
+
+// Copy rows: 1 = one bulk copy of the parent strand into the warp's bitmap,
+// 0 = register streaming six chunks deep (kept for comparison)
+#ifndef CLOTHO_COPY_BULK
+#define CLOTHO_COPY_BULK 1
+#endif
+
+// ---- bulk copies (cp.async.bulk) into the warp's bitmap, completed on an mbarrier
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect(unsigned long long* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+constexpr uint32_t kWaitLimit = 1u << 22;   // try_wait rounds before a copy is given up
+
+// Waits for the phase of the warp's barrier; false (and a sticky error bit) if it did not complete.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t& phase, uint32_t* err) {
+    uint32_t it = 0;
+    while (!mbar_try_wait(bar, phase)) {
+        if (++it >= kWaitLimit) {
+            if ((threadIdx.x & 31u) == 0) atomicOr(err, kErrStall);
+            return false;
+        }
+    }
+    phase ^= 1u;
+    return true;
+}
 
 __device__ __forceinline__ void add4(float (&d)[kMaxTraits], const float4& e) {
     d[0] += e.x;
@@ -449,6 +497,7 @@ __device__ __forceinline__ void row_mutations(const PopDev& P, uint32_t M, const
     }
 }
 
+#if !CLOTHO_COPY_BULK
 // Copy rows (no breakpoint): the top strand with the fixed columns cleared and
 // the new alleles added; the bottom-strand registers of the crossover loop
 // hold more of the top strand here, six chunks ahead.
@@ -479,6 +528,50 @@ __device__ __forceinline__ void row_body_copy(const PopDev& P, uint32_t M, const
             if (do_fs) fold_fs(sF, sV, w, x0, x1);
         }
     }
+}
+
+#endif
+
+// Copy rows through a bulk copy: the whole parent strand (<= 8 KB) lands in
+// the warp's (otherwise idle) bitmap in one asynchronous transfer, then the
+// lanes mask, mutate, store and fold it, and clear the bitmap behind them.
+__device__ __forceinline__ void row_body_copy_bulk(const PopDev& P, uint32_t M, const RowArgs& R,
+                                                   const uint64_t* sfix, uint64_t* buf, unsigned long long* bar,
+                                                   uint32_t& phase, bool do_mut, bool do_fs, uint64_t* sF,
+                                                   uint64_t* sV) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t bytes = R.Wp * 8u;
+    bool ok = true;
+    if (bytes) {
+        // earlier generic-proxy reads and writes of buf come before the asynchronous write
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive_expect(bar, bytes);
+        __syncwarp();
+        const uint32_t off = lane * 2048u;
+        if (off < bytes)
+            bulk_load(reinterpret_cast<char*>(buf) + off, reinterpret_cast<const char*>(R.top) + off,
+                      min(2048u, bytes - off), bar);
+        ok = mbar_wait(bar, phase, &P.st->err);
+    }
+    for (uint32_t w0 = 0; w0 < R.Wc; w0 += 64u) {
+        const uint32_t w = w0 + 2u * lane;
+        uint64_t mx0 = 0, mx1 = 0;
+        if (do_mut && R.mc) row_mutations(P, M, R, w, mx0, mx1);
+        if (w < R.Wc) {
+            ulonglong2 t = make_ulonglong2(0, 0), fm = make_ulonglong2(0, 0);
+            if (w < R.Wp) {
+                ulonglong2* bw = reinterpret_cast<ulonglong2*>(buf + w);
+                if (ok) t = *bw;
+                *bw = make_ulonglong2(0, 0);  // crossover rows expect the bitmap at zero
+                fm = *reinterpret_cast<const ulonglong2*>(sfix + w);
+            }
+            const uint64_t x0 = (t.x & ~fm.x) ^ mx0, x1 = (t.y & ~fm.y) ^ mx1;
+            *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(x0, x1);
+            if (do_fs) fold_fs(sF, sV, w, x0, x1);
+        }
+    }
+    __syncwarp();
 }
 
 // Crossover rows.  MODE 0: switch mask from the warp's mask bitmap; MODE 1:
@@ -515,7 +608,7 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
                 if (live) {
                     ulonglong2* mw = reinterpret_cast<ulonglong2*>(mask + w);
                     const ulonglong2 m = *mw;
-                    *mw = make_ulonglong2(0, 0);
+                    *mw = make_ulonglong2(0, 0);  // the bitmap starts every row at zero
                     m0 = m.x;
                     m1 = m.y;
                 }
@@ -571,8 +664,8 @@ __device__ __forceinline__ uint32_t table_row(uint32_t r, uint32_t A, uint32_t& 
 // at processing position v (k_row_plan): row, top strand, breakpoints, table
 // rows and correction ranks.
 __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st, uint32_t v, const uint64_t* sfix,
-                                            uint64_t* mask, WarpSmem& ws, bool do_mut, bool do_ph, bool gather,
-                                            bool do_fs, uint64_t* sF, uint64_t* sV) {
+                                            uint64_t* mask, WarpSmem& ws, uint32_t& phase, bool do_mut, bool do_ph,
+                                            bool gather, bool do_fs, uint64_t* sF, uint64_t* sV) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint4 pr = __ldg(P.plan_row + v);
     const uint32_t g = pr.x, topr = pr.y, base = pr.z;
@@ -589,7 +682,7 @@ __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st
     R.E = E;
     R.philox = P.mode == kModePhilox;
     R.evg = P.ev_pos + base;
-    prefetch_l2(R.top, R.Wp * 8u);
+    if (E > 0 || !CLOTHO_COPY_BULK) prefetch_l2(R.top, R.Wp * 8u);
     if (E > 0) prefetch_l2(R.bot, R.Wp * 8u);
     R.zbase = 0.0;
     if (do_ph && lane < kMaxTraits)
@@ -599,7 +692,11 @@ __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st
     if (flags & kPlanLong) {
         add4(d, row_body_events(P, st.M, R, sfix, ws.q, do_mut, gather, do_fs, sF, sV));
     } else if (E == 0) {
+#if CLOTHO_COPY_BULK
+        row_body_copy_bulk(P, st.M, R, sfix, mask, &ws.mbar, phase, do_mut, do_fs, sF, sV);
+#else
         row_body_copy(P, st.M, R, sfix, do_mut, do_fs, sF, sV);
+#endif
     } else {
         // corrections: toggle the slots whose rank lies between threshold and table row
         uint32_t* m32 = reinterpret_cast<uint32_t*>(mask);
@@ -929,8 +1026,12 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     // SUF: per-warp mask bitmaps [kWarps][maxW] u64, then one WarpSmem per warp
     uint64_t* mask = s_dyn + (3u + (SUF ? warp : 0u)) * maxW;
     WarpSmem& ws = reinterpret_cast<WarpSmem*>(s_dyn + (3u + kWarps) * maxW)[SUF ? warp : 0u];
-    if (SUF)
+    uint32_t bphase = 0;  // parity of the warp's bulk-copy barrier
+    if (SUF) {
         for (uint32_t w = lane; w < maxW; w += 32u) mask[w] = 0ull;
+        if (lane == 0) mbar_init(&ws.mbar);
+        __syncwarp();
+    }
     const bool do_mut = (fuse & kFuseMut) != 0, do_ph = (fuse & kFusePheno) != 0, do_fs = (fuse & kFuseFs) != 0;
     int cur_pop = -1;
     uint32_t cur_W = 0;
@@ -994,7 +1095,7 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             // path takes its rows in plan order
             const uint32_t g = v < Se ? 2u * v : 2u * (v - Se) + 1u;
             if (SUF)
-                gen_row_suf(P, st, v, sfix, mask, ws, do_mut, do_ph, gather, do_fs, sF, sV);
+                gen_row_suf(P, st, v, sfix, mask, ws, bphase, do_mut, do_ph, gather, do_fs, sF, sV);
             else
                 gen_row_iv(P, st, g, sfix, s_iv[warp], s_thr[warp], s_q[warp], s_sm[warp], do_mut, do_ph, gather,
                            do_fs, sF, sV);

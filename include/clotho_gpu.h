@@ -119,6 +119,7 @@ typedef struct clotho_info {
 #define CLOTHO_DEVERR_SEQ     16u   /* tape mutation row out of range         */
 #define CLOTHO_DEVERR_MUT     32u   /* mutation capacity exceeded             */
 #define CLOTHO_DEVERR_FITNESS 64u   /* all fitness zero: uniform selection used */
+#define CLOTHO_DEVERR_STALL  128u   /* an asynchronous copy did not complete in time (row left unfinished) */
 
 /* ---- lifetime ---------------------------------------------------------- */
 int  clotho_create(const clotho_desc *desc, clotho_ctx **out);
