@@ -99,6 +99,11 @@ class Population:
     def sync(self):
         self._ck(self.L.clotho_sync(self.h), "sync")
 
+    def set_stream(self, stream=None):
+        """Run on the caller's CUDA stream (an integer handle, e.g.
+        torch.cuda.Stream().cuda_stream); None returns to the context's own."""
+        self._ck(self.L.clotho_set_stream(self.h, C.c_void_p(int(stream)) if stream else None), "set_stream")
+
     # ---- set-up
     def init(self, N0: int):
         self._ck(self.L.clotho_init(self.h, N0), "init")
@@ -463,6 +468,10 @@ class Batch:
 
     def set_rows_per_item(self, rows: int):
         self._ck(self.L.clotho_set_rows_per_item(self.h, rows), "set_rows_per_item")
+
+    def set_stream(self, stream=None):
+        """Run on the caller's CUDA stream (integer handle); None returns to the context's own."""
+        self._ck(self.L.clotho_set_stream(self.h, C.c_void_p(int(stream)) if stream else None), "set_stream")
 
     def sync(self):
         self._ck(self.L.clotho_sync(self.h), "sync")

@@ -83,6 +83,7 @@ SIGNATURES = {
     "clotho_get_pairs": (C.c_int, [vp, vp]),
     "clotho_stats_compute": (C.c_int, [vp, C.POINTER(Stats), vp, u32]),
     "clotho_margins": (C.c_int, [vp, vp, vp]),
+    "clotho_set_stream": (C.c_int, [vp, vp]),
     "clotho_run_philox_schedule": (C.c_int, [vp, vp, u32]),
     "clotho_pairwise_difference": (C.c_int, [vp, vp, u32, vp, C.POINTER(Pairwise)]),
     "clotho_pop_pairwise_difference": (C.c_int, [vp, u32, vp, u32, vp, C.POINTER(Pairwise)]),

@@ -83,6 +83,7 @@ struct clotho_ctx {
     int device = 0;
     int num_sms = 152;
     cudaStream_t stream = nullptr, copy_stream = nullptr;
+    cudaStream_t own_stream = nullptr;  // the context's own compute stream (stream may be the caller's)
     std::vector<PopHost*> pops;
     PopDev* d_pops[3] = {nullptr, nullptr, nullptr};  // per set: npops contiguous PopDev
     WorkCtl* d_ctl = nullptr;
@@ -410,11 +411,12 @@ int clotho_create(const clotho_desc* desc, clotho_ctx** out) {
         delete ctx;
         return CLOTHO_E_CUDA;
     }
-    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+    if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete ctx;
         return CLOTHO_E_CUDA;
     }
+    ctx->stream = ctx->own_stream;
     for (int i = 0; i < 2; ++i) {
         cudaEventCreateWithFlags(&ctx->copy_done[i], cudaEventDisableTiming);
         cudaEventCreateWithFlags(&ctx->kern_done[i], cudaEventDisableTiming);
@@ -472,7 +474,7 @@ int clotho_destroy(clotho_ctx* ctx) {
     }
     if (ctx->t0) cudaEventDestroy(ctx->t0);
     if (ctx->t1) cudaEventDestroy(ctx->t1);
-    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     delete ctx;
     return 0;
@@ -491,6 +493,16 @@ int clotho_sync(clotho_ctx* ctx) {
     if (!ctx) return CLOTHO_E_ARG;
     CK(cudaStreamSynchronize(ctx->copy_stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int clotho_set_stream(clotho_ctx* ctx, void* stream) {
+    if (!ctx) return CLOTHO_E_ARG;
+    if (ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "set the stream between generations");
+    // work already queued on the old stream finishes before the new one is used
+    CK(cudaStreamSynchronize(ctx->copy_stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
     return 0;
 }
 

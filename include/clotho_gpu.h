@@ -130,6 +130,13 @@ size_t clotho_footprint(const clotho_ctx *ctx);
 /* Bytes a context with this descriptor would allocate (admission control). */
 size_t clotho_footprint_for(const clotho_desc *desc);
 int  clotho_sync(clotho_ctx *ctx);
+/* The stream the context's kernels run on: the caller's cudaStream_t (cast
+ * to void *), or NULL for the context's own stream.  Work already queued on
+ * the previous stream is finished first.  The caller keeps ownership of its
+ * stream and must not destroy it while the context uses it.  The graph calls
+ * (clotho_run_philox*) capture on this stream, so it must not be the legacy
+ * default stream for them. */
+int  clotho_set_stream(clotho_ctx *ctx, void *stream);
 
 /* ---- population set-up ------------------------------------------------- */
 /* Engine::init(0) (engine_batched_task.hpp:143-161): N0 individuals, no alleles. */

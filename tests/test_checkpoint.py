@@ -183,3 +183,23 @@ def test_growth_schedule_in_one_graph_equals_generation_by_generation():
     for p in (a, b):
         p.close()
     bt.close()
+
+
+def test_runs_on_the_callers_stream():
+    torch = pytest.importorskip("torch")
+    N = 1200
+    a = cg.Population(N, 1 << 13, 2, **KW)
+    b = cg.Population(N, 1 << 13, 2, **KW)
+    for p in (a, b):
+        p.init(N)
+    a.run_philox(N, 8)
+    s = torch.cuda.Stream()
+    b.set_stream(s.cuda_stream)
+    b.run_philox(N, 4)                  # captured and replayed on the caller's stream
+    for _ in range(4):
+        b.simulate_philox(N)
+    s.synchronize()
+    b.set_stream(None)                  # back to the context's own stream
+    _same(_state(a), _state(b))
+    for p in (a, b):
+        p.close()
