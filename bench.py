@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-gens", type=int, default=4)
     p.add_argument("--kernel-only", action="store_true", help="seed + eager generations only (ncu runs)")
+    p.add_argument("--phase-clocks", action="store_true",
+                   help="print the generation kernel's per-phase cycle breakdown (profiling build) and exit")
     p.add_argument("--no-batched", action="store_true", help="skip the batched and serving measurements")
     return p.parse_args()
 
@@ -289,6 +291,44 @@ def reference_arm(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def phase_breakdown(pop, N, warmup, steps):
+    """Where the fused generation kernel spends its time: the profiling build
+    clocks each row's phases (SM cycles summed over warps) over `steps`
+    generations after `warmup` plain ones.  Shares are of the warps' resident
+    cycles; the clock reads and their registers slow that build by a few percent."""
+    for _ in range(warmup):
+        pop.simulate_philox(N)
+    pop.sync()
+    pop.profile(True, phases=True)
+    for _ in range(steps):
+        pop.simulate_philox(N)
+    pop.sync()
+    ph = pop.phase_clocks()
+    ms, launches, rows, _ = pop.kernel_time()
+    pop.profile(False)
+    warp = max(ph["warp_cycles"], 1)
+    nc, nx = max(ph["copy_rows"], 1), max(ph["xo_rows"], 1)
+    per_row = {
+        "copy": {k: ph["copy_" + k] / nc for k in ("setup", "body", "phenotype")},
+        "crossover": {k: ph["xo_" + k] / nx for k in ("setup", "mask", "body", "gather", "phenotype")},
+    }
+    share = {
+        "copy_rows": (ph["copy_setup"] + ph["copy_body"] + ph["copy_phenotype"]) / warp,
+        "xo_setup": ph["xo_setup"] / warp,
+        "xo_mask": ph["xo_mask"] / warp,
+        "xo_stream": (ph["xo_body"] - ph["xo_gather"]) / warp,
+        "xo_gather": ph["xo_gather"] / warp,
+        "xo_phenotype": ph["xo_phenotype"] / warp,
+        "long_rows": ph["long_cycles"] / warp,
+    }
+    share["outside_rows"] = 1.0 - sum(share.values())
+    return {"phase_clocks": True, "N": N, "generations": steps, "rows": {"copy": ph["copy_rows"],
+            "crossover": ph["xo_rows"], "long": ph["long_rows"], "profiled": rows},
+            "kernel_ms_per_gen": ms / max(launches, 1), "warps": ph["warps"],
+            "cycles_per_row": per_row, "share_of_warp_cycles": {k: round(v, 4) for k, v in share.items()},
+            "raw": ph}
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -308,6 +348,10 @@ def main():
     pop = make_population(cg, w, N)
     pos, eff, thr = seeded_start(w, N=N)
     pop.seed_population(N, pos, eff, thr, 99)
+
+    if args.phase_clocks:
+        print(json.dumps(phase_breakdown(pop, N, args.warmup, args.steps)))
+        return
 
     if args.kernel_only:
         for _ in range(args.warmup + args.steps):

@@ -343,8 +343,10 @@ class Population:
         return d
 
     # ---- timing
-    def profile(self, enable: bool):
-        self._ck(self.L.clotho_profile(self.h, 1 if enable else 0), "profile")
+    def profile(self, enable: bool, phases: bool = False):
+        """Kernel events and row counts; phases=True also runs the generation
+        kernel's phase-clock build (slower) for phase_clocks()."""
+        self._ck(self.L.clotho_profile(self.h, (2 if phases else 1) if enable else 0), "profile")
 
     def kernel_time(self):
         ms = C.c_double()
@@ -353,6 +355,16 @@ class Population:
         w = C.c_uint64()
         self._ck(self.L.clotho_kernel_time(self.h, C.byref(ms), C.byref(n), C.byref(r), C.byref(w)), "kernel_time")
         return ms.value, n.value, r.value, w.value
+
+    PHASES = ("copy_rows", "copy_setup", "copy_body", "copy_phenotype", "xo_rows", "xo_setup", "xo_mask",
+              "xo_body", "xo_gather", "xo_phenotype", "long_rows", "long_cycles", "warp_cycles", "warps")
+
+    def phase_clocks(self) -> dict:
+        """Per-phase SM cycles of the fused generation kernel since profile(True, phases=True)
+        (summed over warps; the profiling build clocks each suffix-table row)."""
+        out = (C.c_uint64 * len(self.PHASES))()
+        self._ck(self.L.clotho_phase_clocks(self.h, out, len(self.PHASES)), "phase_clocks")
+        return dict(zip(self.PHASES, (int(x) for x in out)))
 
     def timer_begin(self):
         self._ck(self.L.clotho_timer_begin(self.h), "timer_begin")

@@ -92,6 +92,7 @@ SIGNATURES = {
     "clotho_snapshot": (C.c_int, [vp, vp, C.c_size_t]),
     "clotho_restore": (C.c_int, [vp, vp, C.c_size_t]),
     "clotho_profile": (C.c_int, [vp, C.c_int]),
+    "clotho_phase_clocks": (C.c_int, [vp, C.POINTER(C.c_uint64), C.c_uint32]),
     "clotho_kernel_time": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(u32), C.POINTER(u64), C.POINTER(u64)]),
     "clotho_timer_begin": (C.c_int, [vp]),
     "clotho_timer_end": (C.c_int, [vp, C.POINTER(C.c_double)]),

@@ -98,6 +98,7 @@ struct clotho_ctx {
     cudaEvent_t copy_done[2]{}, kern_done[2]{};
     std::string err;
     bool profiling = false;
+    bool phase_clocks = false;      // profiling with the phase-clock build of k_generation
     std::vector<cudaEvent_t> prof_ev;  // pairs around each k_generation launch
     size_t prof_used = 0;
     double prof_ms = 0.0;
@@ -307,7 +308,8 @@ void launch_gen(clotho_ctx* ctx, const PopDev* pops, uint32_t npops, uint32_t fu
         ctx->launches += 6;  // order count, 3-kernel scan, order scatter, plan
     }
     prof_begin(ctx);
-    launch_generation(cfg(ctx), pops, npops, ctx->d_ctl, ctx->maxW, ctx->maxA, fuse, ctx->profiling ? 1 : 0);
+    launch_generation(cfg(ctx), pops, npops, ctx->d_ctl, ctx->maxW, ctx->maxA, fuse,
+                      ctx->profiling ? (ctx->phase_clocks ? 2 : 1) : 0);
     prof_end(ctx);
     ctx->launches += 1;
 }
@@ -1276,10 +1278,21 @@ int clotho_profile(clotho_ctx* ctx, int enable) {
     int rc = prof_collect(ctx);
     if (rc) return rc;
     ctx->profiling = enable != 0;
+    ctx->phase_clocks = enable == 2;
     ctx->prof_ms = 0.0;
     ctx->prof_launches = 0;
     if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
-    CK(cudaMemsetAsync(&ctx->d_ctl->rows_done, 0, 16, ctx->stream));
+    CK(cudaMemsetAsync(&ctx->d_ctl->rows_done, 0, 16 + sizeof(ctx->d_ctl->phase), ctx->stream));
+    return 0;
+}
+
+int clotho_phase_clocks(clotho_ctx* ctx, uint64_t* out, uint32_t n) {
+    static_assert(kPhCount == CLOTHO_PHASE_COUNT, "phase list of the header and the kernel differ");
+    if (!ctx || (!out && n) || n > CLOTHO_PHASE_COUNT) return CLOTHO_E_ARG;
+    uint64_t ph[kPhCount];
+    CK(cudaMemcpyAsync(ph, ctx->d_ctl->phase, sizeof(ph), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (uint32_t i = 0; i < n; ++i) out[i] = ph[i];
     return 0;
 }
 

@@ -119,6 +119,15 @@ struct WorkCtl {
     uint32_t item_base[257];        // item prefix per population (<= 256 pops)
     uint64_t rows_done;             // profiling: rows processed
     uint64_t words_done;            // profiling: words written
+    uint64_t phase[16];             // profiling: k_generation phase cycles (kPh*)
+};
+
+// Phase counters of the profiling build of k_generation (suffix-table rows):
+// SM cycles summed over warps, per kind of row, and the rows of each kind.
+enum : uint32_t {
+    kPhCopyRows = 0, kPhCopySetup, kPhCopyBody, kPhCopyPheno,
+    kPhXoRows, kPhXoSetup, kPhXoMask, kPhXoBody, kPhXoGather, kPhXoPheno,
+    kPhLongRows, kPhLongCyc, kPhWarpCyc, kPhWarps, kPhCount
 };
 
 constexpr uint32_t kMaxPops = 256;

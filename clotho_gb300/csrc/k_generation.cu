@@ -380,6 +380,10 @@ __device__ CLOTHO_COLD float4 effects_direct(uint64_t m0, uint64_t m1, uint64_t 
 constexpr uint32_t kRoundLane = CLOTHO_ROUND_LANE;   // queue entries gathered per lane per round
 constexpr uint32_t kRound = 32u * kRoundLane;
 constexpr uint32_t kTableInflight = CLOTHO_TABLE_INFLIGHT;
+#ifndef CLOTHO_WARP_CHUNK
+#define CLOTHO_WARP_CHUNK 1
+#endif
+constexpr uint32_t kWarpChunk = CLOTHO_WARP_CHUNK;   // rows a warp claims at a time (one population)
 
 // A gather round in flight: its effects are loaded when the round is issued
 // and folded into the sums one round later, so the loads have a chunk of work
@@ -576,10 +580,12 @@ __device__ __forceinline__ void row_body_copy_bulk(const PopDev& P, uint32_t M, 
 
 // Crossover rows.  MODE 0: switch mask from the warp's mask bitmap; MODE 1:
 // direct event compares (tape rows with more than kMaxEvDevice events).
-template <int MODE>
+// PROF: clock the effect gather into *gcyc (profiling build).
+template <int MODE, bool PROF = false>
 __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const RowArgs& R, const uint64_t* sfix,
                                              uint64_t* mask, uint32_t* Q, bool inv, bool do_mut, bool gather,
-                                             bool do_fs, uint64_t* sF, uint64_t* sV, float (&d)[kMaxTraits]) {
+                                             bool do_fs, uint64_t* sF, uint64_t* sV, float (&d)[kMaxTraits],
+                                             unsigned long long* gcyc = nullptr) {
     const uint32_t lane = threadIdx.x & 31u;
     constexpr bool xo = true;
     const float4* eff4 = reinterpret_cast<const float4*>(P.eff);
@@ -619,9 +625,12 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
             const uint64_t sw0 = m0 & h0, sw1 = m1 & h1;
             x0 = t0 ^ sw0;
             x1 = t1 ^ sw1;
-            if (gather)
+            if (gather) {
+                const long long c0 = PROF ? clock64() : 0;
                 effq_push(inv ? (h0 ^ sw0) : sw0, inv ? (h1 ^ sw1) : sw1, inv ? t0 : b0, inv ? t1 : b1, w, Q, qh, qt,
                           pend, eff4, d);
+                if (PROF) *gcyc += (unsigned long long)(clock64() - c0);
+            }
         }
         if (live) {
             x0 ^= mx0;
@@ -633,12 +642,14 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
         t_b = t_c; b_b = b_c;
     }
     if (gather) {
+        const long long c0 = PROF ? clock64() : 0;
         effq_complete(pend, d);
         if (qt != qh) {
             effq_issue(Q, qh, qt - qh, eff4, pend);
             effq_complete(pend, d);
             __syncwarp();
         }
+        if (PROF) *gcyc += (unsigned long long)(clock64() - c0);
     }
 }
 
@@ -660,13 +671,21 @@ __device__ __forceinline__ uint32_t table_row(uint32_t r, uint32_t A, uint32_t& 
     return b;
 }
 
+// Phase cycles of the profiling build, kept by every lane, flushed by lane 0.
+struct PhaseClk {
+    unsigned long long c[kPhCount];
+};
+
 // One offspring row, the whole warp (suffix-table classifier), from the plan
 // at processing position v (k_row_plan): row, top strand, breakpoints, table
-// rows and correction ranks.
+// rows and correction ranks.  PROF: clock the row's phases into pc.
+template <bool PROF>
 __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st, uint32_t v, const uint64_t* sfix,
                                             uint64_t* mask, WarpSmem& ws, uint32_t& phase, bool do_mut, bool do_ph,
-                                            bool gather, bool do_fs, uint64_t* sF, uint64_t* sV) {
+                                            bool gather, bool do_fs, uint64_t* sF, uint64_t* sV, PhaseClk& pc) {
     const uint32_t lane = threadIdx.x & 31u;
+    const long long c0 = PROF ? clock64() : 0;
+    long long c1 = 0, c2 = 0, c3 = 0;
     const uint4 pr = __ldg(P.plan_row + v);
     const uint32_t g = pr.x, topr = pr.y, base = pr.z;
     const uint32_t E = pr.w & kPlanMaxEvents, flags = pr.w >> kPlanFlagShift;
@@ -689,6 +708,7 @@ __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st
         R.zbase = P.zg[st.cur ^ 1u][(size_t)(inv ? topr ^ 1u : topr) * 4u + lane] - P.st->fixsum[lane];
     float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
     row_mutation_setup(P, st, g, do_mut, gather, R, d);
+    if (PROF) c1 = clock64();
     if (flags & kPlanLong) {
         add4(d, row_body_events(P, st.M, R, sfix, ws.q, do_mut, gather, do_fs, sF, sV));
     } else if (E == 0) {
@@ -743,9 +763,30 @@ __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st
             }
         }
         __syncwarp();
-        row_body_suf<0>(P, st.M, R, sfix, mask, ws.q, inv, do_mut, gather, do_fs, sF, sV, d);
+        if (PROF) c2 = clock64();
+        row_body_suf<0, PROF>(P, st.M, R, sfix, mask, ws.q, inv, do_mut, gather, do_fs, sF, sV, d,
+                              &pc.c[kPhXoGather]);
     }
+    if (PROF) c3 = clock64();
     if (do_ph) row_phenotype(P, st, g, R, d);
+    if (PROF) {
+        const unsigned long long c4 = (unsigned long long)clock64();
+        if (flags & kPlanLong) {
+            pc.c[kPhLongRows] += 1;
+            pc.c[kPhLongCyc] += c4 - c0;
+        } else if (E == 0) {
+            pc.c[kPhCopyRows] += 1;
+            pc.c[kPhCopySetup] += c1 - c0;
+            pc.c[kPhCopyBody] += c3 - c1;
+            pc.c[kPhCopyPheno] += c4 - c3;
+        } else {
+            pc.c[kPhXoRows] += 1;
+            pc.c[kPhXoSetup] += c1 - c0;
+            pc.c[kPhXoMask] += c2 - c1;
+            pc.c[kPhXoBody] += c3 - c2;
+            pc.c[kPhXoPheno] += c4 - c3;
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1008,10 +1049,15 @@ __device__ __forceinline__ void gen_row_iv(const PopDev& P, const DevStatus& st,
 // then (SUF) the warps' mask bitmaps and one WarpSmem per warp.  With gacc set (rows
 // too wide for that layout) the AND/OR fold goes to the population's global
 // accumulators and the fixed mask is read from global memory.
-template <bool SUF>
+// PROF (suffix-table build only): per-phase cycle counters into ctl->phase.
+template <bool SUF, bool PROF>
 __global__ void __launch_bounds__(kGenThreads, 1)
 k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restrict__ ctl, uint32_t fuse,
              int profile, uint32_t maxW, uint32_t gacc) {
+    const long long c_start = PROF ? clock64() : 0;
+    PhaseClk pc;
+    if (PROF)
+        for (uint32_t i = 0; i < kPhCount; ++i) pc.c[i] = 0;
     extern __shared__ __align__(16) uint64_t s_dyn[];
     constexpr uint32_t kIvWarps = SUF ? 1 : kWarps;  // interval-classifier state, unused by the suffix table
     __shared__ uint2 s_iv[kIvWarps][kMaxIvSmem];
@@ -1037,7 +1083,48 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     uint32_t cur_W = 0;
     uint64_t rows_done = 0, words_done = 0;
 
-    for (;;) {
+    if (npops == 1) {
+        // One population: each warp takes kWarpChunk rows at a time from the
+        // step's counter, with no block barrier between them, so no warp waits
+        // for the slowest warp of its block until the kernel's end.
+        const PopDev& P = pops[0];
+        const DevStatus st = *P.st;
+        cur_pop = 0;
+        cur_W = st.W;
+        if (gacc) {
+            sF = P.accF;
+            sV = P.accV;
+            sfix = P.fixmask;
+        } else {
+            if (do_fs)
+                for (uint32_t w = threadIdx.x; w < cur_W; w += blockDim.x) { sF[w] = ~0ull; sV[w] = 0ull; }
+            for (uint32_t w = threadIdx.x; w < st.pW; w += blockDim.x) sfix[w] = P.fixmask[w];
+        }
+        __syncthreads();
+        const bool gather = do_ph && st.nz_eff != 0;
+        const uint32_t S = 2u * st.N;
+        const uint32_t Se = (S + 1u) >> 1;
+        // the next claim is taken before the current rows run, so its
+        // round trip to the counter is hidden behind them
+        uint32_t claim = 0;
+        if (lane == 0) claim = atomicAdd(&ctl->gen_counter, kWarpChunk);
+        for (;;) {
+            const uint32_t k = __shfl_sync(0xffffffffu, claim, 0);
+            if (k >= S) break;
+            if (lane == 0) claim = atomicAdd(&ctl->gen_counter, kWarpChunk);
+            const uint32_t k1 = min(S, k + kWarpChunk);
+            for (uint32_t v = k; v < k1; ++v) {
+                const uint32_t g = v < Se ? 2u * v : 2u * (v - Se) + 1u;
+                if (SUF)
+                    gen_row_suf<PROF>(P, st, v, sfix, mask, ws, bphase, do_mut, do_ph, gather, do_fs, sF, sV, pc);
+                else
+                    gen_row_iv(P, st, g, sfix, s_iv[warp], s_thr[warp], s_q[warp], s_sm[warp], do_mut, do_ph,
+                               gather, do_fs, sF, sV);
+                if (profile && lane == 0) { rows_done += 1; words_done += st.W; }
+            }
+        }
+    }
+    for (; npops > 1;) {
         if (threadIdx.x == 0) {
             s_item = atomicAdd(&ctl->gen_counter, 1u);
             s_next = 0;
@@ -1095,7 +1182,7 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             // path takes its rows in plan order
             const uint32_t g = v < Se ? 2u * v : 2u * (v - Se) + 1u;
             if (SUF)
-                gen_row_suf(P, st, v, sfix, mask, ws, bphase, do_mut, do_ph, gather, do_fs, sF, sV);
+                gen_row_suf<PROF>(P, st, v, sfix, mask, ws, bphase, do_mut, do_ph, gather, do_fs, sF, sV, pc);
             else
                 gen_row_iv(P, st, g, sfix, s_iv[warp], s_thr[warp], s_q[warp], s_sm[warp], do_mut, do_ph, gather,
                            do_fs, sF, sV);
@@ -1110,6 +1197,12 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             atomicAnd((unsigned long long*)&Q.accF[w], (unsigned long long)sF[w]);
             atomicOr((unsigned long long*)&Q.accV[w], (unsigned long long)sV[w]);
         }
+    }
+    if (PROF && lane == 0) {
+        pc.c[kPhWarpCyc] = (unsigned long long)(clock64() - c_start);
+        pc.c[kPhWarps] = 1;
+        for (uint32_t i = 0; i < kPhCount; ++i)
+            if (pc.c[i]) atomicAdd((unsigned long long*)&ctl->phase[i], pc.c[i]);
     }
     if (profile && lane == 0 && rows_done) {
         atomicAdd((unsigned long long*)&ctl->rows_done, (unsigned long long)rows_done);
@@ -1126,18 +1219,23 @@ void launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, W
     const uint32_t gacc = (!suf && 3ull * maxW * sizeof(uint64_t) + kWarps * 3584u > 220u * 1024u) ? 1u : 0u;
     const size_t smem =
         gacc ? 0 : (3ull + (suf ? kWarps : 0u)) * maxW * sizeof(uint64_t) + (suf ? kWarps * sizeof(WarpSmem) : 0);
-    static size_t configured[2] = {0, 0};
-    const int si = suf ? 1 : 0;
+    // profile 2: the suffix-table kernel's build with phase clocks
+    static size_t configured[3] = {0, 0, 0};
+    const int si = suf ? (profile == 2 ? 2 : 1) : 0;
     // static shared memory is above 48 KB on its own, so the opt-in attribute is always needed
     if (smem > configured[si] || configured[si] == 0) {
-        if (suf) cudaFuncSetAttribute(k_generation<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        else cudaFuncSetAttribute(k_generation<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const void* fn = si == 2 ? (const void*)k_generation<true, true>
+                                 : si == 1 ? (const void*)k_generation<true, false> : (const void*)k_generation<false, false>;
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured[si] = smem > 0 ? smem : 1;
     }
-    if (suf)
-        k_generation<true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, 0u);
+    if (si == 2)
+        k_generation<true, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, 0u);
+    else if (si == 1)
+        k_generation<true, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, 0u);
     else
-        k_generation<false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, gacc);
+        k_generation<false, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW,
+                                                                               gacc);
 }
 
 // ---------------------------------------------------------------------------

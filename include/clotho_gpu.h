@@ -262,10 +262,24 @@ int  clotho_pairwise_difference(clotho_ctx *ctx, const uint32_t *sample, uint32_
 /* ---- timing ------------------------------------------------------------- */
 /* CUDA events on the context stream around the fused generation kernel.
  * After enabling, clotho_kernel_time returns total ms and launch count of the
- * dominant kernel since the last reset. */
+ * dominant kernel since the last reset.  enable = 2 also switches the kernel
+ * to its build with phase clocks (clotho_phase_clocks), which runs slower. */
 int  clotho_profile(clotho_ctx *ctx, int enable);
 int  clotho_kernel_time(clotho_ctx *ctx, double *total_ms, uint32_t *launches,
                         uint64_t *rows_processed, uint64_t *words_processed);
+/* Phase cycles of the fused generation kernel while profiling is enabled
+ * with enable = 2 (that build clocks every suffix-table row): SM cycles
+ * summed over warps, reset by clotho_profile.  out[0..n) receives, in order:
+ *   0 copy rows, 1 copy set-up, 2 copy body, 3 copy phenotype,
+ *   4 crossover rows, 5 crossover set-up, 6 switch-mask build,
+ *   7 crossover body (streaming + gather), 8 effect gather (within 7),
+ *   9 crossover phenotype, 10 long-event rows, 11 their cycles,
+ *   12 warp residency cycles, 13 warps.
+ * No reference counterpart: the reference times whole stages
+ * (engine_batched_task.hpp:233-242); here the stages are fused in one kernel.
+ * n <= CLOTHO_PHASE_COUNT. */
+#define CLOTHO_PHASE_COUNT 14u
+int  clotho_phase_clocks(clotho_ctx *ctx, uint64_t *out, uint32_t n);
 int  clotho_timer_begin(clotho_ctx *ctx);
 int  clotho_timer_end(clotho_ctx *ctx, double *ms);
 /* Count of kernels this context launched since creation. */
@@ -309,7 +323,9 @@ int  clotho_batch_run_philox(clotho_ctx *ctx, const uint32_t *N, uint32_t G);
  * the device once and each replay reads its own.  Works on single-population
  * and batched contexts. */
 int  clotho_run_philox_schedule(clotho_ctx *ctx, const uint32_t *N, uint32_t G);
-/* Rows per scheduling item of the generation kernel (autotuner knob). */
+/* Rows per scheduling item of the generation kernel (autotuner knob of
+ * batched contexts; a single-population context has its warps claim one row
+ * at a time and ignores it). */
 int  clotho_set_rows_per_item(clotho_ctx *ctx, uint32_t rows);
 /* Free and total device memory (admission control). */
 int  clotho_mem_info(size_t *free_bytes, size_t *total_bytes);

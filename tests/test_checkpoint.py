@@ -203,3 +203,31 @@ def test_runs_on_the_callers_stream():
     _same(_state(a), _state(b))
     for p in (a, b):
         p.close()
+
+
+def test_phase_clocks_cover_every_row_and_change_no_result():
+    N = 1500
+    a = cg.Population(N, 1 << 13, 2, **KW)
+    b = cg.Population(N, 1 << 13, 2, **KW)
+    for p in (a, b):
+        p.init(N)
+    a.run_philox(N, 5)
+    b.run_philox(N, 2)
+    b.profile(True, phases=True)         # the phase-clock build of the generation kernel
+    for _ in range(3):
+        b.simulate_philox(N)
+    ph = b.phase_clocks()
+    b.profile(False)
+    _same(_state(a), _state(b))
+    assert ph["copy_rows"] + ph["xo_rows"] + ph["long_rows"] == 3 * 2 * N
+    assert ph["copy_rows"] >= 3 * N      # the second gamete of each pair is a copy row
+    assert ph["xo_rows"] > 0 and ph["xo_mask"] > 0 and 0 < ph["xo_gather"] <= ph["xo_body"]
+    assert ph["warps"] > 0 and ph["warps"] % 3 == 0
+    rows_cycles = sum(ph[k] for k in ("copy_setup", "copy_body", "copy_phenotype", "xo_setup", "xo_mask", "xo_body",
+                                      "xo_phenotype", "long_cycles"))
+    assert 0 < rows_cycles <= ph["warp_cycles"]
+    b.profile(True)                      # re-enabling resets the counters; the plain build leaves them at 0
+    b.simulate_philox(N)
+    assert sum(b.phase_clocks().values()) == 0
+    for p in (a, b):
+        p.close()
