@@ -20,7 +20,7 @@ namespace {
 struct PopHost {
     clotho_desc desc{};
     PopDev dev[3]{};          // tape set 0, tape set 1, device-drawn (Philox)
-    std::vector<void*> allocs;
+    void* arena = nullptr;          // every device table of the population, one pool block
     size_t bytes = 0;
     bool acc_valid = false;   // accF/accV hold AND/OR of the current child rows
     bool ready = false;       // init/seed done
@@ -84,6 +84,9 @@ struct clotho_ctx {
     int num_sms = 152;
     cudaStream_t stream = nullptr, copy_stream = nullptr;
     cudaStream_t own_stream = nullptr;  // the context's own compute stream (stream may be the caller's)
+    // populations' device tables come from the context's own stream-ordered pool, which keeps freed
+    // blocks for the next population (a serving loop adds and removes populations every few steps)
+    cudaMemPool_t pool = nullptr;
     std::vector<PopHost*> pops;
     PopDev* d_pops[3] = {nullptr, nullptr, nullptr};  // per set: npops contiguous PopDev
     WorkCtl* d_ctl = nullptr;
@@ -162,9 +165,10 @@ int check_launch(clotho_ctx* ctx, const char* what) {
     return 0;
 }
 
-void free_pop(PopHost* p) {
-    for (void* a : p->allocs) cudaFree(a);
-    p->allocs.clear();
+// The caller has synchronized the context's streams: nothing reads the tables any more.
+void free_pop(clotho_ctx* ctx, PopHost* p) {
+    if (p->arena) cudaFreeAsync(p->arena, ctx->own_stream);
+    p->arena = nullptr;
     delete p;
 }
 
@@ -176,22 +180,23 @@ int alloc_pop(clotho_ctx* ctx, const clotho_desc& d, PopHost** out) {
     p->desc = d;
     std::vector<size_t> sz = sizes_of(g);
     std::vector<void*> ptr(sz.size(), nullptr);
-    for (size_t i = 0; i < sz.size(); ++i) {
-        void* q = nullptr;
-        if (sz[i] == 0) continue;  // optional table not used at this capacity
-        cudaError_t e = cudaMalloc(&q, align256(sz[i]));
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            free_pop(p);
-            return fail(ctx, CLOTHO_E_NOMEM, "device allocation refused (" + std::to_string(align256(sz[i])) + " bytes)");
-        }
-        p->allocs.push_back(q);
-        p->bytes += align256(sz[i]);
-        ptr[i] = q;
+    // one block for all tables, each at a 256-byte aligned offset (optional tables of size 0 stay null)
+    size_t total = 0;
+    for (size_t x : sz) total += align256(x);
+    cudaError_t e = cudaMallocFromPoolAsync(&p->arena, total, ctx->pool, ctx->own_stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->own_stream);  // ready before other streams use it
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        p->arena = nullptr;
+        delete p;
+        return fail(ctx, CLOTHO_E_NOMEM, "device allocation refused (" + std::to_string(total) + " bytes)");
     }
-    // zero the tables (cheap) and the status
-    for (size_t i = 2; i < sz.size(); ++i)
-        if (sz[i]) cudaMemsetAsync(ptr[i], 0, sz[i], ctx->stream);
+    p->bytes = total;
+    for (size_t i = 0, off = 0; i < sz.size(); off += align256(sz[i]), ++i)
+        if (sz[i]) ptr[i] = static_cast<char*>(p->arena) + off;
+    // zero the tables and the status: everything after the two row sets, in one call
+    const size_t rows_bytes = align256(sz[0]) + align256(sz[1]);
+    if (total > rows_bytes) cudaMemsetAsync(static_cast<char*>(p->arena) + rows_bytes, 0, total - rows_bytes, ctx->stream);
     PopDev b{};
     size_t k = 0;
     b.rows[0] = (uint64_t*)ptr[k++]; b.rows[1] = (uint64_t*)ptr[k++];
@@ -235,23 +240,22 @@ int alloc_pop(clotho_ctx* ctx, const clotho_desc& d, PopHost** out) {
     return 0;
 }
 
-// Rebuild the device PopDev arrays after the population set changed.
-int sync_pop_arrays(clotho_ctx* ctx) {
+// Rebuild the device PopDev arrays after the population set changed: entries
+// [from, n) are copied (an add changes the last one, a remove shifts the rest).
+int sync_pop_arrays(clotho_ctx* ctx, uint32_t from = 0) {
     const uint32_t n = (uint32_t)ctx->pops.size();
     if (n > kMaxPops) return fail(ctx, CLOTHO_E_CAPACITY, "more than 256 populations");
     for (int s = 0; s < 3; ++s) {
-        if (ctx->d_pops[s]) cudaFree(ctx->d_pops[s]);
-        if (ctx->d_hdr[s]) cudaFree(ctx->d_hdr[s]);
-        ctx->d_pops[s] = nullptr;
-        ctx->d_hdr[s] = nullptr;
-        if (!n) continue;
-        CK(cudaMalloc(&ctx->d_pops[s], sizeof(PopDev) * n));
-        CK(cudaMalloc(&ctx->d_hdr[s], sizeof(uint32_t) * 2 * n));
-        std::vector<PopDev> h(n);
-        for (uint32_t i = 0; i < n; ++i) h[i] = ctx->pops[i]->dev[s];
-        CK(cudaMemcpyAsync(ctx->d_pops[s], h.data(), sizeof(PopDev) * n, cudaMemcpyHostToDevice, ctx->stream));
+        // sized for kMaxPops once, so adding or removing a population allocates nothing here
+        if (!ctx->d_pops[s]) CK(cudaMalloc(&ctx->d_pops[s], sizeof(PopDev) * kMaxPops));
+        if (!ctx->d_hdr[s]) CK(cudaMalloc(&ctx->d_hdr[s], sizeof(uint32_t) * 2 * kMaxPops));
+        if (from >= n) continue;
+        std::vector<PopDev> h(n - from);
+        for (uint32_t i = from; i < n; ++i) h[i - from] = ctx->pops[i]->dev[s];
+        CK(cudaMemcpyAsync(ctx->d_pops[s] + from, h.data(), sizeof(PopDev) * (n - from), cudaMemcpyHostToDevice,
+                           ctx->stream));
     }
-    ctx->maxW = ctx->maxS = ctx->maxN = 0;
+    ctx->maxW = ctx->maxS = ctx->maxN = ctx->maxNB = ctx->maxA = 0;
     for (PopHost* p : ctx->pops) {
         ctx->maxW = std::max(ctx->maxW, p->dev[0].Wcap);
         ctx->maxS = std::max(ctx->maxS, p->dev[0].Scap);
@@ -419,6 +423,20 @@ int clotho_create(const clotho_desc* desc, clotho_ctx** out) {
         return CLOTHO_E_CUDA;
     }
     ctx->stream = ctx->own_stream;
+    {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = ctx->device;
+        if (cudaMemPoolCreate(&ctx->pool, &props) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->pool = nullptr;
+            clotho_destroy(ctx);
+            return CLOTHO_E_CUDA;
+        }
+        uint64_t keep = ~0ull;  // freed blocks stay in the pool until the context ends
+        cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     for (int i = 0; i < 2; ++i) {
         cudaEventCreateWithFlags(&ctx->copy_done[i], cudaEventDisableTiming);
         cudaEventCreateWithFlags(&ctx->kern_done[i], cudaEventDisableTiming);
@@ -458,8 +476,10 @@ int clotho_destroy(clotho_ctx* ctx) {
     if (!ctx) return CLOTHO_E_ARG;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
-    for (PopHost* p : ctx->pops) free_pop(p);
+    for (PopHost* p : ctx->pops) free_pop(ctx, p);
     ctx->pops.clear();
+    if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+    if (ctx->pool) cudaMemPoolDestroy(ctx->pool);  // its blocks are back: free_pop returned them
     for (int s = 0; s < 3; ++s) {
         if (ctx->d_pops[s]) cudaFree(ctx->d_pops[s]);
         if (ctx->d_hdr[s]) cudaFree(ctx->d_hdr[s]);
@@ -1354,7 +1374,7 @@ int clotho_batch_create(const clotho_desc* descs, uint32_t n, clotho_ctx** out) 
         d.traits = 1;
         int rc = clotho_create(&d, &ctx);
         if (rc) return rc;
-        free_pop(ctx->pops[0]);
+        free_pop(ctx, ctx->pops[0]);
         ctx->pops.clear();
         rc = sync_pop_arrays(ctx);
         if (rc) { clotho_destroy(ctx); return rc; }
@@ -1386,7 +1406,7 @@ int clotho_pop_add(clotho_ctx* ctx, const clotho_desc* desc, uint32_t* index) {
     int rc = alloc_pop(ctx, *desc, &p);
     if (rc) return rc;
     ctx->pops.push_back(p);
-    rc = sync_pop_arrays(ctx);
+    rc = sync_pop_arrays(ctx, (uint32_t)ctx->pops.size() - 1);
     if (rc) return rc;
     if (index) *index = (uint32_t)ctx->pops.size() - 1;
     return 0;
@@ -1396,9 +1416,9 @@ int clotho_pop_remove(clotho_ctx* ctx, uint32_t index) {
     if (!ctx || index >= ctx->pops.size()) return fail(ctx, CLOTHO_E_ARG, "no such population");
     CK(cudaStreamSynchronize(ctx->copy_stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    free_pop(ctx->pops[index]);
+    free_pop(ctx, ctx->pops[index]);
     ctx->pops.erase(ctx->pops.begin() + index);
-    return sync_pop_arrays(ctx);
+    return sync_pop_arrays(ctx, index);
 }
 
 int clotho_pop_init(clotho_ctx* ctx, uint32_t index, uint32_t N0) { return init_pop(ctx, index, N0); }
