@@ -380,6 +380,9 @@ __device__ CLOTHO_COLD float4 effects_direct(uint64_t m0, uint64_t m1, uint64_t 
 constexpr uint32_t kRoundLane = CLOTHO_ROUND_LANE;   // queue entries gathered per lane per round
 constexpr uint32_t kRound = 32u * kRoundLane;
 constexpr uint32_t kTableInflight = CLOTHO_TABLE_INFLIGHT;
+#ifndef CLOTHO_PUSH_MSB
+#define CLOTHO_PUSH_MSB 1
+#endif
 #ifndef CLOTHO_WARP_CHUNK
 #define CLOTHO_WARP_CHUNK 1
 #endif
@@ -450,11 +453,21 @@ __device__ __forceinline__ void effq_push(uint64_t g0, uint64_t g1, uint64_t s0,
 #pragma unroll
     for (uint32_t k = 0; k < 4; ++k) {
         const uint32_t base = w * 64u + 32u * k;
+#if CLOTHO_PUSH_MSB
+        // highest bit first: one leading-zero count per bit, the sign bit shifted into place by it
+        for (uint32_t x = gg[k]; x;) {
+            const uint32_t c = (uint32_t)__clz(x);
+            Q[i & (kQueueCap - 1u)] = (base + 31u - c) | ((ss[k] << c) & 0x80000000u);
+            x ^= 0x80000000u >> c;
+            ++i;
+        }
+#else
         for (uint32_t x = gg[k]; x; x &= x - 1u) {
             const uint32_t j = (uint32_t)(__ffs(x) - 1);
             Q[i & (kQueueCap - 1u)] = (base + j) | ((ss[k] >> j) << 31);
             ++i;
         }
+#endif
     }
     tail += H;
     __syncwarp();
