@@ -271,10 +271,23 @@ __device__ __forceinline__ double row_event(const PopDev& P, const DevStatus& st
 }
 
 // z(child genome g) = z(top strand) - sum(fixed effects) + the row's delta (FP64 warp sum).
+#ifndef CLOTHO_PHENO_F32
+#define CLOTHO_PHENO_F32 1
+#endif
 __device__ __forceinline__ void row_phenotype(const PopDev& P, const DevStatus& st, uint32_t g, const RowArgs& R,
                                               const float (&d)[kMaxTraits]) {
     const uint32_t lane = threadIdx.x & 31u;
     double z[kMaxTraits];
+#if CLOTHO_PHENO_F32
+    // the lanes' FP32 sums are reduced in FP32 (GB300's FP64 pipe is narrow); the row's phenotype stays FP64
+#pragma unroll
+    for (uint32_t t = 0; t < kMaxTraits; ++t) {
+        float v = d[t];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        z[t] = (double)v;
+    }
+#else
 #pragma unroll
     for (uint32_t t = 0; t < kMaxTraits; ++t) {
         double v = (double)d[t];
@@ -282,6 +295,7 @@ __device__ __forceinline__ void row_phenotype(const PopDev& P, const DevStatus& 
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         z[t] = v;
     }
+#endif
     if (lane < kMaxTraits) {
         const double zz = lane == 0 ? z[0] : lane == 1 ? z[1] : lane == 2 ? z[2] : z[3];
         P.zg[st.cur][(size_t)g * 4u + lane] = R.zbase + zz;

@@ -7,7 +7,8 @@ the tape; libclotho_gpu.so replays the same tape.  Bar:
     width, the free list (fixed ascending then lost ascending), counts, the
     allele table (positions, ages), the fixed-allele table;
   * phenotypes: the GPU carries each genome's sum from its parent row and adds
-    the switched alleles' effects as FP32 lane sums folded into FP64; the FP64
+    the switched alleles' effects as FP32 lane sums reduced across the warp in
+    FP32 and added to the FP64 carried sum; the FP64
     oracle re-sums every set bit.  Each generation contributes at most the error
     of an FP32 sum of n terms of magnitude <= sum|w|, and carried sums inherit
     their ancestors' residue, so the tolerance written here is population-wide:
