@@ -20,7 +20,8 @@
 //              + sum(new alleles): the per-genome sum of
 //              batch_phenotype_task_population_space_row.hpp:127-153, carried
 //              from the parent row instead of re-walking every set bit.
-//              Per-lane FP32 partial sums, FP64 per-genome values.
+//              Per-lane FP32 partial sums reduced across the warp in FP32,
+//              FP64 per-genome values.
 //   free space AND/OR of the finished words, the next generation's
 //              FreeSpaceAnalyzerMT input (free_space_task_population_space_row_interlaced.hpp:51-72).
 //
@@ -35,12 +36,13 @@
 //   intervals  (wider allele spaces): sorted thresholds pair into half-open rank
 //              intervals; every heterozygous bit is classified by its rank.
 //
-// Rows are 64-word chunks, two words (one 128-bit load) per lane; parent words
-// are loaded two chunks ahead of use and the whole parent row is prefetched
-// into L2 at row start.  Effects of switched alleles are gathered from a
-// per-warp queue, four entries per lane, so lanes stay balanced.  The kernel is
-// persistent: one CTA per SM takes items of rows from a device counter and its
-// warps claim rows one at a time, so warps never wait on each other inside an item.
+// Rows are 64-word chunks, two words (one 128-bit load) per lane; a crossover
+// row's parent words are loaded one chunk ahead of use and the whole parent row
+// is prefetched into L2 at row start.  Effects of switched alleles are gathered
+// from a per-warp queue, kRoundLane entries per lane a round, so lanes stay
+// balanced.  The kernel is persistent, one CTA per SM: with one population each
+// warp claims rows one at a time from a device counter; a batch hands each CTA
+// items of rows, which its warps claim one at a time.
 #include "engine.cuh"
 
 namespace clotho {
@@ -310,10 +312,10 @@ __device__ __forceinline__ void row_phenotype(const PopDev& P, const DevStatus& 
 // toggled first, then XOR_k suf[g_k] is folded in, many table loads in flight
 // at a time.  The streaming loop reads (and clears) two mask words per lane
 // per chunk, so it waits on nothing but the parent words, which are loaded
-// two chunks ahead.
+// one chunk ahead (CLOTHO_XO_DEPTH).
 //
 // Effects of switched alleles go through the per-warp queue (slot | sign << 31)
-// and are gathered four per lane.  A row gathers the smaller of two sets: the
+// and are gathered kRoundLane per lane a round (loads folded in one round later).  A row gathers the smaller of two sets: the
 // switched heterozygous bits (z = z(top) + sum (bottom - top) w), or, when the
 // breakpoints switch more than half of the rank space, the unswitched ones
 // (z = z(bottom) + sum (top - bottom) w); both give the same phenotype up to
@@ -385,8 +387,11 @@ __device__ CLOTHO_COLD float4 effects_direct(uint64_t m0, uint64_t m1, uint64_t 
     return make_float4(d[0], d[1], d[2], d[3]);
 }
 
+#ifndef CLOTHO_XO_DEPTH
+#define CLOTHO_XO_DEPTH 2   // parent-word chunks held in registers by a crossover row's streaming loop (2 or 3)
+#endif
 #ifndef CLOTHO_ROUND_LANE
-#define CLOTHO_ROUND_LANE 2
+#define CLOTHO_ROUND_LANE 3
 #endif
 #ifndef CLOTHO_TABLE_INFLIGHT
 #define CLOTHO_TABLE_INFLIGHT 16
@@ -407,7 +412,7 @@ constexpr uint32_t kWarpChunk = CLOTHO_WARP_CHUNK;   // rows a warp claims at a 
 // to land behind.
 struct EffRound {
     float4 ef[kRoundLane];
-    float sg[kRoundLane];  // +1 / -1, 0 for an empty entry
+    uint32_t sg;  // bit k: entry k is added (else subtracted); an empty entry loads zeros
 };
 
 __device__ __forceinline__ void effq_issue(const uint32_t* Q, uint32_t head, uint32_t n,
@@ -418,7 +423,8 @@ __device__ __forceinline__ void effq_issue(const uint32_t* Q, uint32_t head, uin
         const uint32_t i = lane + 32u * k;
         const bool ok = i < n;
         const uint32_t e = ok ? Q[(head + i) & (kQueueCap - 1u)] : 0u;
-        r.sg[k] = ok ? ((e >> 31) ? 1.0f : -1.0f) : 0.0f;
+        if (k == 0) r.sg = 0u;
+        r.sg |= (e >> 31) << k;
         r.ef[k] = ok ? __ldg(eff4 + (e & 0x7fffffffu)) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
@@ -426,19 +432,18 @@ __device__ __forceinline__ void effq_issue(const uint32_t* Q, uint32_t head, uin
 __device__ __forceinline__ void effq_complete(const EffRound& r, float (&d)[kMaxTraits]) {
 #pragma unroll
     for (uint32_t k = 0; k < kRoundLane; ++k) {
-        d[0] = fmaf(r.sg[k], r.ef[k].x, d[0]);
-        d[1] = fmaf(r.sg[k], r.ef[k].y, d[1]);
-        d[2] = fmaf(r.sg[k], r.ef[k].z, d[2]);
-        d[3] = fmaf(r.sg[k], r.ef[k].w, d[3]);
+        const float sg = ((r.sg >> k) & 1u) ? 1.0f : -1.0f;
+        d[0] = fmaf(sg, r.ef[k].x, d[0]);
+        d[1] = fmaf(sg, r.ef[k].y, d[1]);
+        d[2] = fmaf(sg, r.ef[k].z, d[2]);
+        d[3] = fmaf(sg, r.ef[k].w, d[3]);
     }
 }
 
 __device__ __forceinline__ void effq_clear(EffRound& r) {
 #pragma unroll
-    for (uint32_t k = 0; k < kRoundLane; ++k) {
-        r.sg[k] = 0.0f;
-        r.ef[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
+    r.sg = 0u;
+    for (uint32_t k = 0; k < kRoundLane; ++k) r.ef[k] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // Queue the gathered bits (g0, g1) of the lane's words w, w+1 (sign +1 where
@@ -619,13 +624,23 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
     uint32_t qh = 0, qt = 0;
     EffRound pend;
     effq_clear(pend);
+#if CLOTHO_XO_DEPTH == 3
     ulonglong2 t_a, b_a, t_b, b_b;
     load_pair(t_a, b_a, R, 2u * lane, xo);
     load_pair(t_b, b_b, R, 2u * lane + 64u, xo);
+#else
+    ulonglong2 t_a, b_a;
+    load_pair(t_a, b_a, R, 2u * lane, xo);
+#endif
     for (uint32_t w0 = 0; w0 < R.Wc; w0 += 64u) {
         const uint32_t w = w0 + 2u * lane;
+#if CLOTHO_XO_DEPTH == 3
         ulonglong2 t_c, b_c;
         load_pair(t_c, b_c, R, w + 128u, xo);
+#else
+        ulonglong2 t_b, b_b;
+        load_pair(t_b, b_b, R, w + 64u, xo);
+#endif
         uint64_t mx0 = 0, mx1 = 0;
         if (do_mut && R.mc) row_mutations(P, M, R, w, mx0, mx1);
         const bool live = w < R.Wc;
@@ -666,7 +681,9 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
             if (do_fs) fold_fs(sF, sV, w, x0, x1);
         }
         t_a = t_b; b_a = b_b;
+#if CLOTHO_XO_DEPTH == 3
         t_b = t_c; b_b = b_c;
+#endif
     }
     if (gather) {
         const long long c0 = PROF ? clock64() : 0;
