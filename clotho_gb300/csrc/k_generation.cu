@@ -1283,6 +1283,8 @@ void launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, W
 }
 
 // ---------------------------------------------------------------------------
+constexpr uint32_t kPlanSmemEv = 16;  // breakpoints of a row the plan kernel ranks in shared memory
+
 // Processing order of the offspring rows (parent-major): rows are sorted by
 // parent individual, so rows reading the same parent strands run side by side
 // and the second read of a strand is an L2 hit.  Counting sort by key; the
@@ -1334,6 +1336,9 @@ __global__ void k_ord_scatter(const PopDev* __restrict__ pops, uint32_t npops) {
 // event offsets.
 __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pops, uint32_t npops) {
     const uint32_t lane = threadIdx.x & 31u;
+    // a thread's thresholds (up to kPlanSmemEv) stay in shared memory while they are ranked
+    // against each other; longer lists use their global slots
+    __shared__ uint32_t s_cr[256][kPlanSmemEv + 1];
     for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         if (!P.plan_row) continue;
@@ -1390,7 +1395,7 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
             if (E > kMaxEvDevice) {
                 flags = kPlanLong;  // tape rows with very long event lists: direct compares
             } else if (E > 0) {
-                uint32_t* cr = P.plan_cr + base;
+                uint32_t* cr = E <= kPlanSmemEv ? s_cr[threadIdx.x] : P.plan_cr + base;
                 for (uint32_t k = 0; k < E; k += 2u) {
                     double e0, e1 = 0.0;
                     if (philox) {
@@ -1420,7 +1425,7 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
                     uint32_t c0, n;
                     const uint32_t b = table_row(cr[k], A, c0, n);
                     P.plan_go[base + k] = (b >> 6) * P.Wcap;
-                    cr[k] = c0 | (n << 20);
+                    P.plan_cr[base + k] = c0 | (n << 20);
                 }
             }
             if (E > kPlanMaxEvents) {
