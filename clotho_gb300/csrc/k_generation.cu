@@ -312,7 +312,7 @@ __device__ __forceinline__ void row_phenotype(const PopDev& P, const DevStatus& 
 // toggled first, then XOR_k suf[g_k] is folded in, many table loads in flight
 // at a time.  The streaming loop reads (and clears) two mask words per lane
 // per chunk, so it waits on nothing but the parent words, which are loaded
-// one chunk ahead (CLOTHO_XO_DEPTH).
+// one chunk ahead.
 //
 // Effects of switched alleles go through the per-warp queue (slot | sign << 31)
 // and are gathered kRoundLane per lane a round (loads folded in one round later).  A row gathers the smaller of two sets: the
@@ -387,9 +387,6 @@ __device__ CLOTHO_COLD float4 effects_direct(uint64_t m0, uint64_t m1, uint64_t 
     return make_float4(d[0], d[1], d[2], d[3]);
 }
 
-#ifndef CLOTHO_XO_DEPTH
-#define CLOTHO_XO_DEPTH 2   // parent-word chunks held in registers by a crossover row's streaming loop (2 or 3)
-#endif
 #ifndef CLOTHO_ROUND_LANE
 #define CLOTHO_ROUND_LANE 3
 #endif
@@ -399,9 +396,6 @@ __device__ CLOTHO_COLD float4 effects_direct(uint64_t m0, uint64_t m1, uint64_t 
 constexpr uint32_t kRoundLane = CLOTHO_ROUND_LANE;   // queue entries gathered per lane per round
 constexpr uint32_t kRound = 32u * kRoundLane;
 constexpr uint32_t kTableInflight = CLOTHO_TABLE_INFLIGHT;
-#ifndef CLOTHO_PUSH_MSB
-#define CLOTHO_PUSH_MSB 1
-#endif
 #ifndef CLOTHO_WARP_CHUNK
 #define CLOTHO_WARP_CHUNK 1
 #endif
@@ -472,7 +466,6 @@ __device__ __forceinline__ void effq_push(uint64_t g0, uint64_t g1, uint64_t s0,
 #pragma unroll
     for (uint32_t k = 0; k < 4; ++k) {
         const uint32_t base = w * 64u + 32u * k;
-#if CLOTHO_PUSH_MSB
         // highest bit first: one leading-zero count per bit, the sign bit shifted into place by it
         for (uint32_t x = gg[k]; x;) {
             const uint32_t c = (uint32_t)__clz(x);
@@ -480,13 +473,6 @@ __device__ __forceinline__ void effq_push(uint64_t g0, uint64_t g1, uint64_t s0,
             x ^= 0x80000000u >> c;
             ++i;
         }
-#else
-        for (uint32_t x = gg[k]; x; x &= x - 1u) {
-            const uint32_t j = (uint32_t)(__ffs(x) - 1);
-            Q[i & (kQueueCap - 1u)] = (base + j) | ((ss[k] >> j) << 31);
-            ++i;
-        }
-#endif
     }
     tail += H;
     __syncwarp();
@@ -624,23 +610,14 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
     uint32_t qh = 0, qt = 0;
     EffRound pend;
     effq_clear(pend);
-#if CLOTHO_XO_DEPTH == 3
-    ulonglong2 t_a, b_a, t_b, b_b;
-    load_pair(t_a, b_a, R, 2u * lane, xo);
-    load_pair(t_b, b_b, R, 2u * lane + 64u, xo);
-#else
+    // parent words one chunk ahead (the strands are prefetched into L2 at row start;
+    // a second chunk in registers measured slower: it takes the registers of the gather rounds)
     ulonglong2 t_a, b_a;
     load_pair(t_a, b_a, R, 2u * lane, xo);
-#endif
     for (uint32_t w0 = 0; w0 < R.Wc; w0 += 64u) {
         const uint32_t w = w0 + 2u * lane;
-#if CLOTHO_XO_DEPTH == 3
-        ulonglong2 t_c, b_c;
-        load_pair(t_c, b_c, R, w + 128u, xo);
-#else
         ulonglong2 t_b, b_b;
         load_pair(t_b, b_b, R, w + 64u, xo);
-#endif
         uint64_t mx0 = 0, mx1 = 0;
         if (do_mut && R.mc) row_mutations(P, M, R, w, mx0, mx1);
         const bool live = w < R.Wc;
@@ -681,9 +658,6 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
             if (do_fs) fold_fs(sF, sV, w, x0, x1);
         }
         t_a = t_b; b_a = b_b;
-#if CLOTHO_XO_DEPTH == 3
-        t_b = t_c; b_b = b_c;
-#endif
     }
     if (gather) {
         const long long c0 = PROF ? clock64() : 0;
