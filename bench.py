@@ -420,17 +420,26 @@ def main():
         pop.info()
         dist.barrier()
         pop.sync()
+        # every step uploads its tape and reads back its status; the next step is issued before the
+        # previous status is collected, so its tape upload overlaps the previous step's kernels
         t0 = time.perf_counter()
-        for k in range(args.steps):
-            pop.simulate(tapes[k % 2])
-            pop.info()  # device->host read of the step's status (mean fitness)
+        pop.simulate(tapes[0])
+        ticket = pop.info_request()
+        for k in range(1, args.steps + 1):
+            nxt = None
+            if k < args.steps:
+                pop.simulate(tapes[k % 2])
+                nxt = pop.info_request()
+            pop.info_wait(ticket)  # device->host read of step k-1's status (mean fitness)
+            ticket = nxt
         dt = time.perf_counter() - t0
         dist.barrier()
         dt = dist.max(dt)
         pop.check()
         e2e = {"value": 2.0 * N * args.steps * world / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": 80, "ms_per_step": 1e3 * dt / args.steps,
-               "note": "tape call per generation (uniform-parent tape), wall clock around H2D + kernels + D2H"}
+               "note": "tape call per generation (uniform-parent tape), wall clock around H2D + kernels + D2H; "
+                       "each step's status read is collected after the next step is issued"}
         for ptr in keep:
             cg.capi.load().clotho_host_free(ptr)
 

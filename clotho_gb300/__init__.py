@@ -211,6 +211,18 @@ class Population:
         self._ck(self.L.clotho_get_info(self.h, C.byref(i)), "get_info")
         return {n: getattr(i, n) for n, _ in capi.Info._fields_}
 
+    def info_request(self) -> int:
+        """Ticket for the status as of the work issued so far (returns at once)."""
+        t = C.c_uint32()
+        self._ck(self.L.clotho_info_request(self.h, C.byref(t)), "info_request")
+        return t.value
+
+    def info_wait(self, ticket: int) -> dict:
+        """The status copied by info_request(ticket), once its copy has landed."""
+        i = capi.Info()
+        self._ck(self.L.clotho_info_wait(self.h, ticket, C.byref(i)), "info_wait")
+        return {n: getattr(i, n) for n, _ in capi.Info._fields_}
+
     def check(self):
         err = self.info()["device_error"]
         if err:
@@ -491,6 +503,16 @@ class Batch:
     def info(self, i: int) -> dict:
         inf = capi.Info()
         self._ck(self.L.clotho_pop_info(self.h, i, C.byref(inf)), "pop_info")
+        return {n: getattr(inf, n) for n, _ in capi.Info._fields_}
+
+    def info_request(self, i: int) -> int:
+        t = C.c_uint32()
+        self._ck(self.L.clotho_pop_info_request(self.h, i, C.byref(t)), "pop_info_request")
+        return t.value
+
+    def info_wait(self, ticket: int) -> dict:
+        inf = capi.Info()
+        self._ck(self.L.clotho_info_wait(self.h, ticket, C.byref(inf)), "info_wait")
         return {n: getattr(inf, n) for n, _ in capi.Info._fields_}
 
     def rows(self, i: int) -> np.ndarray:

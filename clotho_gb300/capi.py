@@ -73,6 +73,8 @@ SIGNATURES = {
     "clotho_fitness": (C.c_int, [vp]),
     "clotho_end_generation": (C.c_int, [vp]),
     "clotho_get_info": (C.c_int, [vp, C.POINTER(Info)]),
+    "clotho_info_request": (C.c_int, [vp, C.POINTER(u32)]),
+    "clotho_info_wait": (C.c_int, [vp, u32, C.POINTER(Info)]),
     "clotho_get_rows": (C.c_int, [vp, vp, C.c_size_t]),
     "clotho_get_alleles": (C.c_int, [vp, vp, vp, vp]),
     "clotho_get_fixed": (C.c_int, [vp, vp, vp, vp]),
@@ -104,6 +106,7 @@ SIGNATURES = {
     "clotho_pop_remove": (C.c_int, [vp, u32]),
     "clotho_pop_init": (C.c_int, [vp, u32, u32]),
     "clotho_pop_info": (C.c_int, [vp, u32, C.POINTER(Info)]),
+    "clotho_pop_info_request": (C.c_int, [vp, u32, C.POINTER(u32)]),
     "clotho_pop_rows": (C.c_int, [vp, u32, vp, C.c_size_t]),
     "clotho_pop_stats": (C.c_int, [vp, u32, C.POINTER(Stats), vp, u32]),
     "clotho_batch_generation_philox": (C.c_int, [vp, vp]),

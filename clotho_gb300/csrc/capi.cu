@@ -94,6 +94,10 @@ struct clotho_ctx {
     // step headers (N, M per population) are staged in a ring of pinned slots:
     // a slot is reused only after the copy that read it has completed
     uint32_t* h_ring = nullptr;                         // [kHdrRing][2 * kMaxPops]
+    // asynchronous status read-back: a pinned ring of status copies, each behind an event
+    DevStatus* h_stat = nullptr;                        // [kStatRing]
+    cudaEvent_t stat_ev[8]{};
+    uint32_t stat_next = 0;                             // tickets issued so far
     cudaEvent_t ring_ev[64]{};
     bool ring_used[64]{};
     uint32_t ring_next = 0;
@@ -118,7 +122,9 @@ struct clotho_ctx {
 namespace {
 
 constexpr uint32_t kHdrRing = 64;
+constexpr uint32_t kStatRing = 8;   // outstanding asynchronous status reads (clotho_info_request)
 static_assert(sizeof(((clotho_ctx*)nullptr)->ring_ev) / sizeof(cudaEvent_t) == kHdrRing, "header ring size");
+static_assert(sizeof(((clotho_ctx*)nullptr)->stat_ev) / sizeof(cudaEvent_t) == kStatRing, "status ring size");
 
 int fail(clotho_ctx* c, int code, const std::string& m) {
     if (c) c->err = m;
@@ -485,6 +491,9 @@ int clotho_destroy(clotho_ctx* ctx) {
         if (ctx->d_hdr[s]) cudaFree(ctx->d_hdr[s]);
     }
     if (ctx->h_ring) cudaFreeHost(ctx->h_ring);
+    if (ctx->h_stat) cudaFreeHost(ctx->h_stat);
+    for (uint32_t k = 0; k < kStatRing; ++k)
+        if (ctx->stat_ev[k]) cudaEventDestroy(ctx->stat_ev[k]);
     for (uint32_t k = 0; k < kHdrRing; ++k)
         if (ctx->ring_ev[k]) cudaEventDestroy(ctx->ring_ev[k]);
     if (ctx->d_ctl) cudaFree(ctx->d_ctl);
@@ -893,6 +902,62 @@ static int info_of(clotho_ctx* ctx, uint32_t idx, clotho_info* out) {
 }
 
 int clotho_get_info(clotho_ctx* ctx, clotho_info* out) { return info_of(ctx, 0, out); }
+
+static void info_from_status(const DevStatus& s, clotho_info* out) {
+    out->generation = s.gen;
+    out->N = s.N;
+    out->A = s.A;
+    out->W = s.W;
+    out->fixed_count = s.fixed_cnt;
+    out->lost_count = s.lost_cnt;
+    out->free_count = s.free_cnt;
+    out->variable_count = (s.pA > s.free_cnt ? s.pA - s.free_cnt : 0);
+    out->fixed_total = s.fixed_total;
+    out->last_M = s.last_M;
+    out->all_neutral = s.all_neutral;
+    out->device_error = s.err;
+    out->mean_fitness = s.N ? s.fit_total / (double)s.N : 0.0;
+}
+
+
+// The status copy is ordered behind everything issued so far on the context's stream; the host
+// thread goes on issuing work and collects the copy with clotho_info_wait.
+static int info_request(clotho_ctx* ctx, uint32_t idx, uint32_t* ticket) {
+    if (!ctx || !ticket || idx >= ctx->pops.size()) return fail(ctx, CLOTHO_E_ARG, "no such population");
+    if (!ctx->h_stat) {
+        if (cudaMallocHost(&ctx->h_stat, sizeof(DevStatus) * kStatRing) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->h_stat = nullptr;
+            return fail(ctx, CLOTHO_E_NOMEM, "pinned host memory refused");
+        }
+        for (uint32_t k = 0; k < kStatRing; ++k) CK(cudaEventCreateWithFlags(&ctx->stat_ev[k], cudaEventDisableTiming));
+    }
+    const uint32_t t = ctx->stat_next;
+    const uint32_t k = t % kStatRing;
+    if (t >= kStatRing) CK(cudaEventSynchronize(ctx->stat_ev[k]));  // the slot's previous copy has landed
+    CK(cudaMemcpyAsync(&ctx->h_stat[k], ctx->pops[idx]->dev[0].st, sizeof(DevStatus), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaEventRecord(ctx->stat_ev[k], ctx->stream));
+    ctx->stat_next = t + 1;
+    *ticket = t;
+    return 0;
+}
+
+static int info_wait(clotho_ctx* ctx, uint32_t ticket, clotho_info* out) {
+    if (!ctx || !out) return CLOTHO_E_ARG;
+    if (ticket >= ctx->stat_next || ctx->stat_next - ticket > kStatRing)
+        return fail(ctx, CLOTHO_E_ARG, "unknown or overwritten info ticket");
+    const uint32_t k = ticket % kStatRing;
+    CK(cudaEventSynchronize(ctx->stat_ev[k]));
+    info_from_status(ctx->h_stat[k], out);
+    return 0;
+}
+
+int clotho_info_request(clotho_ctx* ctx, uint32_t* ticket) { return info_request(ctx, 0, ticket); }
+int clotho_pop_info_request(clotho_ctx* ctx, uint32_t index, uint32_t* ticket) {
+    return info_request(ctx, index, ticket);
+}
+int clotho_info_wait(clotho_ctx* ctx, uint32_t ticket, clotho_info* out) { return info_wait(ctx, ticket, out); }
 
 static int rows_of(clotho_ctx* ctx, uint32_t idx, uint64_t* dst, size_t dst_words) {
     if (!ctx || idx >= ctx->pops.size()) return fail(ctx, CLOTHO_E_ARG, "no such population");

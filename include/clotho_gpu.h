@@ -213,6 +213,15 @@ int  clotho_end_generation(clotho_ctx *ctx);
 
 /* ---- read-back (synchronising) ------------------------------------------ */
 int  clotho_get_info(clotho_ctx *ctx, clotho_info *out);
+/* Asynchronous read-back of the same fields: the request copies the status
+ * behind the work issued so far and returns at once with a ticket, so the
+ * caller can issue the next generation (and its tape upload) before
+ * clotho_info_wait blocks for the copy.  Tickets count up from 0 per context;
+ * at most 8 are outstanding (a ninth request waits for the oldest copy).  No
+ * reference counterpart: the reference engine returns to its caller only
+ * after a generation (engine_batched_task.hpp:163-223). */
+int  clotho_info_request(clotho_ctx *ctx, uint32_t *ticket);
+int  clotho_info_wait(clotho_ctx *ctx, uint32_t ticket, clotho_info *out);
 /* Current child rows, 2N x W words (reference width). */
 int  clotho_get_rows(clotho_ctx *ctx, uint64_t *dst, size_t dst_words);
 /* Allele table [A]: positions, ages, effects [A*T] (FP32). */
@@ -307,6 +316,7 @@ int  clotho_pop_add(clotho_ctx *ctx, const clotho_desc *desc, uint32_t *index);
 int  clotho_pop_remove(clotho_ctx *ctx, uint32_t index);
 int  clotho_pop_init(clotho_ctx *ctx, uint32_t index, uint32_t N0);
 int  clotho_pop_info(clotho_ctx *ctx, uint32_t index, clotho_info *out);
+int  clotho_pop_info_request(clotho_ctx *ctx, uint32_t index, uint32_t *ticket);  /* clotho_info_wait */
 int  clotho_pop_rows(clotho_ctx *ctx, uint32_t index, uint64_t *dst, size_t dst_words);
 int  clotho_pop_stats(clotho_ctx *ctx, uint32_t index, clotho_stats *out, uint32_t *sfs, uint32_t sfs_len);
 int  clotho_pop_margins(clotho_ctx *ctx, uint32_t index, uint32_t *col_counts, uint32_t *row_counts);

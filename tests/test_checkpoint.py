@@ -231,3 +231,34 @@ def test_phase_clocks_cover_every_row_and_change_no_result():
     assert sum(b.phase_clocks().values()) == 0
     for p in (a, b):
         p.close()
+
+
+def test_async_info_requests_match_synchronous_reads():
+    N = 1500
+    a = cg.Population(N, 1 << 13, 2, **KW)
+    b = cg.Population(N, 1 << 13, 2, **KW)
+    for p in (a, b):
+        p.init(N)
+    sync_infos = []
+    for _ in range(6):
+        a.simulate_philox(N)
+        sync_infos.append(a.info())
+    tickets = []
+    for _ in range(6):
+        b.simulate_philox(N)
+        tickets.append(b.info_request())   # issued behind the generation, collected later
+    assert [b.info_wait(t) for t in tickets] == sync_infos
+    assert tickets == list(range(6))
+    for _ in range(9):
+        b.info_request()
+    with pytest.raises(cg.ClothoError):
+        b.info_wait(tickets[0])             # more than 8 requests ago: its slot was reused
+    for p in (a, b):
+        p.close()
+    jobs = [dict(N=1200, seed=5), dict(N=900, seed=6)]
+    bt = cg.Batch([cg.make_desc(j["N"], 1 << 13, 2, mu=0.05, rho=2.0, seed=j["seed"]) for j in jobs])
+    bt.init()
+    bt.run(3)
+    t = [bt.info_request(i) for i in range(2)]
+    assert [bt.info_wait(x) for x in t] == [bt.info(i) for i in range(2)]
+    bt.close()
