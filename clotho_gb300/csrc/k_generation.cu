@@ -396,6 +396,7 @@ __device__ CLOTHO_COLD float4 effects_direct(uint64_t m0, uint64_t m1, uint64_t 
 constexpr uint32_t kRoundLane = CLOTHO_ROUND_LANE;   // queue entries gathered per lane per round
 constexpr uint32_t kRound = 32u * kRoundLane;
 constexpr uint32_t kTableInflight = CLOTHO_TABLE_INFLIGHT;
+constexpr uint32_t kFlatLoads = 4;   // table loads per lane when a narrow row's whole mask is built at once
 #ifndef CLOTHO_WARP_CHUNK
 #define CLOTHO_WARP_CHUNK 1
 #endif
@@ -435,8 +436,8 @@ __device__ __forceinline__ void effq_complete(const EffRound& r, float (&d)[kMax
 }
 
 __device__ __forceinline__ void effq_clear(EffRound& r) {
-#pragma unroll
     r.sg = 0u;
+#pragma unroll
     for (uint32_t k = 0; k < kRoundLane; ++k) r.ef[k] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
@@ -736,45 +737,84 @@ __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st
         row_body_copy(P, st.M, R, sfix, do_mut, do_fs, sF, sV);
 #endif
     } else {
-        // corrections: toggle the slots whose rank lies between threshold and table row
         uint32_t* m32 = reinterpret_cast<uint32_t*>(mask);
-        for (uint32_t k0 = 0; k0 < E; k0 += 32u) {
-            const uint32_t my_cr = (k0 + lane < E) ? __ldg(P.plan_cr + base + k0 + lane) : 0u;
-            const uint32_t ke = min(32u, E - k0);
+        const uint64_t* __restrict__ suf = P.suf;
+        const uint32_t np = R.Wp >> 1;  // word pairs of a table row
+        if (np != 0u && E <= 32u && E * np <= 32u * kFlatLoads) {
+            // narrow rows (batches of small populations): the table rows' words of every breakpoint are
+            // spread over the lanes and loaded at once, then XORed in with shared atomics, so the mask
+            // costs one table round trip instead of one per breakpoint
+            const uint32_t my_cr = lane < E ? __ldg(P.plan_cr + base + lane) : 0u;
+            const uint32_t my_go = lane < E ? __ldg(P.plan_go + base + lane) : 0u;
+            ulonglong2 v[kFlatLoads];
+            uint32_t at[kFlatLoads];
+#pragma unroll
+            for (uint32_t j = 0; j < kFlatLoads; ++j) {
+                const uint32_t i = lane + 32u * j;
+                const uint32_t k = i / np;  // breakpoint of this word pair (np >= 4)
+                const uint32_t go = __shfl_sync(0xffffffffu, my_go, k & 31u);
+                at[j] = i < E * np ? i - k * np : 0xffffffffu;
+                v[j] = i < E * np ? __ldg(reinterpret_cast<const ulonglong2*>(suf + go) + (i - k * np))
+                                  : make_ulonglong2(0, 0);
+            }
+            // corrections: toggle the slots whose rank lies between threshold and table row
 #pragma unroll 4
-            for (uint32_t k = 0; k < ke; ++k) {
+            for (uint32_t k = 0; k < E; ++k) {
                 const uint32_t pc = __shfl_sync(0xffffffffu, my_cr, k);
                 if (lane < (pc >> 20)) {
-                    const uint32_t s = __ldg(P.inv + (pc & 0xfffffu) + lane);
-                    atomicXor(m32 + (s >> 5), 1u << (s & 31u));
+                    const uint32_t sl = __ldg(P.inv + (pc & 0xfffffu) + lane);
+                    atomicXor(m32 + (sl >> 5), 1u << (sl & 31u));
                 }
             }
-        }
-        __syncwarp();
-        // XOR of the events' table rows, kTableInflight 16-byte loads per lane in flight
-        const uint64_t* __restrict__ suf = P.suf;
-        ulonglong2* m2 = reinterpret_cast<ulonglong2*>(mask);
-        for (uint32_t k0 = 0; k0 < E; k0 += 32u) {
-            const uint32_t my_go = (k0 + lane < E) ? __ldg(P.plan_go + base + k0 + lane) : 0u;
-            const uint32_t ke = min(32u, E - k0);
-            for (uint32_t k = 0; k < ke; ++k) {
-                const uint64_t* tk = suf + __shfl_sync(0xffffffffu, my_go, k);
-                for (uint32_t wb = 0; wb < R.Wp; wb += 64u * kTableInflight) {
-                    ulonglong2 v[kTableInflight];
 #pragma unroll
-                    for (uint32_t j = 0; j < kTableInflight; ++j) {
-                        const uint32_t w = wb + 64u * j + 2u * lane;
-                        v[j] = (w < R.Wp) ? __ldg(reinterpret_cast<const ulonglong2*>(tk + w))
-                                          : make_ulonglong2(0, 0);
+            for (uint32_t j = 0; j < kFlatLoads; ++j) {
+                if (at[j] != 0xffffffffu) {
+                    uint32_t* mw = m32 + 4u * at[j];
+                    if ((uint32_t)v[j].x) atomicXor(mw, (uint32_t)v[j].x);
+                    if ((uint32_t)(v[j].x >> 32)) atomicXor(mw + 1, (uint32_t)(v[j].x >> 32));
+                    if ((uint32_t)v[j].y) atomicXor(mw + 2, (uint32_t)v[j].y);
+                    if ((uint32_t)(v[j].y >> 32)) atomicXor(mw + 3, (uint32_t)(v[j].y >> 32));
+                }
+            }
+        } else {
+            // corrections: toggle the slots whose rank lies between threshold and table row
+            for (uint32_t k0 = 0; k0 < E; k0 += 32u) {
+                const uint32_t my_cr = (k0 + lane < E) ? __ldg(P.plan_cr + base + k0 + lane) : 0u;
+                const uint32_t ke = min(32u, E - k0);
+    #pragma unroll 4
+                for (uint32_t k = 0; k < ke; ++k) {
+                    const uint32_t pc = __shfl_sync(0xffffffffu, my_cr, k);
+                    if (lane < (pc >> 20)) {
+                        const uint32_t s = __ldg(P.inv + (pc & 0xfffffu) + lane);
+                        atomicXor(m32 + (s >> 5), 1u << (s & 31u));
                     }
-#pragma unroll
-                    for (uint32_t j = 0; j < kTableInflight; ++j) {
-                        const uint32_t w = wb + 64u * j + 2u * lane;
-                        if (w < R.Wp) {
-                            ulonglong2 x = m2[w >> 1];
-                            x.x ^= v[j].x;
-                            x.y ^= v[j].y;
-                            m2[w >> 1] = x;
+                }
+            }
+            __syncwarp();
+            // XOR of the events' table rows, kTableInflight 16-byte loads per lane in flight
+            ulonglong2* m2 = reinterpret_cast<ulonglong2*>(mask);
+            for (uint32_t k0 = 0; k0 < E; k0 += 32u) {
+                const uint32_t my_go = (k0 + lane < E) ? __ldg(P.plan_go + base + k0 + lane) : 0u;
+                const uint32_t ke = min(32u, E - k0);
+                for (uint32_t k = 0; k < ke; ++k) {
+                    const uint64_t* tk = suf + __shfl_sync(0xffffffffu, my_go, k);
+                    for (uint32_t wb = 0; wb < R.Wp; wb += 64u * kTableInflight) {
+                        ulonglong2 v[kTableInflight];
+    #pragma unroll
+                        for (uint32_t j = 0; j < kTableInflight; ++j) {
+                            const uint32_t w = wb + 64u * j + 2u * lane;
+                            v[j] = (w < R.Wp) ? __ldg(reinterpret_cast<const ulonglong2*>(tk + w))
+                                              : make_ulonglong2(0, 0);
+                        }
+    #pragma unroll
+                        for (uint32_t j = 0; j < kTableInflight; ++j) {
+                            const uint32_t w = wb + 64u * j + 2u * lane;
+                            if (w < R.Wp) {
+                                ulonglong2 x = m2[w >> 1];
+                                x.x ^= v[j].x;
+                                x.y ^= v[j].y;
+                                m2[w >> 1] = x;
+                            }
                         }
                     }
                 }
