@@ -70,6 +70,8 @@ std::vector<size_t> sizes_of(const Geometry& g) {
         A <= kSufMaxSlots ? S * 4 : 0,                            // ord_pos
         A <= kSufMaxSlots ? g.EVcap * 4ull : 0,                   // plan_go
         A <= kSufMaxSlots ? g.EVcap * 4ull : 0,                   // plan_cr
+        A <= kSufMaxSlots ? S * 8 : 0,                            // plan_mut
+        A <= kSufMaxSlots ? S * 32 : 0,                           // plan_z
         sizeof(DevStatus),
         // two tape sets: pairs, swap, ev_off, ev_pos, mut_seq, mut_pos, mut_eff
         S * 4, S, (S + 1) * 4, g.EVcap * 8ull, g.Mcap * 4ull, g.Mcap * 8ull, g.Mcap * T * 4ull,
@@ -224,6 +226,7 @@ int alloc_pop(clotho_ctx* ctx, const clotho_desc& d, PopHost** out) {
     b.ord_off = b.ord_cnt ? b.ord_cnt + (g.Scap + 1) : nullptr;
     b.ord_cur = (uint32_t*)ptr[k++]; b.ord_pos = (uint32_t*)ptr[k++];
     b.plan_go = (uint32_t*)ptr[k++]; b.plan_cr = (uint32_t*)ptr[k++];
+    b.plan_mut = (uint2*)ptr[k++]; b.plan_z = (double*)ptr[k++];
     b.st = (DevStatus*)ptr[k++];
     b.Scap = g.Scap; b.Ncap = g.Ncap; b.Wcap = g.Wcap; b.Acap = g.Aslots; b.Mcap = g.Mcap;
     b.EVcap = g.EVcap; b.FXcap = g.FXcap; b.T = g.T; b.NB = g.NB;

@@ -98,6 +98,8 @@ struct PopDev {
     uint32_t* ord_pos;     // [Scap] processing position of each row
     uint32_t* plan_go;     // [EVcap] table row offset per planned event (with suf)
     uint32_t* plan_cr;     // [EVcap] correction ranks per planned event: first | count << 20 (with suf)
+    uint2*    plan_mut;    // [Scap] new alleles of the planned row (processing order): CSR offset, count
+    double*   plan_z;      // [Scap * 4] phenotype base of the planned row: z(base strand) - sum(fixed)
     DevStatus* st;
     uint32_t Scap, Ncap, Wcap, Acap, Mcap, EVcap, FXcap, T;
     uint32_t NB, pad2;     // position buckets (power of two)

@@ -229,8 +229,9 @@ __device__ __forceinline__ void row_setup(const PopDev& P, const DevStatus& st, 
 }
 
 // The new alleles of row g (lanes hold up to 32 slot indices) and their effects.
-__device__ __forceinline__ void row_mutation_setup(const PopDev& P, const DevStatus& st, uint32_t g, bool do_mut,
-                                                   bool gather, RowArgs& R, float (&d)[kMaxTraits]) {
+// The new alleles of the row: CSR range [mo, mo + mc) of the mutation list.
+__device__ __forceinline__ void row_mutation_setup(const PopDev& P, const DevStatus& st, uint32_t mo, uint32_t mc,
+                                                   bool do_mut, bool gather, RowArgs& R, float (&d)[kMaxTraits]) {
     const uint32_t lane = threadIdx.x & 31u;
     const bool philox = R.philox;
     R.mo = 0;
@@ -238,8 +239,8 @@ __device__ __forceinline__ void row_mutation_setup(const PopDev& P, const DevSta
     R.my_slot = 0xffffffffu;
     const float4* eff4 = reinterpret_cast<const float4*>(P.eff);
     if (do_mut) {
-        R.mo = P.row_off[g];
-        R.mc = P.row_off[g + 1u] - R.mo;
+        R.mo = mo;
+        R.mc = mc;
         if (lane < R.mc) {
             const uint32_t i = R.mo + lane;
             const uint32_t mi = philox ? i : P.row_mut[i];
@@ -260,6 +261,12 @@ __device__ __forceinline__ void row_mutation_setup(const PopDev& P, const DevSta
             }
         }
     }
+}
+
+__device__ __forceinline__ void row_mutation_setup(const PopDev& P, const DevStatus& st, uint32_t g, bool do_mut,
+                                                   bool gather, RowArgs& R, float (&d)[kMaxTraits]) {
+    const uint32_t mo = do_mut ? P.row_off[g] : 0u;
+    row_mutation_setup(P, st, mo, do_mut ? P.row_off[g + 1u] - mo : 0u, do_mut, gather, R, d);
 }
 
 // Breakpoint k of the row as a double.
@@ -706,6 +713,8 @@ __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st
     const long long c0 = PROF ? clock64() : 0;
     long long c1 = 0, c2 = 0, c3 = 0;
     const uint4 pr = __ldg(P.plan_row + v);
+    const uint2 pm = __ldg(P.plan_mut + v);
+    const double pz = (do_ph && lane < kMaxTraits) ? __ldg(P.plan_z + (size_t)v * 4u + lane) : 0.0;
     const uint32_t g = pr.x, topr = pr.y, base = pr.z;
     const uint32_t E = pr.w & kPlanMaxEvents, flags = pr.w >> kPlanFlagShift;
     const bool inv = gather && (flags & kPlanInv) != 0;
@@ -722,11 +731,9 @@ __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st
     R.evg = P.ev_pos + base;
     if (E > 0 || !CLOTHO_COPY_BULK) prefetch_l2(R.top, R.Wp * 8u);
     if (E > 0) prefetch_l2(R.bot, R.Wp * 8u);
-    R.zbase = 0.0;
-    if (do_ph && lane < kMaxTraits)
-        R.zbase = P.zg[st.cur ^ 1u][(size_t)(inv ? topr ^ 1u : topr) * 4u + lane] - P.st->fixsum[lane];
+    R.zbase = pz;  // z(inv ? bottom : top) - sum(fixed), from the plan
     float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
-    row_mutation_setup(P, st, g, do_mut, gather, R, d);
+    row_mutation_setup(P, st, pm.x, pm.y, do_mut, gather, R, d);
     if (PROF) c1 = clock64();
     if (flags & kPlanLong) {
         add4(d, row_body_events(P, st.M, R, sfix, ws.q, do_mut, gather, do_fs, sF, sV));
@@ -1447,7 +1454,17 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
                 E = 0;
                 flags = 0;
             }
-            P.plan_row[P.ord_pos[g]] = make_uint4(g, 2u * pind + (swap ? 1u : 0u), base, E | (flags << kPlanFlagShift));
+            const uint32_t at = P.ord_pos[g];
+            const uint32_t topr = 2u * pind + (swap ? 1u : 0u);
+            P.plan_row[at] = make_uint4(g, topr, base, E | (flags << kPlanFlagShift));
+            // what the row's set-up would otherwise fetch after its plan: the new alleles' CSR
+            // range and the carried phenotype's base strand value less the fixed effects
+            const uint32_t mo = P.row_off[g];
+            P.plan_mut[at] = make_uint2(mo, P.row_off[g + 1u] - mo);
+            const uint32_t zs = ((flags & kPlanInv) && st.nz_eff != 0) ? topr ^ 1u : topr;
+            const double* zp = P.zg[st.cur ^ 1u] + (size_t)zs * 4u;
+#pragma unroll
+            for (uint32_t t = 0; t < kMaxTraits; ++t) P.plan_z[(size_t)at * 4u + t] = zp[t] - P.st->fixsum[t];
         }
     }
 }
