@@ -286,25 +286,29 @@ __device__ __forceinline__ double row_event(const PopDev& P, const DevStatus& st
 __device__ __forceinline__ void row_phenotype(const PopDev& P, const DevStatus& st, uint32_t g, const RowArgs& R,
                                               const float (&d)[kMaxTraits]) {
     const uint32_t lane = threadIdx.x & 31u;
-    double z[kMaxTraits];
+    double z[kMaxTraits] = {0.0, 0.0, 0.0, 0.0};
+    // a copy row without new alleles has nothing to add: one vote instead of the reduction
+    const bool any = __any_sync(0xffffffffu, (d[0] != 0.f) | (d[1] != 0.f) | (d[2] != 0.f) | (d[3] != 0.f));
+    if (any) {
 #if CLOTHO_PHENO_F32
-    // the lanes' FP32 sums are reduced in FP32 (GB300's FP64 pipe is narrow); the row's phenotype stays FP64
+        // the lanes' FP32 sums are reduced in FP32 (GB300's FP64 pipe is narrow); the row's phenotype stays FP64
 #pragma unroll
-    for (uint32_t t = 0; t < kMaxTraits; ++t) {
-        float v = d[t];
+        for (uint32_t t = 0; t < kMaxTraits; ++t) {
+            float v = d[t];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        z[t] = (double)v;
-    }
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            z[t] = (double)v;
+        }
 #else
 #pragma unroll
-    for (uint32_t t = 0; t < kMaxTraits; ++t) {
-        double v = (double)d[t];
+        for (uint32_t t = 0; t < kMaxTraits; ++t) {
+            double v = (double)d[t];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        z[t] = v;
-    }
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            z[t] = v;
+        }
 #endif
+    }
     if (lane < kMaxTraits) {
         const double zz = lane == 0 ? z[0] : lane == 1 ? z[1] : lane == 2 ? z[2] : z[3];
         P.zg[st.cur][(size_t)g * 4u + lane] = R.zbase + zz;
@@ -404,6 +408,7 @@ constexpr uint32_t kRoundLane = CLOTHO_ROUND_LANE;   // queue entries gathered p
 constexpr uint32_t kRound = 32u * kRoundLane;
 constexpr uint32_t kTableInflight = CLOTHO_TABLE_INFLIGHT;
 constexpr uint32_t kFlatLoads = 4;   // table loads per lane when a narrow row's whole mask is built at once
+constexpr uint32_t kDirectCopyChunks = 2;   // copy rows up to 128 words load their strand directly
 #ifndef CLOTHO_WARP_CHUNK
 #define CLOTHO_WARP_CHUNK 1
 #endif
@@ -562,6 +567,47 @@ __device__ __forceinline__ void row_body_copy(const PopDev& P, uint32_t M, const
 
 #endif
 
+// Narrow copy rows (the narrow build of the kernel, every row <= 128 words):
+// one 16-byte load a lane per chunk, all issued at once, cost less than arming
+// a barrier and waiting for a bulk copy.  A separate build keeps the wide rows'
+// code as it is (even an untaken branch to this path slowed them 2%).
+__device__ __forceinline__ void row_body_copy_direct(const PopDev& P, uint32_t M, const RowArgs& R,
+                                                  const uint64_t* sfix, bool do_mut, bool do_fs, uint64_t* sF,
+                                                  uint64_t* sV) {
+    const uint32_t lane = threadIdx.x & 31u;
+    ulonglong2 t[kDirectCopyChunks];
+#pragma unroll
+    for (uint32_t j = 0; j < kDirectCopyChunks; ++j) {
+        const uint32_t w = 64u * j + 2u * lane;
+        t[j] = w < R.Wp ? __ldg(reinterpret_cast<const ulonglong2*>(R.top + w)) : make_ulonglong2(0, 0);
+    }
+#pragma unroll
+    for (uint32_t j = 0; j < kDirectCopyChunks; ++j) {
+        const uint32_t w = 64u * j + 2u * lane;
+        if (64u * j >= R.Wc) break;
+        uint64_t mx0 = 0, mx1 = 0;
+        if (do_mut && R.mc) row_mutations(P, M, R, w, mx0, mx1);
+        if (w < R.Wc) {
+            const ulonglong2 fm =
+                w < R.Wp ? *reinterpret_cast<const ulonglong2*>(sfix + w) : make_ulonglong2(0, 0);
+            const uint64_t x0 = (t[j].x & ~fm.x) ^ mx0, x1 = (t[j].y & ~fm.y) ^ mx1;
+            *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(x0, x1);
+            if (do_fs) fold_fs(sF, sV, w, x0, x1);
+        }
+    }
+    if (R.Wc > 64u * kDirectCopyChunks) {  // a child wider than its parent: the rest is new alleles only
+        for (uint32_t w0 = 64u * kDirectCopyChunks; w0 < R.Wc; w0 += 64u) {
+            const uint32_t w = w0 + 2u * lane;
+            uint64_t mx0 = 0, mx1 = 0;
+            if (do_mut && R.mc) row_mutations(P, M, R, w, mx0, mx1);
+            if (w < R.Wc) {
+                *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(mx0, mx1);
+                if (do_fs) fold_fs(sF, sV, w, mx0, mx1);
+            }
+        }
+    }
+}
+
 // Copy rows through a bulk copy: the whole parent strand (<= 8 KB) lands in
 // the warp's (otherwise idle) bitmap in one asynchronous transfer, then the
 // lanes mask, mutate, store and fold it, and clear the bitmap behind them.
@@ -705,7 +751,7 @@ struct PhaseClk {
 // One offspring row, the whole warp (suffix-table classifier), from the plan
 // at processing position v (k_row_plan): row, top strand, breakpoints, table
 // rows and correction ranks.  PROF: clock the row's phases into pc.
-template <bool PROF>
+template <bool PROF, bool NARROW>
 __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st, uint32_t v, const uint64_t* sfix,
                                             uint64_t* mask, WarpSmem& ws, uint32_t& phase, bool do_mut, bool do_ph,
                                             bool gather, bool do_fs, uint64_t* sF, uint64_t* sV, PhaseClk& pc) {
@@ -739,7 +785,10 @@ __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st
         add4(d, row_body_events(P, st.M, R, sfix, ws.q, do_mut, gather, do_fs, sF, sV));
     } else if (E == 0) {
 #if CLOTHO_COPY_BULK
-        row_body_copy_bulk(P, st.M, R, sfix, mask, &ws.mbar, phase, do_mut, do_fs, sF, sV);
+        if (NARROW)
+            row_body_copy_direct(P, st.M, R, sfix, do_mut, do_fs, sF, sV);
+        else
+            row_body_copy_bulk(P, st.M, R, sfix, mask, &ws.mbar, phase, do_mut, do_fs, sF, sV);
 #else
         row_body_copy(P, st.M, R, sfix, do_mut, do_fs, sF, sV);
 #endif
@@ -1115,7 +1164,8 @@ __device__ __forceinline__ void gen_row_iv(const PopDev& P, const DevStatus& st,
 // too wide for that layout) the AND/OR fold goes to the population's global
 // accumulators and the fixed mask is read from global memory.
 // PROF (suffix-table build only): per-phase cycle counters into ctl->phase.
-template <bool SUF, bool PROF>
+// NARROW (suffix-table build only): every row is at most 128 words.
+template <bool SUF, bool PROF, bool NARROW>
 __global__ void __launch_bounds__(kGenThreads, 1)
 k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restrict__ ctl, uint32_t fuse,
              int profile, uint32_t maxW, uint32_t gacc) {
@@ -1181,7 +1231,7 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             for (uint32_t v = k; v < k1; ++v) {
                 const uint32_t g = v < Se ? 2u * v : 2u * (v - Se) + 1u;
                 if (SUF)
-                    gen_row_suf<PROF>(P, st, v, sfix, mask, ws, bphase, do_mut, do_ph, gather, do_fs, sF, sV, pc);
+                    gen_row_suf<PROF, NARROW>(P, st, v, sfix, mask, ws, bphase, do_mut, do_ph, gather, do_fs, sF, sV, pc);
                 else
                     gen_row_iv(P, st, g, sfix, s_iv[warp], s_thr[warp], s_q[warp], s_sm[warp], do_mut, do_ph,
                                gather, do_fs, sF, sV);
@@ -1247,7 +1297,7 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             // path takes its rows in plan order
             const uint32_t g = v < Se ? 2u * v : 2u * (v - Se) + 1u;
             if (SUF)
-                gen_row_suf<PROF>(P, st, v, sfix, mask, ws, bphase, do_mut, do_ph, gather, do_fs, sF, sV, pc);
+                gen_row_suf<PROF, NARROW>(P, st, v, sfix, mask, ws, bphase, do_mut, do_ph, gather, do_fs, sF, sV, pc);
             else
                 gen_row_iv(P, st, g, sfix, s_iv[warp], s_thr[warp], s_q[warp], s_sm[warp], do_mut, do_ph, gather,
                            do_fs, sF, sV);
@@ -1284,23 +1334,30 @@ void launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, W
     const uint32_t gacc = (!suf && 3ull * maxW * sizeof(uint64_t) + kWarps * 3584u > 220u * 1024u) ? 1u : 0u;
     const size_t smem =
         gacc ? 0 : (3ull + (suf ? kWarps : 0u)) * maxW * sizeof(uint64_t) + (suf ? kWarps * sizeof(WarpSmem) : 0);
-    // profile 2: the suffix-table kernel's build with phase clocks
-    static size_t configured[3] = {0, 0, 0};
-    const int si = suf ? (profile == 2 ? 2 : 1) : 0;
+    // profile 2: the suffix-table kernel's build with phase clocks; rows of at most
+    // 128 words: its narrow build (copy rows by direct loads)
+    static size_t configured[4] = {0, 0, 0, 0};
+    const bool narrow = maxW <= 64u * kDirectCopyChunks;
+    const int si = suf ? (profile == 2 ? 2 : narrow ? 3 : 1) : 0;
+    const void* fns[4] = {(const void*)k_generation<false, false, false>, (const void*)k_generation<true, false, false>,
+                          (const void*)k_generation<true, true, false>, (const void*)k_generation<true, false, true>};
     // static shared memory is above 48 KB on its own, so the opt-in attribute is always needed
     if (smem > configured[si] || configured[si] == 0) {
-        const void* fn = si == 2 ? (const void*)k_generation<true, true>
-                                 : si == 1 ? (const void*)k_generation<true, false> : (const void*)k_generation<false, false>;
-        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(fns[si], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured[si] = smem > 0 ? smem : 1;
     }
-    if (si == 2)
-        k_generation<true, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, 0u);
+    if (si == 3)
+        k_generation<true, false, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
+                                                                                   maxW, 0u);
+    else if (si == 2)
+        k_generation<true, true, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
+                                                                                   maxW, 0u);
     else if (si == 1)
-        k_generation<true, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW, 0u);
+        k_generation<true, false, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
+                                                                                    maxW, 0u);
     else
-        k_generation<false, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile, maxW,
-                                                                               gacc);
+        k_generation<false, false, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
+                                                                                     maxW, gacc);
 }
 
 // ---------------------------------------------------------------------------
