@@ -54,6 +54,30 @@ def test_batch_equals_alone():
         assert bs["mean_fitness"] == st["mean_fitness"]
 
 
+def test_narrow_and_wide_builds_agree():
+    # 512 slots (8-word rows): alone the population runs the narrow build of the generation kernel; batched
+    # with a population of 256-word rows it runs the wide build.  Same rows, spectrum and mean fitness.
+    G = 20
+    s = dict(N=500, T=2, mu=0.01, rho=3.0, fitness="gaussian_vs", fit_param=20.0, seed=21)
+    kw = {k: v for k, v in s.items() if k not in ("N", "T")}
+    d = cg.make_desc(s["N"], 512, s["T"], p_neutral=0.3, **kw)
+    pop = cg.Population(s["N"], 512, s["T"], mu=s["mu"], rho=s["rho"], fitness=s["fitness"],
+                        fit_param=s["fit_param"], p_neutral=0.3, seed=s["seed"], max_events=d.max_events,
+                        max_mutations=d.max_mutations, max_fixed=d.max_fixed)
+    pop.init(s["N"])
+    pop.run_philox(s["N"], G)
+    pop.check()
+    b = cg.Batch([d, desc_of(SPECS[1])])
+    b.init()
+    b.run(G)
+    assert b.info(0)["device_error"] == 0
+    assert np.array_equal(b.rows(0), pop.rows())
+    bs, st = b.stats(0, 64), pop.stats(64)
+    assert np.array_equal(bs["sfs"], st["sfs"]) and bs["mean_fitness"] == st["mean_fitness"]
+    # row capacities (512 and 16,384 slots: 8 and 256 words) decide the build, not the live widths
+    assert d.max_alleles <= 128 * 64 < desc_of(SPECS[1]).max_alleles
+
+
 def test_rows_per_item_does_not_change_results():
     G = 6
     outs = []

@@ -305,3 +305,11 @@ def test_c2_shaped_phenotype_error_stays_within_fp32_bound(capsys):
     with capsys.disabled():
         print(f"\nC2-shaped N={N} G={G}: phenotype |FP32 carried - FP64| max {worst:.3e}, mean {np.mean(means):.3e}"
               f" (|z| up to {scale:.2f}, alleles {gpu.info()['A']})")
+
+
+@pytest.mark.parametrize("q1", [True, False])
+def test_narrow_rows_many_breakpoints(q1):
+    # 512 slots (8-word rows): the narrow build of the kernel (copy rows by direct loads) and the one-pass
+    # mask build (every breakpoint's table words loaded at once), with up to 32 breakpoints a gamete and
+    # the rare longer lists on the per-table-row path; new alleles and phenotypes through the plan
+    run_parity(10, 100, 512, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.1, rho=20.0, p_neutral=0.3, q1=q1)
