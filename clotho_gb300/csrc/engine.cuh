@@ -172,10 +172,21 @@ __device__ inline U4 philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t 
     return U4{c0, c1, c2, c3};
 }
 
-// [0,1) double from 53 random bits
+// [0,1) double from 53 random bits: v * 2^-53, assembled as IEEE-754 bits with
+// integer operations (exactly the value of the FP64 conversion and scaling, which
+// would occupy GB300's narrow FP64 pipe).
 __device__ inline double u01(uint32_t hi, uint32_t lo) {
-    uint64_t v = ((((uint64_t)hi) << 32) | lo) >> 11;
-    return (double)v * 0x1.0p-53;
+    const uint64_t v = ((((uint64_t)hi) << 32) | lo) >> 11;
+    const int msb = 63 - __clzll((long long)(v | 1ull));          // highest set bit, 0..52
+    const uint64_t frac = (v << (52 - msb)) & 0x000FFFFFFFFFFFFFull;
+    const uint64_t bits = ((uint64_t)(1023 - 53 + msb) << 52) | frac;
+    return __longlong_as_double((long long)(v ? bits : 0ull));
+}
+
+// x < y for non-negative, non-NaN doubles, as an integer compare of their bit
+// patterns (IEEE-754 order); exact, and off the FP64 pipe.
+__device__ inline bool lt_nonneg(double x, double y) {
+    return (unsigned long long)__double_as_longlong(x) < (unsigned long long)__double_as_longlong(y);
 }
 
 // 1/k for the Poisson inversion (k = 1..kRecip-1); multiplying by it avoids
@@ -193,13 +204,20 @@ static inline int fill_recip_table() {
 
 // Poisson draw by sequential inversion of the CDF; e = exp(-lambda) from the
 // host.  Used only for small means (per-gamete events, per-row mutations).
+// One step of the Poisson CDF recurrence p_k = p_{k-1} lambda / k, F_k = F_{k-1} + p_k, with
+// explicitly rounded operations (never contracted into FMAs), so every copy of it -- the inversion
+// loop and the plan kernel's table -- gives the same bits.
+__device__ inline void poisson_step(double& p, double& F, double lambda, uint32_t k) {
+    p = __dmul_rn(p, __dmul_rn(lambda, k < kRecip ? c_recip[k] : 1.0 / (double)k));
+    F = __dadd_rn(F, p);
+}
+
 __device__ inline uint32_t poisson_inv(double u, double lambda, double e) {
     double p = e, F = e;
     uint32_t k = 0;
     while (u > F && k < 4096u) {
         ++k;
-        p *= lambda * (k < kRecip ? c_recip[k] : 1.0 / (double)k);
-        F += p;
+        poisson_step(p, F, lambda, k);
     }
     return k;
 }
@@ -207,10 +225,27 @@ __device__ inline uint32_t poisson_inv(double u, double lambda, double e) {
 __device__ inline uint32_t lane_id() { return threadIdx.x & 31u; }
 
 // Monotone bucket of a position in [0,1) (values outside are clamped).
+// floor(x * NB) for x in (0, 1), from the bits with integer operations: 0 for
+// x <= 0 (and subnormals), NB - 1 for x >= 1.  Monotone, which is all the
+// bucket index needs (the rank kernels and the threshold search use this one
+// function; ranks are exact within a bucket), and off the FP64 pipe.
 __device__ inline uint32_t pos_bucket(double x, uint32_t NB) {
-    const double y = x * (double)NB;
-    if (!(y > 0.0)) return 0u;
-    return y >= (double)(NB - 1u) ? NB - 1u : (uint32_t)y;
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    if ((b >> 63) || b == 0ull) return 0u;
+    const int ex = (int)((b >> 52) & 0x7FFu) - 1023;                     // x = 1.f * 2^ex
+    if (ex >= 0) return NB - 1u;
+    const uint64_t m = (b & 0x000FFFFFFFFFFFFFull) | (1ull << 52);      // 53-bit significand
+    const int sh = -ex - 1;                                              // x * 2^53 = m >> sh
+    const uint64_t v = sh >= 64 ? 0ull : (m >> sh);
+    const uint32_t k = (uint32_t)__umul64hi(v << 11, (uint64_t)NB);     // floor(v * NB / 2^53)
+    return k < NB - 1u ? k : NB - 1u;
+}
+
+// x < y for positions (doubles >= 0, -0.0 included) as an integer compare of
+// the bit patterns with the sign cleared.
+__device__ inline bool pos_lt(double x, double y) {
+    return ((unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull) <
+           ((unsigned long long)__double_as_longlong(y) & 0x7FFFFFFFFFFFFFFFull);
 }
 
 }  // namespace clotho

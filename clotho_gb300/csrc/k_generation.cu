@@ -114,7 +114,7 @@ __device__ __forceinline__ uint32_t threshold_rank(const PopDev& P, double e) {
     const uint32_t b = pos_bucket(e, P.NB);
     const uint32_t k0 = __ldg(P.boff + b), k1 = __ldg(P.boff + b + 1u);
     uint32_t r = k0;
-    for (uint32_t k = k0; k < k1; ++k) r += (__ldg(P.bpos + k) < e) ? 1u : 0u;
+    for (uint32_t k = k0; k < k1; ++k) r += pos_lt(__ldg(P.bpos + k), e) ? 1u : 0u;
     return r;
 }
 
@@ -1362,6 +1362,23 @@ void launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, W
 
 // ---------------------------------------------------------------------------
 constexpr uint32_t kPlanSmemEv = 16;  // breakpoints of a row the plan kernel ranks in shared memory
+constexpr uint32_t kPoisTab = 64;     // entries of the plan kernel's Poisson CDF table
+
+// poisson_inv(u, rho, exp(-rho)) from the table cdf[k] = F_k of the same recurrence: the first k with
+// u <= F_k (u and F_k are non-negative, so their bit patterns compare as integers); past the table the
+// recurrence goes on from (p, F) at k = kPoisTab - 1, as poisson_inv would.
+__device__ __forceinline__ uint32_t poisson_tab(double u, const double* cdf, double plast, double lambda) {
+    uint32_t k = 0;
+    while (k < kPoisTab && lt_nonneg(cdf[k], u)) ++k;
+    if (k < kPoisTab) return k;
+    k = kPoisTab - 1u;
+    double pk = plast, F = cdf[k];
+    while (u > F && k < 4096u) {
+        ++k;
+        poisson_step(pk, F, lambda, k);
+    }
+    return k;
+}
 
 // Processing order of the offspring rows (parent-major): rows are sorted by
 // parent individual, so rows reading the same parent strands run side by side
@@ -1417,9 +1434,24 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
     // a thread's thresholds (up to kPlanSmemEv) stay in shared memory while they are ranked
     // against each other; longer lists use their global slots
     __shared__ uint32_t s_cr[256][kPlanSmemEv + 1];
+    // the population's Poisson(rho) CDF, built by the same FP64 recurrence as poisson_inv and
+    // searched with integer compares, so a breakpoint count costs no FP64 work
+    __shared__ double s_cdf[kPoisTab];
+    __shared__ double s_plast;
     for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         if (!P.plan_row) continue;
+        __syncthreads();  // the previous population's table is no longer read
+        if (threadIdx.x == 0) {
+            double pk = P.exp_neg_rho, F = pk;
+            s_cdf[0] = F;
+            for (uint32_t k = 1; k < kPoisTab; ++k) {
+                poisson_step(pk, F, P.rho, k);
+                s_cdf[k] = F;
+            }
+            s_plast = pk;
+        }
+        __syncthreads();
         const DevStatus st = *P.st;
         const uint32_t S = 2u * st.N, A = st.A, Se = (S + 1u) >> 1;
         const bool philox = P.mode == kModePhilox;
@@ -1441,8 +1473,8 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
                 }
                 if (philox) {
                     const U4 x = philox4x32(g, 0u, st.gen, kStreamGamete, P.seed);
-                    E = (q1 && (g & 1u)) ? 0u : poisson_inv(u01(x.x, x.y), P.rho, P.exp_neg_rho);
-                    swap = u01(x.z, x.w) < P.bias;
+                    E = (q1 && (g & 1u)) ? 0u : poisson_tab(u01(x.x, x.y), s_cdf, s_plast, P.rho);
+                    swap = lt_nonneg(u01(x.z, x.w), P.bias);
                     if (E > kMaxEvDevice) {
                         atomicOr(&P.st->err, kErrEvents);
                         E = kMaxEvDevice;

@@ -348,10 +348,10 @@ __global__ void k_select_philox(const PopDev* __restrict__ pops, uint32_t npops)
                     if (id >= Np) id = Np - 1u;
                 } else {
                     const double target = u[h] * total;
-                    uint32_t lo = 0, hi = Np;  // first i with cdf[i] > target
+                    uint32_t lo = 0, hi = Np;  // first i with cdf[i] > target (both >= +0: integer compares)
                     while (lo < hi) {
                         const uint32_t mid = (lo + hi) >> 1;
-                        if (P.cdf[mid] > target) hi = mid; else lo = mid + 1u;
+                        if (lt_nonneg(target, P.cdf[mid])) hi = mid; else lo = mid + 1u;
                     }
                     id = lo >= Np ? Np - 1u : lo;
                 }
