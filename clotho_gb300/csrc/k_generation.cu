@@ -833,7 +833,9 @@ __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st
                 }
             }
         } else {
-            // corrections: toggle the slots whose rank lies between threshold and table row
+            // corrections: toggle the slots whose rank lies between threshold and table row (the table-row
+            // offsets of the first 32 breakpoints are fetched with their correction ranks)
+            const uint32_t go0 = lane < E ? __ldg(P.plan_go + base + lane) : 0u;
             for (uint32_t k0 = 0; k0 < E; k0 += 32u) {
                 const uint32_t my_cr = (k0 + lane < E) ? __ldg(P.plan_cr + base + k0 + lane) : 0u;
                 const uint32_t ke = min(32u, E - k0);
@@ -850,7 +852,7 @@ __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st
             // XOR of the events' table rows, kTableInflight 16-byte loads per lane in flight
             ulonglong2* m2 = reinterpret_cast<ulonglong2*>(mask);
             for (uint32_t k0 = 0; k0 < E; k0 += 32u) {
-                const uint32_t my_go = (k0 + lane < E) ? __ldg(P.plan_go + base + k0 + lane) : 0u;
+                const uint32_t my_go = k0 == 0 ? go0 : (k0 + lane < E) ? __ldg(P.plan_go + base + k0 + lane) : 0u;
                 const uint32_t ke = min(32u, E - k0);
                 for (uint32_t k = 0; k < ke; ++k) {
                     const uint64_t* tk = suf + __shfl_sync(0xffffffffu, my_go, k);
