@@ -124,3 +124,47 @@ def test_admission_waits_for_memory():
     fin = sorted(srv.finished, key=lambda j: j.admitted)
     for a, b in zip(fin, fin[1:]):
         assert b.admitted >= a.done - 1e-6
+
+
+def wf_sojourn(n):
+    """Expected generations an allele born in one of n sequences spends at each count 1..n-1 (count at
+    birth included) under neutral Wright-Fisher resampling, counts i -> Binomial(n, i/n): row 1 of
+    (I - Q)^-1 over the transient counts."""
+    from math import lgamma, log, exp
+    i = np.arange(1, n)
+    lc = np.array([lgamma(n + 1) - lgamma(j + 1) - lgamma(n - j + 1) for j in range(1, n)])
+    Q = np.empty((n - 1, n - 1))
+    for a in range(1, n):
+        p = a / n
+        Q[a - 1] = np.exp(lc + i * log(p) + (n - i) * log(1.0 - p))
+    e1 = np.zeros(n - 1)
+    e1[0] = 1.0
+    return np.linalg.solve((np.eye(n - 1) - Q).T, e1)
+
+
+def test_device_draws_match_neutral_theory():
+    # Device-drawn (Philox) generations have no bit parity with the reference's Boost stream, so they are
+    # checked against the neutral Wright-Fisher expectation with infinite sites: 2N mu new alleles a
+    # generation, each resampled Binomial(2N, i/2N) (every sequence copies a random parent strand at a
+    # neutral site); sites carried by i sequences = 2N mu x the expected generations at count i.  (The
+    # diffusion limit theta / i, theta = 4 N mu, undercounts singletons by about 13% at 2N = 400.)
+    # 64 replicates in one batch, 8N generations of burn-in from an empty start, then 20 samples N/4
+    # generations apart.
+    N, mu, rho, R = 200, 0.05, 0.5, 64
+    b = cg.Batch([cg.make_desc(N, 8192, 1, mu=mu, rho=rho, p_neutral=1.0, fitness="constant", seed=1000 + r)
+                  for r in range(R)])
+    b.init()
+    b.run(8 * N)
+    seg, sfs = [], []
+    for _ in range(20):
+        b.run(N // 4)
+        for i in range(R):
+            st = b.stats(i, 2 * N + 1)
+            assert b.info(i)["device_error"] == 0
+            seg.append(st["segregating"])
+            sfs.append(st["sfs"][1:4].astype(np.float64))
+    xi_expect = 2 * N * mu * wf_sojourn(2 * N)
+    assert abs(np.mean(seg) / xi_expect.sum() - 1.0) < 0.06, (np.mean(seg), xi_expect.sum())
+    xi = np.mean(sfs, axis=0)                      # sites carried by 1, 2, 3 sequences
+    assert np.all(np.abs(xi / xi_expect[:3] - 1.0) < 0.05), (xi, xi_expect[:3])
+    b.close()
