@@ -313,3 +313,14 @@ def test_narrow_rows_many_breakpoints(q1):
     # mask build (every breakpoint's table words loaded at once), with up to 32 breakpoints a gamete and
     # the rare longer lists on the per-table-row path; new alleles and phenotypes through the plan
     run_parity(10, 100, 512, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.1, rho=20.0, p_neutral=0.3, q1=q1)
+
+
+@pytest.mark.parametrize("A_cap", [8192, 16384])
+def test_long_run_stays_bit_exact(A_cap):
+    # hundreds of generations: alleles fix and are cleared, slots are recycled through the free list, the
+    # fixed table grows and the row width changes; every generation is compared (8,192 slots run the
+    # narrow build of the generation kernel, 16,384 the wide one)
+    orc, gpu = run_parity(1000, 150, A_cap, T=2, fitness="gaussian_vs", fit_param=8.0, mu=0.1, rho=2.0,
+                          p_neutral=0.5)
+    i = orc.info()
+    assert i["fixed_total"] > 0 and i["generation"] > 1000
