@@ -167,6 +167,13 @@ int hdr_copy(clotho_ctx* ctx, uint32_t slot, uint32_t* dst, uint32_t n, cudaStre
     return 0;
 }
 
+// Scratch device memory for a call, from the context's stream-ordered pool (freed with cudaFreeAsync on
+// the context's stream): no device-wide synchronisation, unlike cudaMalloc / cudaFree.
+template <class T>
+cudaError_t pool_alloc(clotho_ctx* ctx, T** p, size_t bytes) {
+    return cudaMallocFromPoolAsync(reinterpret_cast<void**>(p), bytes, ctx->pool, ctx->stream);
+}
+
 int check_launch(clotho_ctx* ctx, const char* what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(ctx, CLOTHO_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
@@ -655,12 +662,12 @@ int clotho_seed_population(clotho_ctx* ctx, uint32_t N, uint32_t A, const double
         int rc0 = start_population(ctx, N, A, pos, eff);
         if (rc0) return rc0;
         uint32_t* d_thr = nullptr;
-        CK(cudaMalloc(&d_thr, std::max<size_t>(4, (size_t)A * 4)));
+        CK(pool_alloc(ctx, &d_thr, std::max<size_t>(4, (size_t)A * 4)));
         if (A) CK(cudaMemcpyAsync(d_thr, thr, (size_t)A * 4, cudaMemcpyHostToDevice, ctx->stream));
         launch_seed_rows(cfg(ctx), ctx->d_pops[0], 0, d_thr, seed, A);
         ctx->launches += 1;
+        CK(cudaFreeAsync(d_thr, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
-        cudaFree(d_thr);
         return finish_start(ctx);
     }
 }
@@ -1082,15 +1089,16 @@ static int stats_of(clotho_ctx* ctx, uint32_t idx, clotho_stats* out, uint32_t* 
     const PopDev& D = p->dev[0];
     const uint32_t A = s.A, S = 2 * s.N;
     std::vector<uint32_t> counts(std::max<size_t>(1, (size_t)s.W * 64), 0);
+    // scratch column counts from the context's pool: stream-ordered, no device-wide synchronisation
     uint32_t* d_counts = nullptr;
-    CK(cudaMalloc(&d_counts, counts.size() * 4));
+    CK(pool_alloc(ctx, &d_counts, counts.size() * 4));
     CK(cudaMemsetAsync(d_counts, 0, counts.size() * 4, ctx->stream));
     if (S && s.W) launch_stats(cfg(ctx), ctx->d_pops[0], idx, d_counts, s.W);
     CK(cudaMemcpyAsync(counts.data(), d_counts, counts.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaFreeAsync(d_counts, ctx->stream));
     std::vector<double> zi((size_t)s.N * 4);
     if (s.N) CK(cudaMemcpyAsync(zi.data(), D.zi, (size_t)s.N * 32, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    cudaFree(d_counts);
     ctx->launches += 1;
     *out = clotho_stats{};
     if (sfs)
@@ -1129,14 +1137,14 @@ static int margins_of(clotho_ctx* ctx, uint32_t idx, uint32_t* col, uint32_t* ro
     const uint32_t S = 2 * s.N;
     const size_t ncol = std::max<size_t>(1, (size_t)s.W * 64), nrow = std::max<uint32_t>(1, S);
     uint32_t* d = nullptr;
-    CK(cudaMalloc(&d, (ncol + nrow) * 4));
+    CK(pool_alloc(ctx, &d, (ncol + nrow) * 4));
     CK(cudaMemsetAsync(d, 0, (ncol + nrow) * 4, ctx->stream));
     if (col && S && s.W) launch_stats(cfg(ctx), ctx->d_pops[0], idx, d, s.W);
     if (row && S) launch_row_counts(cfg(ctx), ctx->d_pops[0], idx, d + ncol, S);
     if (col && s.A) CK(cudaMemcpyAsync(col, d, (size_t)s.A * 4, cudaMemcpyDeviceToHost, ctx->stream));
     if (row && S) CK(cudaMemcpyAsync(row, d + ncol, (size_t)S * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaFreeAsync(d, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    cudaFree(d);
     ctx->launches += (col ? 1 : 0) + (row ? 1 : 0);
     return check_launch(ctx, "margins");
 }
@@ -1167,9 +1175,9 @@ static int pairwise_of(clotho_ctx* ctx, uint32_t idx, const uint32_t* sample, ui
     uint32_t* d_smp = nullptr;
     uint32_t* d_dist = nullptr;
     PairwiseOut* d_out = nullptr;
-    CK(cudaMalloc(&d_smp, (size_t)n * 4));
-    CK(cudaMalloc(&d_out, sizeof(PairwiseOut)));
-    if (dist) CK(cudaMalloc(&d_dist, pairs * 4));
+    CK(pool_alloc(ctx, &d_smp, (size_t)n * 4));
+    CK(pool_alloc(ctx, &d_out, sizeof(PairwiseOut)));
+    if (dist) CK(pool_alloc(ctx, &d_dist, pairs * 4));
     PairwiseOut h{};
     h.min = 0xffffffffu;
     CK(cudaMemcpyAsync(d_smp, smp.data(), (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
@@ -1178,10 +1186,10 @@ static int pairwise_of(clotho_ctx* ctx, uint32_t idx, const uint32_t* sample, ui
     rc = check_launch(ctx, "pairwise difference");
     CK(cudaMemcpyAsync(&h, d_out, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
     if (dist) CK(cudaMemcpyAsync(dist, d_dist, pairs * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaFreeAsync(d_smp, ctx->stream));
+    CK(cudaFreeAsync(d_out, ctx->stream));
+    if (d_dist) CK(cudaFreeAsync(d_dist, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    cudaFree(d_smp);
-    cudaFree(d_out);
-    if (d_dist) cudaFree(d_dist);
     ctx->launches += 1;
     if (rc) return rc;
     out->count = h.count;
@@ -1577,8 +1585,8 @@ int clotho_run_philox_schedule(clotho_ctx* ctx, const uint32_t* N, uint32_t G) {
         return 0;
     }
     uint32_t* d_sched = nullptr;
-    CK(cudaMalloc(&d_sched, hdr.size() * 4));
-    CK(cudaMemcpy(d_sched, hdr.data(), hdr.size() * 4, cudaMemcpyHostToDevice));
+    CK(pool_alloc(ctx, &d_sched, hdr.size() * 4));
+    CK(cudaMemcpyAsync(d_sched, hdr.data(), hdr.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     // the first generation runs eagerly (it may need the parent reduction)
     CK(cudaMemcpyAsync(ctx->d_hdr[2], d_sched, 8ull * n, cudaMemcpyDeviceToDevice, ctx->stream));
     enqueue_fused_step(ctx, 2, true);
@@ -1608,8 +1616,8 @@ int clotho_run_philox_schedule(clotho_ctx* ctx, const uint32_t* N, uint32_t G) {
             ctx->launches += ctx->graph_launches;
         }
     }
+    CK(cudaFreeAsync(d_sched, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    cudaFree(d_sched);
     if (rc) return rc;
     for (uint32_t i = 0; i < n; ++i) ctx->pops[i]->hostN = N[(size_t)(G - 1) * n + i];
     return 0;
