@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-gens", type=int, default=4)
     p.add_argument("--kernel-only", action="store_true", help="seed + eager generations only (ncu runs)")
+    p.add_argument("--batch-kernels", action="store_true",
+                   help="the batched workload's 256 populations, warmup + steps eager generations only (ncu runs)")
     p.add_argument("--phase-clocks", action="store_true",
                    help="print the generation kernel's per-phase cycle breakdown (profiling build) and exit")
     p.add_argument("--no-batched", action="store_true", help="skip the batched and serving measurements")
@@ -329,6 +331,22 @@ def phase_breakdown(pop, N, warmup, steps):
             "raw": ph}
 
 
+def batch_kernels(cg, warmup, steps):
+    """The batched measurement's 256 populations (the same job list and tuned-size items), stepped eagerly
+    one generation at a time, for launch lists of a batched step."""
+    from clotho_gb300 import serving
+    jobs = serving.synthetic_jobs(256, rate=1e9, seed=11, N_range=(1_000, 20_000), G_range=(100, 100))
+    b = cg.Batch([j.desc() for j in jobs])
+    b.init()
+    b.set_rows_per_item(1024)
+    for _ in range(warmup + steps):
+        b.step()
+    b.sync()
+    errs = sum(b.info(i)["device_error"] != 0 for i in range(len(jobs)))
+    return {"batch_kernels": True, "populations": len(jobs), "generations": warmup + steps, "device_errors": errs,
+            "max_row_words": max(b.info(i)["W"] for i in range(len(jobs)))}
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -342,6 +360,10 @@ def main():
     import numpy as np
     import clotho_gb300 as cg
     from clotho_gb300.workloads import LARGE_N, seeded_start
+
+    if args.batch_kernels:
+        print(json.dumps(batch_kernels(cg, args.warmup, args.steps)))
+        return
 
     w = LARGE_N
     N = args.n or w.N
