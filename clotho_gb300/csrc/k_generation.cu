@@ -1338,17 +1338,21 @@ void launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, W
         gacc ? 0 : (3ull + (suf ? kWarps : 0u)) * maxW * sizeof(uint64_t) + (suf ? kWarps * sizeof(WarpSmem) : 0);
     // profile 2: the suffix-table kernel's build with phase clocks; rows of at most
     // 128 words: its narrow build (copy rows by direct loads)
-    static size_t configured[4] = {0, 0, 0, 0};
+    static size_t configured[5] = {0, 0, 0, 0, 0};
     const bool narrow = maxW <= 64u * kDirectCopyChunks;
-    const int si = suf ? (profile == 2 ? 2 : narrow ? 3 : 1) : 0;
-    const void* fns[4] = {(const void*)k_generation<false, false, false>, (const void*)k_generation<true, false, false>,
-                          (const void*)k_generation<true, true, false>, (const void*)k_generation<true, false, true>};
+    const int si = suf ? (profile == 2 ? (narrow ? 4 : 2) : narrow ? 3 : 1) : 0;
+    const void* fns[5] = {(const void*)k_generation<false, false, false>, (const void*)k_generation<true, false, false>,
+                          (const void*)k_generation<true, true, false>, (const void*)k_generation<true, false, true>,
+                          (const void*)k_generation<true, true, true>};
     // static shared memory is above 48 KB on its own, so the opt-in attribute is always needed
     if (smem > configured[si] || configured[si] == 0) {
         cudaFuncSetAttribute(fns[si], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured[si] = smem > 0 ? smem : 1;
     }
-    if (si == 3)
+    if (si == 4)
+        k_generation<true, true, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
+                                                                                  maxW, 0u);
+    else if (si == 3)
         k_generation<true, false, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
                                                                                    maxW, 0u);
     else if (si == 2)
