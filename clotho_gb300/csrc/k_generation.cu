@@ -1288,11 +1288,29 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
         const uint32_t r0 = (item - ctl->item_base[p]) * rpi;
         const uint32_t r1 = min(S, r0 + rpi);
         const uint32_t Se = (S + 1u) >> 1;
+        // narrow build: each warp claims its next row one ahead and fetches that row's plan entries into L1
+        // behind the current row (narrow rows are bound by their chains of dependent loads)
+        uint32_t kc = 0;
+        if (NARROW && lane == 0) kc = atomicAdd(&s_next, 1u);
         for (;;) {
             uint32_t k = 0;
-            if (lane == 0) k = atomicAdd(&s_next, 1u);
+            if (NARROW) {
+                k = kc;
+                if (lane == 0) kc = atomicAdd(&s_next, 1u);
+            } else if (lane == 0) {
+                k = atomicAdd(&s_next, 1u);
+            }
             const uint32_t v = r0 + __shfl_sync(0xffffffffu, k, 0);
             if (v >= r1) break;
+            if (NARROW && SUF) {
+                const uint32_t vn = r0 + __shfl_sync(0xffffffffu, kc, 0);
+                if (vn < r1) {
+                    const void* a = lane == 0   ? (const void*)(P.plan_row + vn)
+                                    : lane == 1 ? (const void*)(P.plan_mut + vn)
+                                                : (const void*)(P.plan_z + (size_t)vn * 4u);
+                    if (lane < 3) asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
+                }
+            }
             // interval classifier: even gametes first, then odd ones (the second
             // gamete of a mate pair is a copy row under the reference's crossover
             // rule), so a CTA runs one kind of row at a time; the suffix-table
