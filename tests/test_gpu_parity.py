@@ -324,3 +324,24 @@ def test_long_run_stays_bit_exact(A_cap):
                           p_neutral=0.5)
     i = orc.info()
     assert i["fixed_total"] > 0 and i["generation"] > 1000
+
+
+@pytest.mark.parametrize("q1", [True, False])
+def test_seeded_wide_rows_bench_shape(q1):
+    # the N=1e6 bench workload's shape at small N: 50,000 seeded alleles in 65,536 slots (about 780-word rows,
+    # the wide build: bulk-copied copy rows, masks from one suffix-table row at a time, large effect gathers
+    # in both directions), four traits, rho = 5, the reference gaussian metric
+    rng = np.random.default_rng(17)
+    N, A, T = 150, 50_000, 4
+    pos = rng.random(A)
+    eff = rng.standard_normal(A * T).astype(np.float32)
+    k = np.minimum(np.floor(1.0 / rng.random(A)), 2 * N - 1)          # carrier counts ~ 1/i
+    thr = np.minimum(k / (2 * N) * 2.0 ** 32, 2.0 ** 32 - 1).astype(np.uint32)
+    orc, gpu = make_pair(N, 65_536, T=T, fitness="gaussian", mu=0.01, rho=5.0, p_neutral=0.0, q1=q1)
+    orc.seed_population(N, pos, eff, thr, 7)
+    gpu.seed_population(N, pos, eff, thr, 7)
+    compare_state(orc, gpu, -1, kind="gaussian", mu=0.01)
+    for g in range(6):
+        gpu.simulate(orc.step_record(N))
+        compare_state(orc, gpu, g, kind="gaussian", mu=0.01)
+    assert gpu.info()["W"] > 512
