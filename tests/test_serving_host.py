@@ -2,15 +2,16 @@
 batch: admission under the byte budget and the slot limit, retirement by
 index from the highest down (every job gets its own population's result),
 chunked stepping that never runs a job past its generation count, and the
-error for a job larger than the whole budget.  The footprint of each job comes
-from the real library (`clotho_footprint_for` needs no GPU)."""
+error for a job larger than the whole budget; and the autotuner's choice of
+rows per item and its cache.  The footprint of each job comes from the real
+library (`clotho_footprint_for` needs no GPU)."""
 import itertools
 
 import numpy as np
 import pytest
 
 import clotho_gb300 as cg
-from clotho_gb300 import serving
+from clotho_gb300 import autotune, serving
 
 
 class FakeBatch:
@@ -116,3 +117,42 @@ def test_summary_percentiles():
         j.arrival, j.done, j.result = 0.0, float(i + 1), {"device_error": 1 if i == 4 else 0}
     s = serving.summarize(jobs, 5.0)
     assert s["jobs"] == 5 and s["jobs_per_s"] == 1.0 and s["p50_s"] == 3.0 and s["errors"] == 1
+
+
+class TimedBatch:
+    """Stand-in with a per-grain step cost (ms), for the autotuner."""
+
+    def __init__(self, cost, N=(1000, 2000), A=4096):
+        self.cost, self.N = cost, list(N)
+        self.descs = [cg.make_desc(n, A) for n in N]
+        self.rpi, self.steps, self.ms = None, 0, 0.0
+
+    def set_rows_per_item(self, r):
+        self.rpi = r
+
+    def step(self):
+        self.steps += 1
+        self.ms += self.cost[self.rpi]
+
+    def sync(self):
+        pass
+
+    def timer_begin(self):
+        self.ms = 0.0
+
+    def timer_end(self):
+        return self.ms
+
+
+def test_autotuner_keeps_the_fastest_grain_and_caches_it(tmp_path):
+    cost = {64: 5.0, 128: 3.0, 256: 1.5, 512: 2.0, 1024: 4.0}
+    b = TimedBatch(cost)
+    path = str(tmp_path / "sub" / "tune.json")
+    assert autotune.tune(b, gens_per_trial=2, cache_path=path) == 256 and b.rpi == 256
+    assert b.steps == 3 * len(autotune.CANDIDATES)
+    b2 = TimedBatch({k: 1.0 for k in cost})  # a cache hit runs nothing
+    assert autotune.tune(b2, cache_path=path) == 256 and b2.rpi == 256 and b2.steps == 0
+    # another bucket (wider rows) is tuned afresh
+    b3 = TimedBatch({64: 1.0, 128: 2.0, 256: 3.0, 512: 4.0, 1024: 5.0}, A=1 << 20)
+    assert autotune.bucket(b3) != autotune.bucket(b)
+    assert autotune.tune(b3, cache_path=path) == 64
