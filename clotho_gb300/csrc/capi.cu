@@ -400,9 +400,9 @@ void enqueue_fused_step(clotho_ctx* ctx, uint32_t set, bool philox) {
     launch_individuals(L, pops, n);
     launch_cdf(L, pops, n, ctx->maxN);
     launch_end(L, pops, n);
-    // begin, mutation counts or CSR (4 or 5), finalize, resolve, ranks (6, + suffix table), selection (device
+    // begin, mutation counts or CSR (4 or 6), finalize, resolve, ranks (6, + suffix table), selection (device
     // draws), individuals, 3-kernel prefix sum, end; launch_gen and ensure_parent_acc count their own
-    ctx->launches += 19u + (ctx->maxA <= kSufMaxSlots ? 1u : 0u);
+    ctx->launches += 19u + (philox ? 0u : 1u) + (ctx->maxA <= kSufMaxSlots ? 1u : 0u);
     for (PopHost* p : ctx->pops) p->acc_valid = true;
 }
 

@@ -200,8 +200,10 @@ void launch_uscan_order(const LaunchCfg& L, const PopDev* pops, uint32_t npops, 
 }
 
 // ---------------------------------------------------------------------------
-// Tape mutations grouped by target row (device counting sort; the in-row order
-// does not affect any result).
+// Tape mutations grouped by target row (device counting sort, then each row's
+// list in ascending mutation index: the list order is the order in which the
+// new alleles' FP32 effects enter the row's carried phenotype, so it must not
+// depend on the order of the scatter's atomics).
 __global__ void k_csr_count(const PopDev* __restrict__ pops, uint32_t npops) {
     for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
@@ -226,11 +228,56 @@ __global__ void k_csr_scatter(const PopDev* __restrict__ pops, uint32_t npops) {
         }
     }
 }
+// Ascending order of a[0..n): insertion sort for short lists, heapsort beyond
+// (a tape may send many mutations to one row).
+__device__ void sort_ascending(uint32_t* a, uint32_t n) {
+    if (n <= 16u) {
+        for (uint32_t i = 1; i < n; ++i) {
+            const uint32_t x = a[i];
+            uint32_t j = i;
+            for (; j > 0 && a[j - 1] > x; --j) a[j] = a[j - 1];
+            a[j] = x;
+        }
+        return;
+    }
+    auto sift = [a](uint32_t r, uint32_t end) {
+        const uint32_t x = a[r];
+        for (uint32_t c = 2u * r + 1u; c < end; c = 2u * r + 1u) {
+            if (c + 1u < end && a[c + 1u] > a[c]) ++c;
+            if (a[c] <= x) break;
+            a[r] = a[c];
+            r = c;
+        }
+        a[r] = x;
+    };
+    for (uint32_t r = n / 2u; r-- > 0;) sift(r, n);
+    for (uint32_t end = n - 1u; end > 0; --end) {
+        const uint32_t x = a[0];
+        a[0] = a[end];
+        a[end] = x;
+        sift(0, end);
+    }
+}
+// One thread per list position; the thread at a row's first position sorts the
+// row's list.  Ownership is decided by position, which never moves, and every
+// entry of a row's segment names that row, so no other thread acts on it.
+__global__ void k_csr_order(const PopDev* __restrict__ pops, uint32_t npops) {
+    for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
+        const PopDev& P = pops[p];
+        const uint32_t S = 2u * P.st->N, listed = P.row_off[S];
+        for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < listed; t += gridDim.x * blockDim.x) {
+            const uint32_t s = P.mut_seq[P.row_mut[t]];
+            const uint32_t off = P.row_off[s], n = P.row_off[s + 1u] - off;
+            if (t == off && n >= 2u) sort_ascending(P.row_mut + off, n);
+        }
+    }
+}
 void launch_mut_csr_tape(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
     const dim3 g = pop_grid(npops, L.num_sms * 2u, L.num_sms, 2);
     k_csr_count<<<g, 256, 0, L.stream>>>(pops, npops);
     launch_uscan(L, pops, npops, maxS, 0, 0);
     k_csr_scatter<<<g, 256, 0, L.stream>>>(pops, npops);
+    k_csr_order<<<g, 256, 0, L.stream>>>(pops, npops);
 }
 
 // Device-drawn mutation counts: Poisson(mu) per offspring row.  The sum over

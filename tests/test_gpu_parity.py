@@ -345,3 +345,65 @@ def test_seeded_wide_rows_bench_shape(q1):
         gpu.simulate(orc.step_record(N))
         compare_state(orc, gpu, g, kind="gaussian", mu=0.01)
     assert gpu.info()["W"] > 512
+
+
+def test_tape_replay_is_deterministic():
+    # the same tapes replayed into two populations give bit-identical phenotypes and fitness, not only
+    # genomes: a row with several new alleles adds their FP32 effects in mutation-index order, whatever
+    # order the device's counting sort scattered them in (mu = 1.5 puts two or more new alleles on
+    # about half of the rows; a few rows get more than 16, the heapsort branch)
+    N, G = 300, 25
+    orc, a = make_pair(N, 1 << 15, T=4, fitness="gaussian", mu=1.5, rho=1.0, p_neutral=0.0)
+    _, b = make_pair(N, 1 << 15, T=4, fitness="gaussian", mu=1.5, rho=1.0, p_neutral=0.0)
+    orc.init(N)
+    a.init(N)
+    b.init(N)
+    multi = 0
+    for g in range(G):
+        tape = orc.step_record(N)
+        multi += int((np.bincount(tape.mut_seq, minlength=2 * N) >= 2).sum())
+        a.simulate(tape)
+        b.simulate(tape)
+        assert np.array_equal(a.phenotypes(), b.phenotypes()), f"gen {g}"
+        assert np.array_equal(a.fitness(), b.fitness()), f"gen {g}"
+    assert np.array_equal(a.rows(), b.rows())
+    assert np.array_equal(orc.rows(), a.rows())
+    assert a.info()["device_error"] == 0
+    assert multi > G * N // 2
+
+
+def hand_tape(rng, N, T, heavy):
+    """A tape with uniform parents, Poisson(0.5) sorted breakpoints per gamete and, besides one new
+    allele on every fourth row, `heavy[row]` new alleles on the given rows, all in shuffled order."""
+    S = 2 * N
+    E = rng.poisson(0.5, S)
+    ev_off = np.concatenate([[0], np.cumsum(E)]).astype(np.uint32)
+    ev_pos = np.concatenate([np.sort(rng.random(e)) for e in E] + [np.zeros(0)])
+    seq = np.concatenate([np.arange(0, S, 4)] + [np.full(n, r) for r, n in heavy.items()])
+    seq = rng.permutation(seq).astype(np.uint32)
+    M = len(seq)
+    return oracle.Tape(N, M, rng.integers(0, N, S), rng.integers(0, 2, S), ev_off, ev_pos, seq, rng.random(M),
+                       rng.standard_normal(M * T).astype(np.float32))
+
+
+def test_tape_rows_with_many_new_alleles_sort_their_lists():
+    # hand-made tapes sending 40 new alleles to one row and 17 to another (past the insertion-sort bound,
+    # so the heapsort branch orders them) and 3 to a third, in shuffled order: genomes match the oracle
+    # bit for bit, phenotypes stay within the FP32 bound, and two replays agree bit for bit
+    N, T = 64, 2
+    rng = np.random.default_rng(5)
+    orc, a = make_pair(N, 4096, T=T, fitness="constant", mu=0.01, rho=0.5, p_neutral=0.0)
+    _, b = make_pair(N, 4096, T=T, fitness="constant", mu=0.01, rho=0.5, p_neutral=0.0)
+    orc.init(N)
+    a.init(N)
+    b.init(N)
+    for g in range(4):
+        tape = hand_tape(rng, N, T, {5: 40, 90: 17, 33: 3})
+        orc.step_tape(tape)
+        a.simulate(tape)
+        b.simulate(tape)
+        assert np.array_equal(orc.rows(), a.rows()), f"gen {g}"
+        assert np.array_equal(a.phenotypes(), b.phenotypes()), f"gen {g}"
+        err = np.abs(orc.phenotypes() - a.phenotypes())
+        assert np.all(err <= pheno_bound(a.rows(), a.alleles()[2], g + 1)), f"gen {g}"
+    assert a.info()["device_error"] == 0
