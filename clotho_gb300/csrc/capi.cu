@@ -435,7 +435,8 @@ int clotho_create(const clotho_desc* desc, clotho_ctx** out) {
     }
     if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
-        delete ctx;
+        cudaGetLastError();
+        clotho_destroy(ctx);  // releases whichever stream was made
         return CLOTHO_E_CUDA;
     }
     ctx->stream = ctx->own_stream;
@@ -450,25 +451,40 @@ int clotho_create(const clotho_desc* desc, clotho_ctx** out) {
             clotho_destroy(ctx);
             return CLOTHO_E_CUDA;
         }
-        uint64_t keep = ~0ull;  // freed blocks stay in the pool until the context ends
-        cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        // freed blocks stay in the pool until the context ends; if the attribute is refused, the pool
+        // returns memory at each synchronization instead, which is slower, not wrong
+        uint64_t keep = ~0ull;
+        if (cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess)
+            cudaGetLastError();
     }
-    for (int i = 0; i < 2; ++i) {
-        cudaEventCreateWithFlags(&ctx->copy_done[i], cudaEventDisableTiming);
-        cudaEventCreateWithFlags(&ctx->kern_done[i], cudaEventDisableTiming);
-        cudaEventRecord(ctx->kern_done[i], ctx->stream);
+    {
+        bool ok = true;
+        for (int i = 0; i < 2; ++i) {
+            ok = ok && cudaEventCreateWithFlags(&ctx->copy_done[i], cudaEventDisableTiming) == cudaSuccess;
+            ok = ok && cudaEventCreateWithFlags(&ctx->kern_done[i], cudaEventDisableTiming) == cudaSuccess;
+            ok = ok && cudaEventRecord(ctx->kern_done[i], ctx->stream) == cudaSuccess;
+        }
+        ok = ok && cudaEventCreate(&ctx->t0) == cudaSuccess && cudaEventCreate(&ctx->t1) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();
+            clotho_destroy(ctx);
+            return CLOTHO_E_CUDA;
+        }
     }
-    cudaEventCreate(&ctx->t0);
-    cudaEventCreate(&ctx->t1);
     if (cudaMalloc(&ctx->d_ctl, sizeof(WorkCtl)) != cudaSuccess) {
+        cudaGetLastError();
         clotho_destroy(ctx);
         return CLOTHO_E_NOMEM;
     }
-    cudaMemsetAsync(ctx->d_ctl, 0, sizeof(WorkCtl), ctx->stream);
     {
         const uint32_t rpi = kRowsPerItem;
-        cudaMemcpyAsync(&ctx->d_ctl->rows_per_item, &rpi, 4, cudaMemcpyHostToDevice, ctx->stream);
-        cudaStreamSynchronize(ctx->stream);
+        if (cudaMemsetAsync(ctx->d_ctl, 0, sizeof(WorkCtl), ctx->stream) != cudaSuccess ||
+            cudaMemcpyAsync(&ctx->d_ctl->rows_per_item, &rpi, 4, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+            cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+            cudaGetLastError();
+            clotho_destroy(ctx);
+            return CLOTHO_E_CUDA;
+        }
     }
     PopHost* p = nullptr;
     int rc = alloc_pop(ctx, *desc, &p);
