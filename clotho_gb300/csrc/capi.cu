@@ -298,7 +298,11 @@ void prof_begin(clotho_ctx* ctx) {
     if (ctx->prof_used + 2 > ctx->prof_ev.size()) {
         for (int i = 0; i < 64; ++i) {
             cudaEvent_t e;
-            cudaEventCreate(&e);
+            if (cudaEventCreate(&e) != cudaSuccess) {  // out of events: stop timing, keep running
+                cudaGetLastError();
+                ctx->profiling = false;
+                return;
+            }
             ctx->prof_ev.push_back(e);
         }
     }
