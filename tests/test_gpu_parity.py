@@ -407,3 +407,24 @@ def test_tape_rows_with_many_new_alleles_sort_their_lists():
         err = np.abs(orc.phenotypes() - a.phenotypes())
         assert np.all(err <= pheno_bound(a.rows(), a.alleles()[2], g + 1)), f"gen {g}"
     assert a.info()["device_error"] == 0
+
+
+@pytest.mark.parametrize("q1", [True, False])
+def test_population_size_changing_every_generation(q1):
+    # a growth model's sizes through the tape call: the population grows, shrinks to one individual and
+    # regrows (row counts, parent ranges and fitness tables change every generation; after the bottleneck
+    # almost every allele is lost and the new ones reuse the slots); bit-exact against the oracle throughout
+    sizes = [150, 220, 90, 90, 300, 40, 1, 2, 60, 200, 299, 17]
+    orc, gpu = make_pair(300, 4096, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.3, rho=1.0, p_neutral=0.3,
+                         q1=q1)
+    orc.init(sizes[0])
+    gpu.init(sizes[0])
+    lost, alleles = 0, 1
+    for g, N in enumerate(sizes):
+        gpu.simulate(orc.step_record(N))
+        compare_state(orc, gpu, g, kind="gaussian_vs", fit_param=4.0)
+        info = gpu.info()
+        assert info["N"] == N
+        if N == 2:  # the generation after the single-individual one
+            lost, alleles = info["lost_count"], info["A"]
+    assert lost > 0.9 * alleles
