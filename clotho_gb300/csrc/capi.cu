@@ -104,6 +104,7 @@ struct clotho_ctx {
     bool ring_used[64]{};
     uint32_t ring_next = 0;
     uint32_t set = 0;                                    // next tape set
+    uint32_t pairs_set = 0;                              // the set whose pairs the last generation used
     cudaEvent_t copy_done[2]{}, kern_done[2]{};
     std::string err;
     bool profiling = false;
@@ -392,6 +393,7 @@ void enqueue_fused_step(clotho_ctx* ctx, uint32_t set, bool philox) {
     const uint32_t n = (uint32_t)ctx->pops.size();
     const PopDev* pops = ctx->d_pops[set];
     LaunchCfg L = cfg(ctx);
+    ctx->pairs_set = set == 1u ? 1u : 0u;  // the device-drawn set (2) shares set 0's buffers
     launch_begin(L, pops, n, ctx->d_hdr[set], ctx->d_ctl);
     ensure_parent_acc(ctx, pops, n);
     if (philox) launch_mut_counts_philox(L, pops, n, ctx->maxS);
@@ -822,6 +824,7 @@ int clotho_set_pairs(clotho_ctx* ctx, const uint32_t* pairs) {
     if (!ctx || !ctx->in_step) return fail(ctx, CLOTHO_E_STATE, "clotho_begin_generation first");
     PopHost* p = ctx->pops[0];
     int rc = h2d(ctx, p->dev[0].pairs, pairs, 2ull * p->hostN, ctx->stream);
+    ctx->pairs_set = 0;
     if (rc) return rc;
     CK(cudaStreamSynchronize(ctx->stream));
     return 0;
@@ -833,6 +836,7 @@ int clotho_select(clotho_ctx* ctx, uint32_t* pairs_out) {
     // device draws write the pairs of the Philox set, which shares buffers with set 0
     launch_select_philox(cfg(ctx), ctx->d_pops[2], 1);
     ctx->launches += 1;
+    ctx->pairs_set = 0;
     int rc = check_launch(ctx, "select");
     if (rc) return rc;
     if (pairs_out) {
@@ -1093,8 +1097,8 @@ int clotho_get_pairs(clotho_ctx* ctx, uint32_t* dst) {
     int rc;
     DevStatus s = read_status(ctx, ctx->pops[0], &rc);
     if (rc) return rc;
-    // the last tape step used set (set ^ 1); device draws use set 0's buffer
-    const PopDev& D = ctx->pops[0]->dev[ctx->set ^ 1u];
+    // tape steps alternate between sets 0 and 1; device draws and the staged calls use set 0's buffer
+    const PopDev& D = ctx->pops[0]->dev[ctx->pairs_set];
     if (s.N) CK(cudaMemcpyAsync(dst, D.pairs, 2ull * s.N * 4, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return 0;

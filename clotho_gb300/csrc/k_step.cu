@@ -99,10 +99,15 @@ struct ScanSel {
     uint32_t L;      // elements (counts) to scan; off gets L entries
     uint32_t ncur;   // cursors to zero
 };
-// which == 0: per-row mutation counts; 1: position buckets; 2: rows per ordering key
+// which == 0: per-row mutation counts; 1: position buckets; 2: rows per ordering key.  The ordering keys
+// are parent individuals (below pN, which exceeds 2N when the population shrinks more than twofold) or, in
+// the measurement orders, below 2N or N + pN: the scan covers max(2N, N + pN) keys, at most 2 * Ncap.
 __device__ inline ScanSel scan_sel(const PopDev& P, int which) {
     if (which == 0) return ScanSel{P.row_cnt, P.row_off, P.row_cur, 2u * P.st->N + 1u, 2u * P.st->N};
-    if (which == 2) return ScanSel{P.ord_cnt, P.ord_off, P.ord_cur, 2u * P.st->N + 1u, 2u * P.st->N};
+    if (which == 2) {
+        const uint32_t keys = max(2u * P.st->N, P.st->N + P.st->pN);
+        return ScanSel{P.ord_cnt, P.ord_off, P.ord_cur, keys + 1u, keys};
+    }
     return ScanSel{P.bcnt, P.boff, P.bcur, P.NB + 1u, P.NB};
 }
 

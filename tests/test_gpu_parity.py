@@ -428,3 +428,35 @@ def test_population_size_changing_every_generation(q1):
         if N == 2:  # the generation after the single-individual one
             lost, alleles = info["lost_count"], info["A"]
     assert lost > 0.9 * alleles
+
+
+@pytest.mark.parametrize("bias", [0.0, 1.0, 0.3])
+def test_device_draws_copy_the_reported_parent_strand(bias):
+    # device-drawn generations without breakpoints or new alleles: every offspring row is a copy of one
+    # strand of the parent that pairs() reports for it, the second strand exactly when the strand-swap
+    # draw (probability bias) says so; the first step runs on a fresh context (no tape step before it)
+    rng = np.random.default_rng(23)
+    N, A = 400, 3000
+    pos = rng.random(A)
+    thr = (rng.random(A) * 0.3 * 2.0 ** 32).astype(np.uint32)  # carried by under 30% of rows: none fixed
+    pop = cg.Population(N, 4096, 1, mu=0.0, rho=0.0, bias=bias, p_neutral=1.0, seed=29)
+    pop.seed_population(N, pos, np.zeros(A, np.float32), thr, 31)
+    swaps, total = 0, 0
+    for g in range(3):
+        parent = pop.rows()
+        pop.simulate_philox(N)
+        child, pairs = pop.rows(), pop.pairs()
+        assert child.shape == parent.shape and pairs.max() < N
+        for r in range(2 * N):
+            top, bot = parent[2 * pairs[r]], parent[2 * pairs[r] + 1]
+            is_top, is_bot = np.array_equal(child[r], top), np.array_equal(child[r], bot)
+            assert is_top or is_bot, f"gen {g} row {r}: not a copy of parent {pairs[r]}"
+            if is_top != is_bot:
+                swaps += int(is_bot)
+                total += 1
+    assert pop.info()["device_error"] == 0 and total > 0.95 * 3 * 2 * N
+    frac = swaps / total
+    if bias in (0.0, 1.0):
+        assert frac == bias
+    else:
+        assert abs(frac - bias) < 5 * np.sqrt(bias * (1 - bias) / total)
