@@ -185,6 +185,33 @@ def test_growth_schedule_in_one_graph_equals_generation_by_generation():
     bt.close()
 
 
+def test_batch_schedules_that_shrink_match_populations_run_alone():
+    # per-population sizes that shrink more than tenfold in one generation and regrow, on a batch of
+    # three: each member ends bit-identical (rows, phenotypes, fitness, allele tables) to the same
+    # population stepped alone through the same sizes, since its draws depend only on its own seed
+    sched = [[300, 50, 120], [30, 400, 120], [250, 9, 20], [1, 150, 300], [90, 300, 2]]
+    descs, alone = [], []
+    for k in range(3):
+        kw = dict(KW, seed=101 + k, max_events=1 << 16, max_mutations=1 << 13)
+        pop = cg.Population(400, 1 << 13, 2, **kw)
+        pop.init([200, 100, 300][k])
+        for row in sched:
+            pop.simulate_philox(row[k])
+        alone.append(pop)
+        descs.append(pop.desc)
+    bt = cg.Batch(descs)
+    bt.N = [200, 100, 300]
+    bt.init()
+    bt.run_schedule(sched)
+    for k, pop in enumerate(alone):
+        ib = bt.info(k)
+        assert ib["device_error"] == 0 and ib["N"] == sched[-1][k]
+        assert np.array_equal(bt.rows(k), pop.rows()), f"population {k}"
+        assert bt.stats(k)["mean_fitness"] == pop.stats()["mean_fitness"]
+        pop.close()
+    bt.close()
+
+
 def test_runs_on_the_callers_stream():
     torch = pytest.importorskip("torch")
     N = 1200

@@ -460,3 +460,46 @@ def test_device_draws_copy_the_reported_parent_strand(bias):
         assert frac == bias
     else:
         assert abs(frac - bias) < 5 * np.sqrt(bias * (1 - bias) / total)
+
+
+def test_device_draws_with_the_size_changing_copy_the_reported_parents():
+    # device-drawn copy generations (no breakpoints, no new alleles) while the population shrinks tenfold,
+    # grows and shrinks again: each offspring row is one strand of the parent pairs() reports for it, less
+    # the alleles every parent row carries (fixed: cleared before the copy; after the one-individual
+    # generation these are the alleles on both of its strands)
+    rng = np.random.default_rng(41)
+    N0, A = 400, 2000
+    pos = rng.random(A)
+    thr = (rng.random(A) * 0.3 * 2.0 ** 32).astype(np.uint32)
+    pop = cg.Population(N0, 4096, 1, mu=0.0, rho=0.0, bias=0.5, p_neutral=1.0, seed=43)
+    pop.seed_population(N0, pos, np.zeros(A, np.float32), thr, 47)
+    for g, N in enumerate([40, 400, 7, 300, 1, 90]):
+        parent = pop.rows()
+        pN = parent.shape[0] // 2
+        parent = parent & ~np.bitwise_and.reduce(parent, axis=0)
+        pop.simulate_philox(N)
+        child, pairs = pop.rows(), pop.pairs()
+        assert child.shape[0] == 2 * N and len(pairs) == 2 * N and pairs.max() < pN, f"gen {g}"
+        for r in range(2 * N):
+            p = int(pairs[r])
+            assert np.array_equal(child[r], parent[2 * p]) or np.array_equal(child[r], parent[2 * p + 1]), \
+                f"gen {g} (N {pN} -> {N}) row {r}: not a strand of parent {p}"
+    assert pop.info()["device_error"] == 0
+
+
+def test_staged_policies_with_the_size_changing():
+    # the stage-by-stage calls on a population that shrinks more than twofold and regrows: the same rows
+    # as the fused step and the oracle
+    sizes = [180, 60, 200, 25, 180, 90]
+    orc, gpu = make_pair(200, 4096, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.2, rho=1.5, p_neutral=0.4)
+    gpu2 = cg.Population(200, 4096, 2, fitness="gaussian_vs", fit_param=4.0, mu=0.2, rho=1.5, p_neutral=0.4,
+                         max_events=8192, max_mutations=8192, max_fixed=1 << 16)
+    orc.init(sizes[0])
+    gpu.init(sizes[0])
+    gpu2.init(sizes[0])
+    for g, N in enumerate(sizes):
+        tape = orc.step_record(N)
+        gpu.simulate(tape)
+        gpu2.simulate_staged(tape)
+        compare_state(orc, gpu2, g, kind="gaussian_vs", fit_param=4.0)
+        assert np.array_equal(gpu.rows(), gpu2.rows()), f"gen {g}"
