@@ -409,13 +409,15 @@ def test_tape_rows_with_many_new_alleles_sort_their_lists():
     assert a.info()["device_error"] == 0
 
 
+@pytest.mark.parametrize("mu", [0.3, 1.0])
 @pytest.mark.parametrize("q1", [True, False])
-def test_population_size_changing_every_generation(q1):
+def test_population_size_changing_every_generation(q1, mu):
     # a growth model's sizes through the tape call: the population grows, shrinks to one individual and
     # regrows (row counts, parent ranges and fitness tables change every generation; after the bottleneck
-    # almost every allele is lost and the new ones reuse the slots); bit-exact against the oracle throughout
+    # almost every allele is lost and the new ones reuse the slots); at mu = 1 the rows also widen from 8
+    # to 16 to 24 words in generations that change the size; bit-exact against the oracle throughout
     sizes = [150, 220, 90, 90, 300, 40, 1, 2, 60, 200, 299, 17]
-    orc, gpu = make_pair(300, 4096, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.3, rho=1.0, p_neutral=0.3,
+    orc, gpu = make_pair(300, 4096, T=2, fitness="gaussian_vs", fit_param=4.0, mu=mu, rho=1.0, p_neutral=0.3,
                          q1=q1)
     orc.init(sizes[0])
     gpu.init(sizes[0])
