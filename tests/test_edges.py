@@ -1,6 +1,6 @@
 """Edge cases through the C-ABI: very long breakpoint lists, tapes with
-out-of-range indices, allele-capacity overflow, all-zero fitness and a
-one-individual population.  Invalid tape entries are bounds-checked on the
+out-of-range indices, overflow of the allele, fixed-allele, event and
+mutation capacities, all-zero fitness and a one-individual population.  Invalid tape entries are bounds-checked on the
 device: they are skipped and reported as sticky error bits
 (CLOTHO_DEVERR_*), and the population stays usable."""
 import numpy as np
@@ -104,4 +104,56 @@ def test_one_individual_population():
     i = gpu.info()
     assert i["N"] == 1 and gpu.rows().shape[0] == 2
     assert np.isfinite(gpu.phenotypes()).all()
+    gpu.close()
+
+
+def test_fixed_table_overflow_is_flagged_and_capped():
+    # every offspring row copies one strand, so the next step finds all of its alleles fixed: more than the
+    # fixed table holds.  The first max_fixed are recorded (the oracle's list is unbounded), the rest are
+    # still cleared and their slots freed, so rows and free list stay bit-exact
+    N, A = 20, 40
+    orc = oracle.Oracle(T=1, fitness=oracle.FIT_CONSTANT, mu=0.0, rho=0.0, p_neutral=1.0, q1=True, threads=1, seed=3)
+    gpu = cg.Population(N, 4096, 1, mu=0.0, rho=0.0, p_neutral=1.0, max_events=64, max_mutations=64, max_fixed=4)
+    pos, eff, thr = np.linspace(0.01, 0.99, A), np.zeros(A, np.float32), np.full(A, 2 ** 31, np.uint32)
+    orc.seed_population(N, pos, eff, thr, 7)
+    gpu.seed_population(N, pos, eff, thr, 7)
+    rng = np.random.default_rng(4)
+    for pairs in (np.zeros(2 * N), rng.integers(0, N, 2 * N), rng.integers(0, N, 2 * N)):
+        tape = _tape(N, pairs, [], rng=rng)
+        orc.step_tape(tape)
+        gpu.simulate(tape)
+        assert np.array_equal(orc.rows(), gpu.rows())
+        assert np.array_equal(orc.free_list(), gpu.free_list())
+    i, oi = gpu.info(), orc.info()
+    assert oi["fixed_total"] > 4
+    assert i["device_error"] & 2                       # CLOTHO_DEVERR_FIXED
+    assert i["fixed_total"] == 4
+    assert np.array_equal(gpu.fixed()[0], orc.fixed()[0][:4])
+    gpu.close()
+
+
+def test_device_event_overflow_is_flagged_and_clamped():
+    # device-drawn breakpoint counts past 128 a gamete are clamped to 128 and flagged; the run goes on
+    N = 50
+    gpu = cg.Population(N, 4096, 1, mu=0.05, rho=300.0, p_neutral=1.0, max_events=1 << 16, max_mutations=1024)
+    gpu.init(N)
+    gpu.simulate_philox(N)
+    gpu.simulate_philox(N)
+    i = gpu.info()
+    assert i["device_error"] & 4                       # CLOTHO_DEVERR_EVENTS
+    assert i["generation"] == 3 and i["N"] == N
+    gpu.close()
+
+
+def test_device_mutation_overflow_is_flagged_and_capped():
+    # a device-drawn mutation count past max_mutations is capped at it and flagged
+    N = 100
+    gpu = cg.Population(N, 1 << 14, 1, mu=5.0, rho=0.5, p_neutral=1.0, max_events=4096, max_mutations=64)
+    gpu.init(N)
+    gpu.simulate_philox(N)
+    i = gpu.info()
+    assert i["device_error"] & 32                      # CLOTHO_DEVERR_MUT
+    assert i["last_M"] == 64 and i["A"] <= 64
+    gpu.simulate_philox(N)
+    assert gpu.info()["generation"] == 3
     gpu.close()
