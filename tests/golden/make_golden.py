@@ -17,7 +17,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 import oracle  # noqa: E402
 
 CASES = {
-    # name: (oracle params, N, generations)
+    # name: (oracle params, N or the list of per-generation sizes, generations)
     "neutral_wf": (dict(T=1, fitness=oracle.FIT_CONSTANT, mu=0.3, rho=0.5, p_neutral=1.0, seed=101), 64, 12),
     "qtl_two_traits": (dict(T=2, fitness=oracle.FIT_GAUSSIAN_VS, fit_param=4.0, mu=0.3, rho=2.0, p_neutral=0.3,
                             seed=202), 48, 10),
@@ -27,17 +27,24 @@ CASES = {
     # slots reused (engine_batched_task.hpp:303-345)
     "drift_fixation": (dict(T=2, fitness=oracle.FIT_QUADRATIC, fit_param=2.0, mu=0.5, rho=0.5, p_neutral=0.5,
                             seed=404), 6, 60),
+    # a size per generation (a growth model): growth, a fall below half (the parent individuals outnumber
+    # the offspring rows), a one-individual bottleneck and regrowth
+    "size_changes": (dict(T=2, fitness=oracle.FIT_GAUSSIAN_VS, fit_param=4.0, mu=0.6, rho=1.5, p_neutral=0.3,
+                          seed=505), [60, 150, 20, 1, 3, 70, 200, 45], 8),
 }
 
 
 def make(name, params, N, G):
+    sizes = list(N) if isinstance(N, list) else [N] * G
+    assert len(sizes) == G
     orc = oracle.Oracle(threads=1, **params)
-    orc.init(N)
-    d = {"N": np.array([N]), "G": np.array([G]), "T": np.array([params["T"]])}
+    orc.init(sizes[0])
+    d = {"N": np.array([sizes[0]]), "Ncap": np.array([max(sizes)]), "G": np.array([G]),
+         "T": np.array([params["T"]])}
     for k, v in params.items():
         d[f"param_{k}"] = np.array([v])
     for g in range(G):
-        t = orc.step_record(N)
+        t = orc.step_record(sizes[g])
         d[f"g{g}_NM"] = np.array([t.N, t.M], np.int64)
         for f in ("pairs", "swap", "ev_off", "ev_pos", "mut_seq", "mut_pos", "mut_eff"):
             d[f"g{g}_{f}"] = getattr(t, f)
@@ -57,6 +64,9 @@ def make(name, params, N, G):
 
 
 if __name__ == "__main__":
+    # python tests/golden/make_golden.py [name ...]  (all cases when none is named)
     for name, (params, N, G) in CASES.items():
+        if len(sys.argv) > 1 and name not in sys.argv[1:]:
+            continue
         info = make(name, params, N, G)
         print(name, info)

@@ -68,7 +68,8 @@ def test_gpu_replays_golden(path):
     names = {oracle.FIT_CONSTANT: "constant", oracle.FIT_GAUSSIAN: "gaussian", oracle.FIT_QUADRATIC: "quadratic",
              oracle.FIT_GAUSSIAN_VS: "gaussian_vs"}
     N = int(z["N"][0])
-    pop = cg.Population(N, 4096, p["T"], fitness=names[p["fitness"]], fit_param=p.get("fit_param", 1.0),
+    cap = int(z["Ncap"][0]) if "Ncap" in z.files else N
+    pop = cg.Population(cap, 4096, p["T"], fitness=names[p["fitness"]], fit_param=p.get("fit_param", 1.0),
                         mu=p["mu"], rho=p["rho"], p_neutral=p["p_neutral"], q1=p.get("q1", True),
                         max_events=1 << 14, max_mutations=1 << 12, max_fixed=1 << 14)
     pop.init(N)
@@ -84,8 +85,8 @@ def test_gpu_replays_golden(path):
     assert np.array_equal(fpos, z["fixed_pos"]) and np.array_equal(fage, z["fixed_age"])
     # phenotype: the tolerance of tests/test_gpu_parity.py over G generations
     G = len(tapes)
-    S = 2 * N
     rows = z["rows"]
+    S = rows.shape[0]
     A = eff.shape[0]
     bits = np.unpackbits(rows.view(np.uint8).reshape(S, -1), axis=1, bitorder="little")[:, :A].astype(np.float64)
     s = bits @ np.abs(eff.astype(np.float64))
