@@ -505,3 +505,28 @@ def test_staged_policies_with_the_size_changing():
         gpu2.simulate_staged(tape)
         compare_state(orc, gpu2, g, kind="gaussian_vs", fit_param=4.0)
         assert np.array_equal(gpu.rows(), gpu2.rows()), f"gen {g}"
+
+
+def test_pairs_report_the_parents_of_the_last_generation_on_every_path():
+    # tape steps alternate between two upload sets; device-drawn and staged steps use the first one.  After
+    # every step, in any order, pairs() returns the parents that step used (the tape's own, for tape steps)
+    N = 120
+    orc, gpu = make_pair(N, 4096, T=1, mu=0.1, rho=1.0, p_neutral=1.0)
+    orc.init(N)
+    gpu.init(N)
+    for g, kind in enumerate(["tape", "tape", "tape", "philox", "tape", "staged", "tape", "philox", "philox",
+                              "staged", "staged", "tape"]):
+        if kind == "philox":
+            gpu.simulate_philox(N)
+            got = gpu.pairs()
+            assert len(got) == 2 * N and got.max() < N, f"step {g}"
+            # the device-drawn parents explain the rows: continue the oracle from the GPU's state
+            orc.load_population(N, gpu.rows(), *gpu.alleles()[0:3:2])
+            continue
+        tape = orc.step_record(N)
+        if kind == "tape":
+            gpu.simulate(tape)
+        else:
+            gpu.simulate_staged(tape)
+        assert np.array_equal(gpu.pairs(), tape.pairs), f"step {g} ({kind})"
+        assert np.array_equal(gpu.rows(), orc.rows()), f"step {g} ({kind})"
