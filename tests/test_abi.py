@@ -57,3 +57,47 @@ def test_oracle_exports_its_header():
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     names = sorted(set(re.findall(r"\b(orc_[a-z_0-9]+)\s*\(", text)))
     assert names and all(hasattr(lib, n) for n in names)
+
+
+def test_calls_without_a_context_or_with_bad_arguments_return_a_status():
+    # argument checks come before any CUDA call, so they answer on a machine without a GPU too
+    from clotho_gb300 import capi
+    L = capi.load()
+    E_ARG, E_CAPACITY = -1, -3
+    info = capi.Info()
+    assert L.clotho_destroy(None) == E_ARG
+    assert L.clotho_last_error(None) == b"null context"
+    assert L.clotho_get_info(None, ctypes.byref(info)) == E_ARG
+    assert L.clotho_init(None, 10) == E_ARG
+    assert L.clotho_generation_philox(None, 10) == E_ARG
+    assert L.clotho_sync(None) == E_ARG
+    assert L.clotho_set_stream(None, None) == E_ARG
+    assert L.clotho_pop_count(None) == 0 and L.clotho_launch_count(None) == 0
+    assert L.clotho_snapshot_size(None) == 0
+    assert L.clotho_footprint_for(None) == 0
+    out = ctypes.c_void_p()
+    assert L.clotho_create(None, ctypes.byref(out)) == E_ARG
+    d = capi.Desc(100, 1024, 1, 100, 100, 100, 0, 1, 1.0, 0.01, 0.01, 0.5, 0.5, 0.0, 1.0, 1)
+    assert L.clotho_create(ctypes.byref(d), None) == E_ARG
+    assert L.clotho_batch_create(None, 3, ctypes.byref(out)) == E_ARG           # descriptors missing
+    many = (capi.Desc * 257)(*([d] * 257))
+    assert L.clotho_batch_create(many, 257, ctypes.byref(out)) == E_ARG         # more than 256 populations
+    # the allocation-free entry point: output pointers checked, then the width limit (16,384 words)
+    counts = (ctypes.c_uint32 * 3)()
+    free_list = (ctypes.c_uint32 * 8)()
+    assert L.clotho_free_space_noalloc(None, 0, 0, 64, None, counts, None) == E_ARG
+    assert L.clotho_free_space_noalloc(None, 0, 0, 64 * 16_384 + 1, free_list, counts, None) == E_CAPACITY
+    assert L.clotho_free_space_noalloc(None, 4, 16, 64, free_list, counts, None) == E_ARG  # rows missing
+
+
+def test_create_without_a_device_fails_cleanly():
+    # no GPU here: clotho_create reports a CUDA error and hands back no context
+    from tests.conftest import gpu_available
+    if gpu_available():
+        pytest.skip("a CUDA device is present")
+    from clotho_gb300 import capi
+    L = capi.load()
+    d = capi.Desc(100, 1024, 1, 100, 100, 100, 0, 1, 1.0, 0.01, 0.01, 0.5, 0.5, 0.0, 1.0, 1)
+    out = ctypes.c_void_p(1234)
+    assert L.clotho_create(ctypes.byref(d), ctypes.byref(out)) == -2            # CLOTHO_E_CUDA
+    assert not out.value
