@@ -6,8 +6,9 @@ ascending), fixed-column clearing (engine_batched_task.hpp:303-345), the
 child width (:287-301), crossover by breakpoint parity with upper_bound ties
 (position_classifier.hpp:59-93, block_crossover.hpp:46-63; Q1 keeps the second
 gamete whole), mutation into free slots then appended ones
-(batch_mutation_mt.hpp:114-150), and per-genome effect sums
-(batch_phenotype_mt_population_space_row.hpp:111-156).  The numpy version
+(batch_mutation_mt.hpp:114-150), per-genome effect sums
+(batch_phenotype_mt_population_space_row.hpp:111-156), and the fitness
+metrics on the resulting phenotypes (general_fitness.hpp:101-119).  The numpy version
 works on whole bit matrices, so it shares no code or loop structure with the
 C++ restatement it checks."""
 import numpy as np
@@ -102,3 +103,39 @@ def test_oracle_step_matches_numpy_restatement(q1, Np, N, M):
     assert np.array_equal(oeff.reshape(-1, T), want_eff.astype(np.float32).astype(np.float64))
     assert np.array_equal(orc.fixed()[0], pos[want_fixed])
     np.testing.assert_allclose(orc.phenotypes().reshape(-1, T), want_z, rtol=1e-12, atol=1e-12)
+
+
+def numpy_fitness(z, kind, fit_param, N, mu):
+    """The toolkit metrics (normal_fitness_metric.cpp:25-31 with sigma = sqrt(4 N mu), normal_fitness_generator.cpp:36-52;
+    quadratic_fitness_metric.cpp:23-28; constant) on trait 0, and exp(-|z|^2 / 2 Vs) over all traits."""
+    n4 = np.sqrt(4.0 * N * mu)
+    if kind == oracle.FIT_GAUSSIAN:
+        return np.exp(-z[:, 0] ** 2 / (2.0 * n4 * n4)) / (n4 * np.sqrt(2.0 * np.pi))
+    if kind == oracle.FIT_QUADRATIC:
+        r = (z[:, 0] / (fit_param * n4)) ** 2
+        return np.where(r >= 1.0, 0.0, 1.0 - r)
+    if kind == oracle.FIT_GAUSSIAN_VS:
+        return np.exp(-(z ** 2).sum(axis=1) / (2.0 * fit_param))
+    return np.ones(len(z))
+
+
+@pytest.mark.parametrize("kind", [oracle.FIT_GAUSSIAN, oracle.FIT_QUADRATIC, oracle.FIT_GAUSSIAN_VS,
+                                  oracle.FIT_CONSTANT])
+def test_oracle_fitness_matches_the_metric_formulas(kind):
+    rng = np.random.default_rng(77 + kind)
+    Np, N, A, T, mu = 30, 24, 300, 2, 0.05
+    rows, pos, eff, tape = random_case(rng, Np, N, A, T, 10, rho=1.0)
+    # the metric's scale from the phenotypes (numpy restatement), so that its values spread out
+    z = numpy_step(rows, pos, eff.astype(np.float64), tape, True)[5]
+    n4 = np.sqrt(4.0 * N * mu)
+    fit_param = {oracle.FIT_QUADRATIC: float(np.median(np.abs(z[:, 0]))) / n4,
+                 oracle.FIT_GAUSSIAN_VS: float(np.median((z ** 2).sum(axis=1))) / 2.0}.get(kind, 1.0)
+    orc = oracle.Oracle(T=T, fitness=kind, fit_param=fit_param, mu=mu, rho=1.0, p_neutral=0.0, q1=True,
+                        threads=2, seed=5)
+    orc.load_population(Np, rows, pos, eff)
+    orc.step_tape(tape)
+    z = orc.phenotypes().reshape(-1, T)
+    f = numpy_fitness(z, kind, fit_param, N, mu)
+    if kind == oracle.FIT_QUADRATIC:
+        assert 0 < (f == 0.0).sum() < N        # both branches of the metric are exercised
+    np.testing.assert_allclose(orc.fitness(), f, rtol=1e-13, atol=1e-300)
