@@ -289,3 +289,23 @@ def test_async_info_requests_match_synchronous_reads():
     t = [bt.info_request(i) for i in range(2)]
     assert [bt.info_wait(x) for x in t] == [bt.info(i) for i in range(2)]
     bt.close()
+
+
+def test_a_qtlsim_configuration_runs_end_to_end():
+    # a reference configuration file (string values, as Boost writes them) read into a device population
+    # and run for its generations under its growth model
+    from clotho_gb300 import config
+    cfg = {"configuration": {
+        "generations": {"size": "12"},
+        "population_growth": {"name": "predefined", "params": {"sizes": ["400", "150", "600"]}},
+        "mutation": {"mu": "0.05"}, "recombination": {"rho": "1.5", "sequence_bias": {"p": "0.4"}},
+        "traits": {"N": "2"}, "neutral": {"p": "0.3"}, "fitness": {"name": "quadratic", "params": {"scale": "4"}},
+        "random_number": {"seed": "9"}}}
+    rc = config.from_reference(cfg)
+    pop = rc.population()
+    assert pop.info()["N"] == 400
+    pop.run_philox_schedule(rc.sizes())
+    i = pop.info()
+    assert i["device_error"] == 0 and i["N"] == rc.sizes()[-1] and i["generation"] == 13
+    assert pop.stats(16)["segregating"] > 0
+    pop.close()
