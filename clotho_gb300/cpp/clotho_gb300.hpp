@@ -347,6 +347,63 @@ private:
     std::map<std::string, Factory> tools_;
 };
 
+// ---- QTLSim configuration trees (boost::property_tree::ptree, or any tree with get<T>(path, default),
+// get_child_optional(path), get_child(path), iteration over (key, child) pairs and data()): the keys
+// QTLSim reads, from its "configuration" block or the root (qtlsim_main.cpp:111-113), with the
+// defaults of the reference's parameter objects.  The allele and individual capacities have no key.
+template <class Tree>
+const Tree& configuration_block(const Tree& config) {
+    auto b = config.get_child_optional("configuration");
+    return b ? config.get_child("configuration") : config;
+}
+
+template <class Tree>
+Parameters params_from(const Tree& config, uint32_t max_individuals, uint32_t max_alleles) {
+    const Tree& c = configuration_block(config);
+    Parameters p;
+    p.max_individuals = max_individuals;
+    p.max_alleles = max_alleles;
+    p.mu = c.template get<double>("mutation.mu", 1e-4);                       // mutation_rate_parameter.hpp:24-39
+    p.rho = c.template get<double>("recombination.rho", 1e-4);                // recombination_rate_parameter.hpp:24-39
+    p.bias = c.template get<double>("recombination.sequence_bias.p", 0.5);    // sequence_bias_parameter.hpp:23-42
+    p.traits = c.template get<uint32_t>("traits.N", 1u);                      // trait_count_parameter.hpp:23-38
+    p.eff_mean = c.template get<double>("traits.mean", 0.0);                  // normal_distribution_parameter.hpp:23-41
+    p.eff_sigma = c.template get<double>("traits.sigma", 1.0);
+    p.p_neutral = c.template get<double>("neutral.p", 0.5);                   // neutral_parameter.hpp:35-50
+    const std::string f = c.template get<std::string>("fitness.name", "");    // fitness_toolkit.cpp:50-69
+    if (f.empty() || f == "constant") p.fitness = CLOTHO_FIT_CONSTANT;
+    else if (f == "gaussian") p.fitness = CLOTHO_FIT_GAUSSIAN;
+    else if (f == "quadratic") p.fitness = CLOTHO_FIT_QUADRATIC;
+    else throw Error("unknown fitness metric: " + f);
+    p.fit_param = p.fitness == CLOTHO_FIT_QUADRATIC ? c.template get<double>("fitness.params.scale", 1.0) : 1.0;
+    p.seed = c.template get<uint64_t>("random_number.seed", 0u);              // seed_parameter.hpp:25-46
+    if (p.traits < 1 || p.traits > 4) throw Error("traits.N must be 1..4");
+    return p;
+}
+
+// population_growth.{name, params} (population_growth_toolkit.cpp:36-58): null without a model.
+template <class Tree>
+std::shared_ptr<PopulationGrowth> growth_from(const Tree& config) {
+    const Tree& c = configuration_block(config);
+    const std::string name = c.template get<std::string>("population_growth.name", "");
+    if (name.empty()) return nullptr;
+    GrowthToolkit::Params prm;
+    if (c.get_child_optional("population_growth.params")) {
+        for (const auto& kv : c.get_child("population_growth.params")) {
+            std::vector<double>& v = prm[kv.first];
+            if (!kv.second.data().empty()) v.push_back(std::stod(kv.second.data()));
+            for (const auto& item : kv.second) v.push_back(std::stod(item.second.data()));  // lists ("sizes")
+        }
+    }
+    return GrowthToolkit::instance().get_tool(name, prm);
+}
+
+// generations.size (examples/generation_parameter.cpp:17-33)
+template <class Tree>
+unsigned generations_from(const Tree& config) {
+    return configuration_block(config).template get<unsigned>("generations.size", 10000u);
+}
+
 // ---- Engine<...> restated on the device (engine_batched_task.hpp:110-223).
 // staged = true drives the policies one by one; false uses the fused call.
 template <class RNG = std::mt19937_64>
