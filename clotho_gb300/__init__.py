@@ -275,6 +275,8 @@ class Population:
         return out
 
     def pairs(self) -> np.ndarray:
+        """Parent individual of each of the last generation's 2N gametes (gametes 2k and 2k+1 make
+        individual k), whichever call made that generation: a tape, device draws or the staged calls."""
         N = self.info()["N"]
         out = np.zeros(2 * N, np.uint32)
         self._ck(self.L.clotho_get_pairs(self.h, _ptr(out)), "get_pairs")
