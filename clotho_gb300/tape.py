@@ -14,7 +14,6 @@ with numpy, vectorised; it is the host-side producer used for end-to-end runs.
 """
 from __future__ import annotations
 
-import io
 from dataclasses import dataclass
 
 import numpy as np

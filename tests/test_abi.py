@@ -4,7 +4,6 @@ import ctypes
 import glob
 import os
 import re
-import subprocess
 
 import pytest
 

@@ -8,7 +8,6 @@ tape-driven run stays bit-exact against the oracle after the restore.
 import numpy as np
 import pytest
 
-import oracle
 from tests.conftest import gpu_available
 
 pytestmark = pytest.mark.gpu
