@@ -139,3 +139,21 @@ def test_oracle_fitness_matches_the_metric_formulas(kind):
     if kind == oracle.FIT_QUADRATIC:
         assert 0 < (f == 0.0).sum() < N        # both branches of the metric are exercised
     np.testing.assert_allclose(orc.fitness(), f, rtol=1e-13, atol=1e-300)
+
+
+def test_oracle_results_do_not_depend_on_its_thread_count():
+    # the partitioned stages (crossover by pairs, phenotype by genomes, free space by columns) give the same
+    # rows, tables, phenotypes and fitness on one thread and on four, generation after generation
+    runs = []
+    for threads in (1, 4):
+        orc = oracle.Oracle(T=2, fitness=oracle.FIT_GAUSSIAN_VS, fit_param=4.0, mu=0.4, rho=2.0, p_neutral=0.3,
+                            q1=False, threads=threads, seed=17)
+        orc.init(150)
+        states = []
+        for N in (150, 150, 90, 200, 200, 60):
+            orc.step_record(N)
+            states.append((orc.rows(), orc.free_list(), orc.alleles()[0], orc.phenotypes(), orc.fitness()))
+        runs.append(states)
+    for g, (a, b) in enumerate(zip(*runs)):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y), f"generation {g}"
