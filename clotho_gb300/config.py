@@ -35,6 +35,13 @@ from . import growth as _growth
 FITNESS_NAMES = {"": "constant", "constant": "constant", "gaussian": "gaussian", "quadratic": "quadratic"}
 
 
+def neutral_capacity(N: int, mu: float, G: int) -> int:
+    """Allele slots for a run of G generations at N individuals: about 1.5x the neutral transient's
+    segregating sites, 2 N mu (1 + 2 ln G), at least 2,048 and at most 2^22."""
+    est = 2.0 * N * mu * (1.0 + 2.0 * math.log(max(G, 2)))
+    return int(min(1 << 22, max(2048, 1.5 * est + 1024)))
+
+
 def _block(cfg: dict, key: str) -> dict:
     v = cfg.get(key, {})
     return v if isinstance(v, dict) else {}
@@ -70,10 +77,8 @@ class RunConfig:
         return max([self.N0] + self.sizes()) if self.generations else self.N0
 
     def max_alleles(self) -> int:
-        """About 1.5x the neutral transient's segregating sites, 2 N mu (1 + 2 ln G), at the largest size."""
-        n = self.max_individuals()
-        est = 2.0 * n * self.mu * (1.0 + 2.0 * math.log(max(self.generations, 2)))
-        return int(min(1 << 22, max(2048, 1.5 * est + 1024)))
+        """The neutral capacity at the largest size."""
+        return neutral_capacity(self.max_individuals(), self.mu, self.generations)
 
     def desc(self, max_alleles: int | None = None, **caps):
         from . import make_desc

@@ -21,6 +21,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import Batch, make_desc, footprint_of, Population
+from .config import neutral_capacity
 
 
 @dataclass
@@ -42,9 +43,7 @@ class Job:
     result: dict = field(default_factory=dict)
 
     def max_alleles(self) -> int:
-        # neutral transient: ~2N mu (1 + 2 ln G) segregating slots, with head room
-        est = 2.0 * self.N * self.mu * (1.0 + 2.0 * math.log(max(self.G, 2)))
-        return int(min(1 << 22, max(2048, 1.5 * est + 1024)))
+        return neutral_capacity(self.N, self.mu, self.G)
 
     def desc(self):
         return make_desc(self.N, self.max_alleles(), self.T, mu=self.mu, rho=self.rho, fitness=self.fitness,
