@@ -46,13 +46,26 @@ def make_pair(N, A_cap, T=1, fitness="constant", fit_param=1.0, mu=0.05, rho=0.5
 
 
 def pheno_bound(rows, eff, gens=0):
-    """(g+1)(n+1) 2^-24 sum|w| per individual from the rows and the FP32 effects."""
+    """(g+1)(n+1) 2^-24 sum|w| per individual from the rows and the FP32 effects.
+    Only the nonzero words are unpacked, so populations of 1e5 individuals with
+    wide rows fit in host memory."""
     S, W = rows.shape
-    A = eff.shape[0]
-    bits = np.unpackbits(rows.view(np.uint8).reshape(S, W * 8), axis=1, bitorder="little")[:, :A].astype(np.float64)
+    A, T = eff.shape
     absw = np.abs(eff.astype(np.float64))
-    s = bits @ absw                       # [S, T]
-    n = bits.sum(axis=1)                  # [S]
+    s = np.zeros((S, T))
+    n = np.zeros(S)
+    for r0 in range(0, S, 16384):
+        r, w = np.nonzero(rows[r0:r0 + 16384])
+        if r.size == 0:
+            continue
+        words = np.ascontiguousarray(rows[r0 + r, w])
+        bits = np.unpackbits(words.view(np.uint8).reshape(-1, 8), axis=1, bitorder="little")
+        k, b = np.nonzero(bits)
+        slot = w[k].astype(np.int64) * 64 + b
+        ok = slot < A
+        row = r0 + r[k][ok]
+        np.add.at(s, row, absw[slot[ok]])
+        n += np.bincount(row, minlength=S)
     s_ind = s[0::2] + s[1::2]
     n_ind = (n[0::2] + n[1::2])[:, None]
     worst = ((n_ind + 1.0) * s_ind).max(axis=0) if len(s_ind) else np.zeros(s.shape[1])
@@ -530,3 +543,48 @@ def test_pairs_report_the_parents_of_the_last_generation_on_every_path():
             gpu.simulate_staged(tape)
         assert np.array_equal(gpu.pairs(), tape.pairs), f"step {g} ({kind})"
         assert np.array_equal(gpu.rows(), orc.rows()), f"step {g} ({kind})"
+
+
+def test_c1_neutral_wright_fisher_at_its_stated_size():
+    # the neutral configuration as stated: N = 1e4 diploid (2e4 rows), mu = 0.01 per sequence, rho = 0.01
+    # per gamete, uniform parents, 1,000 generations, free-space analysis every generation; every
+    # generation's state compared with the oracle
+    from clotho_gb300 import workloads
+    w = workloads.NEUTRAL_WF
+    orc, gpu = make_pair(w.N, w.max_alleles, T=1, fitness="constant", mu=w.mu, rho=w.rho, p_neutral=1.0,
+                         seed=20261203, threads=4)
+    orc.init(w.N)
+    gpu.init(w.N)
+    for g in range(w.generations):
+        gpu.simulate(orc.step_record(w.N))
+        compare_state(orc, gpu, g, kind="constant", mu=w.mu)
+    i = gpu.info()
+    assert i["generation"] == w.generations + 1 and i["A"] > 1000
+
+
+def test_c2_qtl_selection_at_its_stated_population_size(capsys):
+    # the QTL-with-selection configuration at its stated size: N = 1e5 (2e5 rows), mu = 0.1 per sequence
+    # (2e4 new alleles a generation), rho = 1, one trait with N(0,1) effects, exp(-z^2/2), parents from the
+    # FP64 prefix sum over 1e5 fitness values (25 scan chunks), parent-major ordering over 1e5 parents; the
+    # allele count passes 65,536 slots, so the interval classifier runs.  12 generations (the oracle's
+    # cost grows with the rows' width); state compared every fourth generation and at the end.
+    import os
+    from clotho_gb300 import workloads
+    w = workloads.QTL_SELECTION
+    G = 12
+    orc, gpu = make_pair(w.N, w.max_alleles, T=1, fitness="gaussian_vs", fit_param=w.fit_param, mu=w.mu,
+                         rho=w.rho, p_neutral=w.p_neutral, seed=4242, threads=os.cpu_count() or 4)
+    orc.init(w.N)
+    gpu.init(w.N)
+    worst, mean = 0.0, 0.0
+    for g in range(G):
+        gpu.simulate(orc.step_record(w.N))
+        if g % 4 == 3 or g == G - 1:
+            compare_state(orc, gpu, g, kind="gaussian_vs", fit_param=w.fit_param, mu=w.mu)
+            err = np.abs(orc.phenotypes() - gpu.phenotypes())
+            worst, mean = max(worst, float(err.max())), float(err.mean())
+    i = gpu.info()
+    assert i["A"] > 65_536
+    with capsys.disabled():
+        print(f"\nC2 at N={w.N} G={G}: rows bit-exact; phenotype |FP32 carried - FP64| max {worst:.3e}, "
+              f"mean {mean:.3e} at generation {G} (alleles {i['A']}, row width {i['W']} words)")
