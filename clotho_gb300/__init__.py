@@ -25,7 +25,8 @@ FLAG_Q1 = 1
 DEVICE_ERRORS = {1: "allele capacity exceeded", 2: "fixed table capacity exceeded",
                  4: "more than 128 device-drawn events in a gamete", 8: "tape parent index out of range",
                  16: "tape mutation row out of range", 32: "mutation capacity exceeded",
-                 64: "all fitness values zero", 128: "asynchronous copy wait expired"}
+                 64: "all fitness values zero", 128: "a parent strand copy outlived the wait limit",
+                 256: "a parent strand copy never landed (rows left unfinished)"}
 
 
 class ClothoError(RuntimeError):
@@ -222,6 +223,10 @@ class Population:
         i = capi.Info()
         self._ck(self.L.clotho_info_wait(self.h, ticket, C.byref(i)), "info_wait")
         return {n: getattr(i, n) for n, _ in capi.Info._fields_}
+
+    def set_copy_wait_limit(self, rounds: int):
+        """try_wait rounds a copy row's bulk copy may take before the STALL flag is raised (0: default)."""
+        self._ck(self.L.clotho_set_copy_wait_limit(self.h, rounds), "set_copy_wait_limit")
 
     def check(self):
         err = self.info()["device_error"]

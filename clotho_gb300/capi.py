@@ -112,6 +112,7 @@ SIGNATURES = {
     "clotho_batch_generation_philox": (C.c_int, [vp, vp]),
     "clotho_batch_run_philox": (C.c_int, [vp, vp, u32]),
     "clotho_set_rows_per_item": (C.c_int, [vp, u32]),
+    "clotho_set_copy_wait_limit": (C.c_int, [vp, u32]),
     "clotho_mem_info": (C.c_int, [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     "clotho_free_space_noalloc": (C.c_int, [vp, u32, u32, u32, vp, vp, vp]),
     "clotho_host_free": (C.c_int, [vp]),

@@ -120,6 +120,7 @@ struct clotho_ctx {
     std::vector<uint32_t> graph_key;
     bool in_step = false;
     uint32_t maxW = 0, maxS = 0, maxN = 0, maxNB = 0, maxA = 0;
+    cudaError_t launch_err = cudaSuccess;  // a launch set-up failure, reported by the next check_launch
 };
 
 namespace {
@@ -177,6 +178,10 @@ cudaError_t pool_alloc(clotho_ctx* ctx, T** p, size_t bytes) {
 
 int check_launch(clotho_ctx* ctx, const char* what) {
     cudaError_t e = cudaGetLastError();
+    if (ctx->launch_err != cudaSuccess) {
+        e = ctx->launch_err;
+        ctx->launch_err = cudaSuccess;
+    }
     if (e != cudaSuccess) return fail(ctx, CLOTHO_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
     return 0;
 }
@@ -333,8 +338,9 @@ void launch_gen(clotho_ctx* ctx, const PopDev* pops, uint32_t npops, uint32_t fu
         ctx->launches += 6;  // order count, 3-kernel scan, order scatter, plan
     }
     prof_begin(ctx);
-    launch_generation(cfg(ctx), pops, npops, ctx->d_ctl, ctx->maxW, ctx->maxA, fuse,
-                      ctx->profiling ? (ctx->phase_clocks ? 2 : 1) : 0);
+    const cudaError_t e = launch_generation(cfg(ctx), pops, npops, ctx->d_ctl, ctx->maxW, ctx->maxA, fuse,
+                                            ctx->profiling ? (ctx->phase_clocks ? 2 : 1) : 0);
+    if (e != cudaSuccess && ctx->launch_err == cudaSuccess) ctx->launch_err = e;
     prof_end(ctx);
     ctx->launches += 1;
 }
@@ -410,6 +416,39 @@ void enqueue_fused_step(clotho_ctx* ctx, uint32_t set, bool philox) {
     // draws), individuals, 3-kernel prefix sum, end; launch_gen and ensure_parent_acc count their own
     ctx->launches += 19u + (philox ? 0u : 1u) + (ctx->maxA <= kSufMaxSlots ? 1u : 0u);
     for (PopHost* p : ctx->pops) p->acc_valid = true;
+}
+
+// Captures one fused device-drawn step as the context's graph, keyed by the sizes it serves (a graph
+// with the same key is reused).  Whatever fails between the start of the capture and the graph's
+// instantiation, the capture is ended and the partial graph discarded, so the stream stays usable.
+int capture_step_graph(clotho_ctx* ctx, const std::vector<uint32_t>& key) {
+    if (ctx->graph && ctx->graph_key == key) return 0;
+    if (ctx->graph) {
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+    }
+    ctx->graph_key.clear();
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const uint64_t l0 = ctx->launches;
+    enqueue_fused_step(ctx, 2, true);
+    ctx->graph_launches = ctx->launches - l0;
+    ctx->launches = l0;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && ctx->launch_err != cudaSuccess) e = ctx->launch_err;
+    ctx->launch_err = cudaSuccess;
+    cudaGraph_t gr = nullptr;
+    const cudaError_t e_end = cudaStreamEndCapture(ctx->stream, &gr);  // ends the capture in every case
+    if (e == cudaSuccess) e = e_end;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&ctx->graph, gr, 0);
+    if (gr) cudaGraphDestroy(gr);
+    if (e != cudaSuccess) {
+        ctx->graph = nullptr;
+        cudaGetLastError();
+        return fail(ctx, CLOTHO_E_CUDA, std::string("graph capture of a generation: ") + cudaGetErrorString(e));
+    }
+    ctx->graph_key = key;
+    return 0;
 }
 
 }  // namespace
@@ -755,20 +794,7 @@ int clotho_run_philox(clotho_ctx* ctx, uint32_t N, uint32_t G) {
         return 0;
     }
     const std::vector<uint32_t> key(ctx->pops.size(), N);
-    if (!ctx->graph || ctx->graph_key != key) {
-        if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
-        cudaGraph_t gr;
-        CK(cudaStreamSynchronize(ctx->stream));
-        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        const uint64_t l0 = ctx->launches;
-        enqueue_fused_step(ctx, 2, true);
-        ctx->graph_launches = ctx->launches - l0;
-        ctx->launches = l0;
-        CK(cudaStreamEndCapture(ctx->stream, &gr));
-        CK(cudaGraphInstantiate(&ctx->graph, gr, 0));
-        cudaGraphDestroy(gr);
-        ctx->graph_key = key;
-    }
+    if ((rc = capture_step_graph(ctx, key))) return rc;
     for (uint32_t g = 1; g < G; ++g) {
         CK(cudaGraphLaunch(ctx->graph, ctx->stream));
         ctx->launches += ctx->graph_launches;
@@ -1358,10 +1384,49 @@ int clotho_restore(clotho_ctx* ctx, const void* src, size_t len) {
         return fail(ctx, CLOTHO_E_ARG, "snapshot parameters differ from the context's");
     if (st.N > D.Ncap || st.A > D.Acap || st.W > D.Wcap || st.fixed_total > D.FXcap || st.free_cnt > D.Acap)
         return fail(ctx, CLOTHO_E_CAPACITY, "snapshot does not fit the context's capacities");
-    int rc = init_pop(ctx, 0, st.N);  // zeroed tables and counters
-    if (rc) return rc;
     const char* b = static_cast<const char*>(src);
     const size_t S = 2ull * st.N, F = st.fixed_total;
+    // Everything below reaches device kernels as an index or a count: check it here, on the host, so a
+    // damaged or hand-edited snapshot is refused instead of sending a kernel out of bounds.
+    {
+        if ((uint64_t)st.fixed_cnt + st.lost_cnt != st.free_cnt)
+            return fail(ctx, CLOTHO_E_ARG, "snapshot free-list counts are inconsistent");
+        std::vector<uint32_t> fl(st.free_cnt);
+        if (st.free_cnt) std::memcpy(fl.data(), b + L.free_list, fl.size() * 4);
+        for (uint32_t v : fl)
+            if (v >= st.W * 64u) return fail(ctx, CLOTHO_E_ARG, "snapshot free list holds a slot beyond the rows");
+        std::vector<double> pos(st.A);
+        if (st.A) std::memcpy(pos.data(), b + L.pos, pos.size() * 8);
+        for (double x : pos)
+            if (!(x >= 0.0) || !std::isfinite(x)) return fail(ctx, CLOTHO_E_ARG, "snapshot allele position invalid");
+        std::vector<float> eff((size_t)st.A * 4);
+        if (st.A) std::memcpy(eff.data(), b + L.eff, eff.size() * 4);
+        int64_t nz = 0;
+        for (size_t a = 0; a < st.A; ++a)
+            for (uint32_t t = 0; t < 4; ++t) {
+                if (t >= D.T && eff[a * 4 + t] != 0.0f)
+                    return fail(ctx, CLOTHO_E_ARG, "snapshot effects of unused traits are not zero");
+                nz += eff[a * 4 + t] != 0.0f;
+            }
+        if (nz != st.nz_eff) return fail(ctx, CLOTHO_E_ARG, "snapshot effect count is inconsistent");
+        // no row carries a slot at or beyond A (the reference never sets one; the classifiers index by slot)
+        const uint32_t tail = st.A % 64u, last = st.A / 64u;
+        if (st.W && (tail || last < st.W))
+            for (size_t r = 0; r < S; ++r) {
+                const uint64_t* row = reinterpret_cast<const uint64_t*>(b + L.rows) + r * st.W;
+                uint64_t beyond = 0;
+                std::memcpy(&beyond, row + last, last < st.W ? 8 : 0);
+                if (tail) beyond &= ~((1ull << tail) - 1ull);
+                for (uint32_t w = last + 1; w < st.W; ++w) {
+                    uint64_t x;
+                    std::memcpy(&x, row + w, 8);
+                    beyond |= x;
+                }
+                if (beyond) return fail(ctx, CLOTHO_E_ARG, "snapshot rows carry slots beyond the allele count");
+            }
+    }
+    int rc = init_pop(ctx, 0, st.N);  // zeroed tables and counters
+    if (rc) return rc;
     cudaStream_t s = ctx->stream;
     CK(cudaMemcpyAsync(D.st, &st, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
     if (S * st.W)
@@ -1566,21 +1631,8 @@ int clotho_batch_run_philox(clotho_ctx* ctx, const uint32_t* N, uint32_t G) {
             if ((rc = clotho_batch_generation_philox(ctx, N))) return rc;
         return 0;
     }
-    std::vector<uint32_t> key(N, N + ctx->pops.size());
-    if (!ctx->graph || ctx->graph_key != key) {
-        if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
-        cudaGraph_t gr;
-        CK(cudaStreamSynchronize(ctx->stream));
-        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        const uint64_t l0 = ctx->launches;
-        enqueue_fused_step(ctx, 2, true);
-        ctx->graph_launches = ctx->launches - l0;
-        ctx->launches = l0;
-        CK(cudaStreamEndCapture(ctx->stream, &gr));
-        CK(cudaGraphInstantiate(&ctx->graph, gr, 0));
-        cudaGraphDestroy(gr);
-        ctx->graph_key = key;
-    }
+    const std::vector<uint32_t> key(N, N + ctx->pops.size());
+    if ((rc = capture_step_graph(ctx, key))) return rc;
     for (uint32_t g = 1; g < G; ++g) {
         CK(cudaGraphLaunch(ctx->graph, ctx->stream));
         ctx->launches += ctx->graph_launches;
@@ -1610,40 +1662,40 @@ int clotho_run_philox_schedule(clotho_ctx* ctx, const uint32_t* N, uint32_t G) {
     }
     uint32_t* d_sched = nullptr;
     CK(pool_alloc(ctx, &d_sched, hdr.size() * 4));
-    CK(cudaMemcpyAsync(d_sched, hdr.data(), hdr.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-    // the first generation runs eagerly (it may need the parent reduction)
-    CK(cudaMemcpyAsync(ctx->d_hdr[2], d_sched, 8ull * n, cudaMemcpyDeviceToDevice, ctx->stream));
-    enqueue_fused_step(ctx, 2, true);
-    rc = check_launch(ctx, "run_philox_schedule");
-    if (!rc && G > 1) {
+    // every exit after the allocation goes through the one free below
+    auto body = [&]() -> int {
+        CK(cudaMemcpyAsync(d_sched, hdr.data(), hdr.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+        // the first generation runs eagerly (it may need the parent reduction)
+        CK(cudaMemcpyAsync(ctx->d_hdr[2], d_sched, 8ull * n, cudaMemcpyDeviceToDevice, ctx->stream));
+        enqueue_fused_step(ctx, 2, true);
+        int r = check_launch(ctx, "run_philox_schedule");
+        if (r || G == 1) return r;
         // every size of a step is read from the device status word, so one graph
         // serves all generations; only the step header changes between replays
-        const std::vector<uint32_t> key{0xffffffffu, n};
-        if (!ctx->graph || ctx->graph_key != key) {
-            if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
-            cudaGraph_t gr;
-            CK(cudaStreamSynchronize(ctx->stream));
-            CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-            const uint64_t l0 = ctx->launches;
-            enqueue_fused_step(ctx, 2, true);
-            ctx->graph_launches = ctx->launches - l0;
-            ctx->launches = l0;
-            CK(cudaStreamEndCapture(ctx->stream, &gr));
-            CK(cudaGraphInstantiate(&ctx->graph, gr, 0));
-            cudaGraphDestroy(gr);
-            ctx->graph_key = key;
-        }
+        if ((r = capture_step_graph(ctx, std::vector<uint32_t>{0xffffffffu, n}))) return r;
         for (uint32_t g = 1; g < G; ++g) {
             CK(cudaMemcpyAsync(ctx->d_hdr[2], d_sched + 2ull * n * g, 8ull * n, cudaMemcpyDeviceToDevice,
                                ctx->stream));
             CK(cudaGraphLaunch(ctx->graph, ctx->stream));
             ctx->launches += ctx->graph_launches;
         }
-    }
-    CK(cudaFreeAsync(d_sched, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+        return 0;
+    };
+    rc = body();
+    const cudaError_t e_free = cudaFreeAsync(d_sched, ctx->stream);
+    const cudaError_t e_sync = cudaStreamSynchronize(ctx->stream);
     if (rc) return rc;
+    CK(e_free);
+    CK(e_sync);
     for (uint32_t i = 0; i < n; ++i) ctx->pops[i]->hostN = N[(size_t)(G - 1) * n + i];
+    return 0;
+}
+
+int clotho_set_copy_wait_limit(clotho_ctx* ctx, uint32_t rounds) {
+    if (!ctx) return CLOTHO_E_ARG;
+    if (rounds > (1u << 30)) return fail(ctx, CLOTHO_E_ARG, "wait limit above 2^30 rounds");
+    CK(cudaMemcpyAsync(&ctx->d_ctl->wait_limit, &rounds, sizeof(rounds), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     return 0;
 }
 

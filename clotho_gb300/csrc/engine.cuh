@@ -25,7 +25,7 @@ constexpr uint32_t kSufMaxSlots = 65536;   // allele capacity up to which the su
 
 // sticky device error bits (CLOTHO_DEVERR_* in clotho_gpu.h)
 constexpr uint32_t kErrAlleles = 1u, kErrFixed = 2u, kErrEvents = 4u, kErrParent = 8u,
-                   kErrSeq = 16u, kErrMut = 32u, kErrFitness = 64u, kErrStall = 128u;
+                   kErrSeq = 16u, kErrMut = 32u, kErrFitness = 64u, kErrStall = 128u, kErrAbandon = 256u;
 
 enum Mode : uint32_t { kModeTape = 0, kModePhilox = 1 };
 
@@ -117,7 +117,7 @@ struct WorkCtl {
     uint32_t gen_counter;           // dynamic item counter of k_generation
     uint32_t gen_items;             // total items
     uint32_t rows_per_item;         // scheduling granularity (set by the host)
-    uint32_t pad;
+    uint32_t wait_limit;            // try_wait rounds before a bulk copy is flagged late (0: default)
     uint32_t item_base[257];        // item prefix per population (<= 256 pops)
     uint64_t rows_done;             // profiling: rows processed
     uint64_t words_done;            // profiling: words written
@@ -281,8 +281,8 @@ void launch_mut_csr_tape(const LaunchCfg&, const PopDev* pops, uint32_t npops, u
 void launch_mut_counts_philox(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
 void launch_mut_resolve(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_select_philox(const LaunchCfg&, const PopDev* pops, uint32_t npops);
-void launch_generation(const LaunchCfg&, const PopDev* pops, uint32_t npops, WorkCtl* ctl,
-                       uint32_t maxW, uint32_t maxA, uint32_t fuse, int profile);
+cudaError_t launch_generation(const LaunchCfg&, const PopDev* pops, uint32_t npops, WorkCtl* ctl,
+                              uint32_t maxW, uint32_t maxA, uint32_t fuse, int profile);
 void launch_mut_scatter(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_phenotype(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_individuals(const LaunchCfg&, const PopDev* pops, uint32_t npops);

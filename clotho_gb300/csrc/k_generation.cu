@@ -45,9 +45,13 @@
 // items of rows, which its warps claim one at a time.
 #include "engine.cuh"
 
+#include <mutex>
+
 namespace clotho {
 
 namespace {
+
+constexpr int kMaxGenDevices = 64;
 
 // Rare paths: inlined (measured faster than out-of-line calls for this kernel).
 #define CLOTHO_COLD __forceinline__
@@ -335,7 +339,8 @@ __device__ __forceinline__ void row_phenotype(const PopDev& P, const DevStatus& 
 struct WarpSmem {
     uint32_t q[kQueueCap];            // effect queue: slot | sign << 31
     unsigned long long mbar;          // completion barrier of the warp's bulk copies
-    unsigned long long pad;
+    uint32_t dead;                    // a bulk copy of this warp never landed: it does no further row
+    uint32_t pad;
 };
 
 // Copy rows: 1 = one bulk copy of the parent strand into the warp's bitmap,
@@ -369,19 +374,42 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
 }
-constexpr uint32_t kWaitLimit = 1u << 22;   // try_wait rounds before a copy is given up
+constexpr uint32_t kWaitLimit = 1u << 22;   // default try_wait rounds before a copy is flagged late
 
-// Waits for the phase of the warp's barrier; false (and a sticky error bit) if it did not complete.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t& phase, uint32_t* err) {
-    uint32_t it = 0;
-    while (!mbar_try_wait(bar, phase)) {
-        if (++it >= kWaitLimit) {
-            if ((threadIdx.x & 31u) == 0) atomicOr(err, kErrStall);
-            return false;
+__device__ __forceinline__ bool mbar_test_wait(unsigned long long* bar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the phase of the warp's barrier.  Round 1 is a probe that does not wait (test_wait),
+// later rounds are try_waits.  A copy still in flight after `limit` unsuccessful rounds sets
+// kErrStall and is waited for kWaitLimit rounds more, so its buffer is never touched while the copy
+// can still land; if it has not landed by then, kErrAbandon is set and the result is false (the
+// whole warp agrees).  No wait is unbounded.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t& phase, uint32_t* err,
+                                          const uint32_t* wait_limit) {
+    bool ok = true;
+    if (!mbar_test_wait(bar, phase)) {
+        // the limit is read only here, off the path of copies that have landed by the first probe
+        const uint32_t lim = *wait_limit, limit = lim ? lim : kWaitLimit;
+        for (uint32_t it = 1;; ++it) {
+            if (it == limit) atomicOr(err, kErrStall);
+            if (it >= limit + kWaitLimit) {
+                atomicOr(err, kErrAbandon);
+                ok = false;
+                break;
+            }
+            if (mbar_try_wait(bar, phase)) break;
         }
     }
-    phase ^= 1u;
-    return true;
+    ok = __all_sync(0xffffffffu, ok);
+    if (ok) phase ^= 1u;
+    return ok;
 }
 
 __device__ __forceinline__ void add4(float (&d)[kMaxTraits], const float4& e) {
@@ -611,10 +639,12 @@ __device__ __forceinline__ void row_body_copy_direct(const PopDev& P, uint32_t M
 // Copy rows through a bulk copy: the whole parent strand (<= 8 KB) lands in
 // the warp's (otherwise idle) bitmap in one asynchronous transfer, then the
 // lanes mask, mutate, store and fold it, and clear the bitmap behind them.
-__device__ __forceinline__ void row_body_copy_bulk(const PopDev& P, uint32_t M, const RowArgs& R,
+// false: the strand's copy never landed (kErrAbandon); the row is written without it and the warp
+// must not use its bitmap again, since the copy may still land there.
+__device__ __forceinline__ bool row_body_copy_bulk(const PopDev& P, uint32_t M, const RowArgs& R,
                                                    const uint64_t* sfix, uint64_t* buf, unsigned long long* bar,
-                                                   uint32_t& phase, bool do_mut, bool do_fs, uint64_t* sF,
-                                                   uint64_t* sV) {
+                                                   uint32_t& phase, const uint32_t* wait_limit, bool do_mut,
+                                                   bool do_fs, uint64_t* sF, uint64_t* sV) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t bytes = R.Wp * 8u;
     bool ok = true;
@@ -628,7 +658,7 @@ __device__ __forceinline__ void row_body_copy_bulk(const PopDev& P, uint32_t M, 
         if (off < bytes)
             bulk_load(reinterpret_cast<char*>(buf) + off, reinterpret_cast<const char*>(R.top) + off,
                       min(2048u, bytes - off), bar);
-        ok = mbar_wait(bar, phase, &P.st->err);
+        ok = mbar_wait(bar, phase, &P.st->err, wait_limit);
     }
     for (uint32_t w0 = 0; w0 < R.Wc; w0 += 64u) {
         const uint32_t w = w0 + 2u * lane;
@@ -648,6 +678,7 @@ __device__ __forceinline__ void row_body_copy_bulk(const PopDev& P, uint32_t M, 
         }
     }
     __syncwarp();
+    return ok;
 }
 
 // Crossover rows.  MODE 0: switch mask from the warp's mask bitmap; MODE 1:
@@ -751,10 +782,12 @@ struct PhaseClk {
 // One offspring row, the whole warp (suffix-table classifier), from the plan
 // at processing position v (k_row_plan): row, top strand, breakpoints, table
 // rows and correction ranks.  PROF: clock the row's phases into pc.
+// Returns false when the row's bulk copy was abandoned (the warp then stops working on rows).
 template <bool PROF, bool NARROW>
-__device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st, uint32_t v, const uint64_t* sfix,
-                                            uint64_t* mask, WarpSmem& ws, uint32_t& phase, bool do_mut, bool do_ph,
-                                            bool gather, bool do_fs, uint64_t* sF, uint64_t* sV, PhaseClk& pc) {
+__device__ __forceinline__ bool gen_row_suf(const PopDev& P, const DevStatus& st, uint32_t v, const uint64_t* sfix,
+                                            uint64_t* mask, WarpSmem& ws, uint32_t& phase,
+                                            const uint32_t* wait_limit, bool do_mut, bool do_ph, bool gather, bool do_fs, uint64_t* sF,
+                                            uint64_t* sV, PhaseClk& pc) {
     const uint32_t lane = threadIdx.x & 31u;
     const long long c0 = PROF ? clock64() : 0;
     long long c1 = 0, c2 = 0, c3 = 0;
@@ -780,6 +813,7 @@ __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st
     R.zbase = pz;  // z(inv ? bottom : top) - sum(fixed), from the plan
     float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
     row_mutation_setup(P, st, pm.x, pm.y, do_mut, gather, R, d);
+    bool landed = true;
     if (PROF) c1 = clock64();
     if (flags & kPlanLong) {
         add4(d, row_body_events(P, st.M, R, sfix, ws.q, do_mut, gather, do_fs, sF, sV));
@@ -788,7 +822,7 @@ __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st
         if (NARROW)
             row_body_copy_direct(P, st.M, R, sfix, do_mut, do_fs, sF, sV);
         else
-            row_body_copy_bulk(P, st.M, R, sfix, mask, &ws.mbar, phase, do_mut, do_fs, sF, sV);
+            landed = row_body_copy_bulk(P, st.M, R, sfix, mask, &ws.mbar, phase, wait_limit, do_mut, do_fs, sF, sV);
 #else
         row_body_copy(P, st.M, R, sfix, do_mut, do_fs, sF, sV);
 #endif
@@ -903,6 +937,7 @@ __device__ __forceinline__ void gen_row_suf(const PopDev& P, const DevStatus& st
             pc.c[kPhXoPheno] += c4 - c3;
         }
     }
+    return landed;
 }
 
 // ---------------------------------------------------------------------------
@@ -1190,9 +1225,13 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     uint64_t* mask = s_dyn + (3u + (SUF ? warp : 0u)) * maxW;
     WarpSmem& ws = reinterpret_cast<WarpSmem*>(s_dyn + (3u + kWarps) * maxW)[SUF ? warp : 0u];
     uint32_t bphase = 0;  // parity of the warp's bulk-copy barrier
+    const uint32_t* wait_limit = &ctl->wait_limit;  // read only when a copy is late
     if (SUF) {
         for (uint32_t w = lane; w < maxW; w += 32u) mask[w] = 0ull;
-        if (lane == 0) mbar_init(&ws.mbar);
+        if (lane == 0) {
+            mbar_init(&ws.mbar);
+            ws.dead = 0u;
+        }
         __syncwarp();
     }
     const bool do_mut = (fuse & kFuseMut) != 0, do_ph = (fuse & kFusePheno) != 0, do_fs = (fuse & kFuseFs) != 0;
@@ -1232,13 +1271,18 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             const uint32_t k1 = min(S, k + kWarpChunk);
             for (uint32_t v = k; v < k1; ++v) {
                 const uint32_t g = v < Se ? 2u * v : 2u * (v - Se) + 1u;
-                if (SUF)
-                    gen_row_suf<PROF, NARROW>(P, st, v, sfix, mask, ws, bphase, do_mut, do_ph, gather, do_fs, sF, sV, pc);
-                else
+                if (SUF) {
+                    if (!gen_row_suf<PROF, NARROW>(P, st, v, sfix, mask, ws, bphase, wait_limit, do_mut, do_ph,
+                                                   gather, do_fs, sF, sV, pc)) {
+                        ws.dead = 1u;
+                        break;
+                    }
+                } else
                     gen_row_iv(P, st, g, sfix, s_iv[warp], s_thr[warp], s_q[warp], s_sm[warp], do_mut, do_ph,
                                gather, do_fs, sF, sV);
                 if (profile && lane == 0) { rows_done += 1; words_done += st.W; }
             }
+            if (SUF && ws.dead) break;  // no further row: the warp leaves the loop
         }
     }
     for (; npops > 1;) {
@@ -1316,9 +1360,14 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             // rule), so a CTA runs one kind of row at a time; the suffix-table
             // path takes its rows in plan order
             const uint32_t g = v < Se ? 2u * v : 2u * (v - Se) + 1u;
-            if (SUF)
-                gen_row_suf<PROF, NARROW>(P, st, v, sfix, mask, ws, bphase, do_mut, do_ph, gather, do_fs, sF, sV, pc);
-            else
+            if (SUF) {
+                // a warp whose copy never landed keeps taking its rows (leaving them undone) and the
+                // block's barriers
+                if (ws.dead) continue;
+                if (!gen_row_suf<PROF, NARROW>(P, st, v, sfix, mask, ws, bphase, wait_limit, do_mut, do_ph, gather,
+                                               do_fs, sF, sV, pc))
+                    ws.dead = 1u;
+            } else
                 gen_row_iv(P, st, g, sfix, s_iv[warp], s_thr[warp], s_q[warp], s_sm[warp], do_mut, do_ph, gather,
                            do_fs, sF, sV);
             if (profile && lane == 0) { rows_done += 1; words_done += st.W; }
@@ -1346,9 +1395,10 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
 }
 
 // The suffix-table classifier runs when every population has a table
-// (capacity <= kSufMaxSlots slots, so maxW <= 1,024 words).
-void launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, WorkCtl* ctl, uint32_t maxW,
-                       uint32_t maxA, uint32_t fuse, int profile) {
+// (capacity <= kSufMaxSlots slots, so maxW <= 1,024 words).  Returns the error of
+// the shared-memory opt-in (the kernel is not launched then), else cudaSuccess.
+cudaError_t launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, WorkCtl* ctl, uint32_t maxW,
+                              uint32_t maxA, uint32_t fuse, int profile) {
     const bool suf = maxA <= kSufMaxSlots;
     // the interval classifier keeps 3.5 KB of static shared memory per warp
     const uint32_t gacc = (!suf && 3ull * maxW * sizeof(uint64_t) + kWarps * 3584u > 220u * 1024u) ? 1u : 0u;
@@ -1356,16 +1406,27 @@ void launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, W
         gacc ? 0 : (3ull + (suf ? kWarps : 0u)) * maxW * sizeof(uint64_t) + (suf ? kWarps * sizeof(WarpSmem) : 0);
     // profile 2: the suffix-table kernel's build with phase clocks; rows of at most
     // 128 words: its narrow build (copy rows by direct loads)
-    static size_t configured[5] = {0, 0, 0, 0, 0};
     const bool narrow = maxW <= 64u * kDirectCopyChunks;
     const int si = suf ? (profile == 2 ? (narrow ? 4 : 2) : narrow ? 3 : 1) : 0;
     const void* fns[5] = {(const void*)k_generation<false, false, false>, (const void*)k_generation<true, false, false>,
                           (const void*)k_generation<true, true, false>, (const void*)k_generation<true, false, true>,
                           (const void*)k_generation<true, true, true>};
-    // static shared memory is above 48 KB on its own, so the opt-in attribute is always needed
-    if (smem > configured[si] || configured[si] == 0) {
-        cudaFuncSetAttribute(fns[si], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        configured[si] = smem > 0 ? smem : 1;
+    // static shared memory is above 48 KB on its own, so the opt-in attribute is always needed; it is a
+    // property of the function on each device, so it is kept per device (host threads share the table)
+    {
+        static std::mutex mu;
+        static size_t configured[kMaxGenDevices][5] = {};
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        if (dev < 0 || dev >= kMaxGenDevices) return cudaErrorInvalidDevice;
+        std::lock_guard<std::mutex> lock(mu);
+        size_t& c = configured[dev][si];
+        if (smem > c || c == 0) {
+            e = cudaFuncSetAttribute(fns[si], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            c = smem > 0 ? smem : 1;
+        }
     }
     if (si == 4)
         k_generation<true, true, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
@@ -1382,6 +1443,7 @@ void launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, W
     else
         k_generation<false, false, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
                                                                                      maxW, gacc);
+    return cudaSuccess;
 }
 
 // ---------------------------------------------------------------------------

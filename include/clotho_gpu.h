@@ -119,7 +119,12 @@ typedef struct clotho_info {
 #define CLOTHO_DEVERR_SEQ     16u   /* tape mutation row out of range         */
 #define CLOTHO_DEVERR_MUT     32u   /* mutation capacity exceeded             */
 #define CLOTHO_DEVERR_FITNESS 64u   /* all fitness zero: uniform selection used */
-#define CLOTHO_DEVERR_STALL  128u   /* an asynchronous copy did not complete in time (row left unfinished) */
+#define CLOTHO_DEVERR_STALL  128u   /* a parent strand's asynchronous copy outlived the wait limit
+                                       (clotho_set_copy_wait_limit); the warp kept waiting for it, so
+                                       the row is complete unless CLOTHO_DEVERR_ABANDONED is also set */
+#define CLOTHO_DEVERR_ABANDONED 256u /* such a copy had still not landed after 2^22 more rounds: its
+                                       row was written without the parent strand and that warp did no
+                                       further rows (the generation is invalid) */
 
 /* ---- lifetime ---------------------------------------------------------- */
 int  clotho_create(const clotho_desc *desc, clotho_ctx **out);
@@ -333,6 +338,13 @@ int  clotho_batch_run_philox(clotho_ctx *ctx, const uint32_t *N, uint32_t G);
  * the device once and each replay reads its own.  Works on single-population
  * and batched contexts. */
 int  clotho_run_philox_schedule(clotho_ctx *ctx, const uint32_t *N, uint32_t G);
+/* Rounds of mbarrier try_wait a copy row's bulk copy of its parent strand may
+ * take before CLOTHO_DEVERR_STALL is raised (0 = the default, 2^22; at most
+ * 2^30).  The warp keeps waiting for the copy after that, 2^22 rounds more at
+ * most, before it touches the copy's buffer.  A diagnostic knob: a limit of 1
+ * makes the flag fire on ordinary copies without changing any result.  No
+ * reference counterpart (the reference has no asynchronous copies). */
+int  clotho_set_copy_wait_limit(clotho_ctx *ctx, uint32_t rounds);
 /* Rows per scheduling item of the generation kernel (autotuner knob of
  * batched contexts; a single-population context has its warps claim one row
  * at a time and ignores it). */
@@ -354,7 +366,11 @@ int  clotho_mem_info(size_t *free_bytes, size_t *total_bytes);
  * At most 16,384 words per row (A <= 1,048,576); larger A returns
  * CLOTHO_E_CAPACITY.  The fixed array (256 KB) stays on every device that
  * loaded the library until the process exits.  The first call on a device
- * looks up the array's address; make it before any stream capture.  All calls
+ * looks up the array's address; make it before any stream capture (inside a
+ * capture it returns CLOTHO_E_STATE).  Calls on a stream that is not
+ * capturing look the address up again, so a context made after
+ * cudaDeviceReset is followed.  S = 0 reads every slot of every word as
+ * lost, as the reference's analysis of an empty population does.  All calls
  * share the array: calls that overlap on the GPU race, so order them on one
  * stream.  Work is enqueued on `stream`; results are ready when it completes. */
 int  clotho_free_space_noalloc(const uint64_t *rows, uint32_t S, uint32_t row_stride_words, uint32_t A,

@@ -308,3 +308,54 @@ def test_a_qtlsim_configuration_runs_end_to_end():
     assert i["device_error"] == 0 and i["N"] == rc.sizes()[-1] and i["generation"] == 13
     assert pop.stats(16)["segregating"] > 0
     pop.close()
+
+
+def _snapshot_offsets(snap):
+    """Offsets of the status fields and of the free list, positions and rows inside a snapshot."""
+    import struct
+    header_bytes = struct.unpack_from("<I", snap, 12)[0]
+    assert struct.unpack_from("<Q", snap, header_bytes - 8)[0] == len(snap)   # total_bytes ends the header
+    st = 16 + 96                                                                # after magic, versions, desc
+    T = struct.unpack_from("<I", snap, 16 + 8)[0]
+    N, A, W = struct.unpack_from("<3I", snap, st + 8)
+    free_cnt, fixed_total = struct.unpack_from("<2I", snap, st + 44)
+
+    def r8(b):
+        return (b + 7) & ~7
+    o = {"rows": header_bytes}
+    o["pos"] = o["rows"] + r8(2 * N * W * 8)
+    o["free"] = o["pos"] + r8(A * 8) + r8(A * 4) + r8(A * 16) + r8(fixed_total * 8) + r8(fixed_total * 4) + \
+        r8(fixed_total * T * 4)
+    return dict(N=N, A=A, W=W, free_cnt=free_cnt), o
+
+
+def test_restore_refuses_snapshots_whose_indices_leave_the_population():
+    # a damaged or hand-edited snapshot is refused on the host, before any of its indices reach a
+    # kernel: a free-list slot beyond the rows, a NaN allele position, a row bit at or beyond the
+    # allele count
+    import struct
+    N = 300
+    a = cg.Population(N, 4096, 2, **KW)
+    a.init(N)
+    a.run_philox(N, 8)
+    snap = a.snapshot()
+    f, o = _snapshot_offsets(snap)
+    assert f["free_cnt"] > 0 and f["A"] < f["W"] * 64
+    same = cg.Population(N, 4096, 2, **KW)
+    bad = bytearray(snap)
+    struct.pack_into("<I", bad, o["free"], f["W"] * 64 + 3)
+    with pytest.raises(cg.ClothoError, match="free list"):
+        same.restore(bytes(bad))
+    bad = bytearray(snap)
+    struct.pack_into("<d", bad, o["pos"] + 8, float("nan"))
+    with pytest.raises(cg.ClothoError, match="position"):
+        same.restore(bytes(bad))
+    bad = bytearray(snap)
+    word = o["rows"] + 8 * (f["A"] // 64)                 # row 0, the word holding slot A
+    struct.pack_into("<Q", bad, word, struct.unpack_from("<Q", bad, word)[0] | (1 << (f["A"] % 64)))
+    with pytest.raises(cg.ClothoError, match="beyond the allele count"):
+        same.restore(bytes(bad))
+    same.restore(snap)
+    assert np.array_equal(same.rows(), a.rows())
+    a.close()
+    same.close()

@@ -157,3 +157,35 @@ def test_device_mutation_overflow_is_flagged_and_capped():
     gpu.simulate_philox(N)
     assert gpu.info()["generation"] == 3
     gpu.close()
+
+
+def test_copy_wait_limit_flags_late_copies_and_changes_no_result():
+    # copy rows of wide populations (rows above 128 words) receive their parent strand by bulk copy; with a
+    # wait limit of one round (a probe that does not wait) every such copy outlives the limit: the STALL
+    # bit is raised, the warps keep waiting for their copies, no copy is abandoned, and rows, phenotypes
+    # and fitness equal those of the same run with the default limit
+    rng = np.random.default_rng(3)
+    N, A = 300, 20_000
+    pos = rng.random(A)
+    eff = rng.standard_normal(A).astype(np.float32)
+    thr = (rng.random(A) * 0.2 * 2.0 ** 32).astype(np.uint32)
+    kw = dict(fitness="gaussian_vs", fit_param=4.0, mu=0.05, rho=1.0, p_neutral=0.0, seed=5,
+              max_events=1 << 14, max_mutations=1 << 12)
+    late = cg.Population(N, 32_768, 1, **kw)
+    ref = cg.Population(N, 32_768, 1, **kw)
+    for p in (late, ref):
+        p.seed_population(N, pos, eff, thr, 9)
+    assert late.info()["W"] > 128
+    late.set_copy_wait_limit(1)
+    late.run_philox(N, 4)
+    ref.run_philox(N, 4)
+    err = late.info()["device_error"]
+    assert err & 128, "a one-round limit must flag the copies"
+    assert not err & 256, "no copy may be abandoned"
+    assert ref.info()["device_error"] == 0
+    assert np.array_equal(late.rows(), ref.rows())
+    assert np.array_equal(late.phenotypes(), ref.phenotypes())
+    assert np.array_equal(late.fitness(), ref.fitness())
+    with pytest.raises(cg.ClothoError):
+        late.set_copy_wait_limit(1 << 31)
+    late.set_copy_wait_limit(0)
