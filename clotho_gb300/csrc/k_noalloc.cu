@@ -14,8 +14,10 @@
 //  * rows of at most kNoAllocMaxWords 64-bit words (A <= 1,048,576 alleles);
 //    larger widths are rejected with CLOTHO_E_CAPACITY;
 //  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (once per device, with that device current); make
-//    that first call before any stream capture;
+//    cudaGetSymbolAddress (with that device current); make that first call
+//    before any stream capture (inside a capture it returns CLOTHO_E_STATE).
+//    Later calls on a stream that is not capturing look it up again, so a
+//    context made after cudaDeviceReset is followed;
 //  * every call shares the one array and resets the accumulators it uses at
 //    its start, so calls that overlap on the GPU (different streams, or
 //    concurrent host threads without ordering) race: order them on one stream.
@@ -134,19 +136,28 @@ __global__ void __launch_bounds__(1024) k_na_compact(const unsigned long long* a
     }
 }
 
-// Device address of g_fs_scratch, looked up once per device.
+// Device address of g_fs_scratch, per device.  It is looked up on the first
+// call on a device and again on every call whose stream is not capturing, so
+// a context made anew after cudaDeviceReset (which loads the module at a new
+// address) is followed; a capturing stream uses the address found last.
 constexpr int kMaxDevices = 64;
 std::mutex g_na_mutex;
 void* g_na_addr[kMaxDevices] = {};
 
-int scratch_address(void** out) {
+int scratch_address(cudaStream_t stream, void** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         cudaGetLastError();
         return CLOTHO_E_CUDA;
     }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        cap = cudaStreamCaptureStatusActive;  // the legacy stream under another stream's global capture
+    }
     std::lock_guard<std::mutex> g(g_na_mutex);
-    if (!g_na_addr[dev]) {
+    if (!g_na_addr[dev] || cap == cudaStreamCaptureStatusNone) {
+        if (cap != cudaStreamCaptureStatusNone) return CLOTHO_E_STATE;  // first call inside a capture
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_fs_scratch) != cudaSuccess || !p) {
             cudaGetLastError();
@@ -169,6 +180,7 @@ extern "C" int clotho_free_space_noalloc(const uint64_t* rows, uint32_t S, uint3
     if (W > kNoAllocMaxWords) return CLOTHO_E_CAPACITY;
     if (S > 0 && W > 0 && (!rows || row_stride_words < W)) return CLOTHO_E_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaGetLastError();  // an error left by earlier, unrelated work is not this call's
     if (A == 0) {  // nothing to analyse (free_space_mt_population_space_row_interlaced.hpp:46)
         if (cudaMemsetAsync(counts, 0, 3 * sizeof(uint32_t), st) != cudaSuccess) {
             cudaGetLastError();
@@ -177,7 +189,7 @@ extern "C" int clotho_free_space_noalloc(const uint64_t* rows, uint32_t S, uint3
         return 0;
     }
     void* addr = nullptr;
-    int rc = scratch_address(&addr);
+    int rc = scratch_address(st, &addr);
     if (rc) return rc;
     unsigned long long* acc = static_cast<unsigned long long*>(addr);
     k_na_reset<<<(W + 255) / 256, 256, 0, st>>>(acc, W);

@@ -76,3 +76,34 @@ def test_noalloc_rejects_widths_beyond_its_array():
     dummy = C.c_void_p(16)   # never dereferenced: the size check fails first
     rc = L.clotho_free_space_noalloc(dummy, 2, 20000, 2_000_000, dummy, dummy, None)
     assert rc == -3  # CLOTHO_E_CAPACITY
+
+
+def test_noalloc_matches_the_oracle_including_an_empty_population():
+    # the same analysis against the CPU restatement directly (oracle.free_space), on rows with fixed,
+    # lost and padding columns, and on S = 0 rows, which the reference reads as every slot of every
+    # word lost (no row seeds the AND/OR, so the tail padding step never runs)
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+    torch = pytest.importorskip("torch")
+    import oracle
+    from clotho_gb300 import capi
+    L = capi.load()
+    rng = np.random.default_rng(29)
+    for S, A, fixed, lost in [(64, 700, [3, 699], [0, 640]), (0, 700, [], []), (0, 64, [], []),
+                              (2, 513, [512], [1])]:
+        rows, W = _rows(rng, max(S, 1), A, fixed, lost)
+        rows = rows[:S]
+        want, nfix, nlost = oracle.free_space(rows.reshape(S, W), A)
+        d_rows = torch.from_numpy(np.ascontiguousarray(rows).view(np.int64).reshape(-1)).cuda() if S else None
+        d_free = torch.full((W * 64,), -1, dtype=torch.int32, device="cuda")
+        d_counts = torch.full((3,), -1, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        rc = L.clotho_free_space_noalloc(C.c_void_p(d_rows.data_ptr()) if S else None, S, W, A,
+                                         C.c_void_p(d_free.data_ptr()), C.c_void_p(d_counts.data_ptr()), None)
+        torch.cuda.synchronize()
+        assert rc == 0
+        counts = d_counts.cpu().numpy().astype(np.int64)
+        assert list(counts) == [nfix, nlost, nfix + nlost], (S, A)
+        assert np.array_equal(d_free.cpu().numpy()[:nfix + nlost].astype(np.uint32), want), (S, A)
+        if S == 0:
+            assert nfix == 0 and nlost == W * 64
