@@ -17,8 +17,10 @@ generation (free space, selection, crossover, mutation, phenotype, fitness).
   cpu_baseline  the CPU oracle (restatement of the reference's path) on the
            host cores, on a bounded sample of the same workload.
 
---impl reference times that CPU restatement alone: the reference's own engine
-needs Boost (every hot-path header includes it), which this image lacks.
+--impl reference times that CPU restatement alone, on this arm's configuration
+(N=1e6, all host threads), with the single-core rate beside it: the
+reference's own engine needs Boost (every hot-path header includes it), which
+this image lacks.
 """
 from __future__ import annotations
 
@@ -38,7 +40,9 @@ sys.path.insert(0, ROOT)
 METRIC = "sequence-generations/s at N=1e6 (HBM % peak)"
 UNIT = "seq-gen/s"
 FALLBACK_HBM_GBS = 6800.0
-CPU_SAMPLE_N = 20_000
+CPU_SAMPLE_N = 20_000     # single-core sample (individuals)
+CPU_LEG_N = 100_000       # all-cores sample of the in-line CPU leg (individuals)
+REF_N = None              # individuals of the reference arm (None: the workload's own N)
 
 
 def parse():
@@ -279,23 +283,43 @@ def batched_and_serving():
     return batched, serve
 
 
+def single_core_rate(w, warmup=1, steps=2, N=None):
+    """The reference's default thread count is the master thread alone (T=0,
+    thread_count_parameter.hpp:22): the oracle on one core over a bounded sample
+    of the workload (N=CPU_SAMPLE_N individuals, the same allele load and row
+    width; the per-row cost does not depend on N)."""
+    N = N or CPU_SAMPLE_N
+    v, dt, info, _ = run_cpu_oracle(w, N, steps, warmup, 1)
+    return {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": (f"oracle/clotho_oracle.cpp on 1 thread (the reference's default T=0), N={N} "
+                       f"individuals, same allele load (A={info['A']}, W={info['B']} words/row), {steps} "
+                       f"generations after {warmup} warm-up, {dt:.1f} s")}
+
+
 def reference_arm(args, rank):
+    """The reference's CPU path (its restatement, oracle/clotho_oracle.cpp: the reference itself needs Boost,
+    absent here) on this arm's own configuration: N=1e6 individuals with the same pre-seeded allele load,
+    every host thread, K generations after W warm-up; beside it the single-core rate."""
     from clotho_gb300.workloads import LARGE_N
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    N = CPU_SAMPLE_N
-    v, dt, info, stages = run_cpu_oracle(LARGE_N, N, args.steps, args.warmup, threads)
-    sample = (f"CPU restatement of the reference path (oracle/clotho_oracle.cpp), N={N} individuals "
-              f"({2 * N} rows) with the same pre-seeded allele load (A={info['A']}, W={info['B']} words/row), "
-              f"{args.steps} generations after {args.warmup} warm-up")
+    w = LARGE_N
+    N = REF_N or getattr(args, "n", None) or w.N
+    t_setup = time.perf_counter()
+    v, dt, info, stages = run_cpu_oracle(w, N, args.steps, args.warmup, threads)
+    t_setup = time.perf_counter() - t_setup - dt
+    sample = (f"CPU restatement of the reference path (oracle/clotho_oracle.cpp) on {threads} host threads, the "
+              f"full workload: N={N} individuals ({2 * N} rows), pre-seeded allele load (A={info['A']}, "
+              f"W={info['B']} words/row), {args.steps} generations after {args.warmup} warm-up")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-            "config": {"workload": LARGE_N.name, "N_sample": N, "T": LARGE_N.T, "rho": LARGE_N.rho,
-                       "mu": LARGE_N.mu, "threads": threads},
+            "config": {"workload": w.name, "N": N, "T": w.T, "A": info["A"], "W_live": info["B"], "rho": w.rho,
+                       "mu": w.mu, "fitness": w.fitness, "threads": threads, "same_config": N == w.N},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
-                             "stage_seconds": stages},
+                             "stage_seconds": stages, "setup_seconds": t_setup},
+            "single_core": single_core_rate(w, N=min(CPU_SAMPLE_N, N)),
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -354,8 +378,30 @@ def batch_kernels(cg, warmup, steps):
             "max_row_words": max(b.info(i)["W"] for i in range(len(jobs)))}
 
 
+def free_port() -> int:
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        return sk.getsockname()[1]
+
+
+def relaunch_as_ranks(gpus: int) -> int:
+    """`bench.py --gpus N` started without a launcher: start its N replica processes (one per GPU) on this
+    node with the environment torchrun gives its ranks, and return the first nonzero exit status."""
+    port = str(free_port())
+    procs = []
+    for r in range(gpus):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(gpus), LOCAL_WORLD_SIZE=str(gpus),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=port)
+        procs.append(subprocess.Popen([sys.executable, os.path.abspath(__file__), *sys.argv[1:]], env=env))
+    codes = [p.wait() for p in procs]
+    return next((c for c in codes if c), 0)
+
+
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch_as_ranks(args.gpus))
     rank, world, local = dist_env()
     if args.impl == "reference":
         reference_arm(args, rank)
@@ -468,7 +514,9 @@ def main():
         e2e = {"value": 2.0 * N * args.steps * world / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": 80, "ms_per_step": 1e3 * dt / args.steps,
                "note": "tape call per generation (uniform-parent tape), wall clock around H2D + kernels + D2H; "
-                       "each step's status read is collected after the next step is issued"}
+                       "each step's status read is collected after the next step is issued; the two tapes are "
+                       "drawn on the host before the timed region and replayed, so host-side drawing of the "
+                       "tape (the reference's serial RNG draws) is not in this number"}
         for ptr in keep:
             cg.capi.load().clotho_host_free(ptr)
 
@@ -476,11 +524,12 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, dt, oinfo, stages = run_cpu_oracle(w, CPU_SAMPLE_N, 2, 0, threads)
+        v, dt, oinfo, stages = run_cpu_oracle(w, CPU_LEG_N, 4, 1, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": (f"oracle/clotho_oracle.cpp on {threads} host threads, N={CPU_SAMPLE_N} individuals, same "
-                          f"allele load (A={oinfo['A']}, W={oinfo['B']}), 2 generations, {dt:.1f} s"),
-               "stage_seconds": stages}
+               "sample": (f"oracle/clotho_oracle.cpp on {threads} host threads, N={CPU_LEG_N} individuals, same "
+                          f"allele load (A={oinfo['A']}, W={oinfo['B']}), 4 generations after 1 warm-up, "
+                          f"{dt:.1f} s"),
+               "stage_seconds": stages, "single_core": single_core_rate(w)}
 
     batched = serve = None
     if rank == 0 and world == 1 and not args.no_batched:

@@ -1,5 +1,5 @@
 """bench.py's output contract on CPU: the reference arm's JSON line (the CPU
-restatement timed on a small sample) carries every key the runner reads, other
+restatement, here timed on a small population) carries every key the runner reads, other
 ranks print nothing, and the clock sampler's parser flags throttle reasons."""
 import argparse
 import contextlib
@@ -18,7 +18,8 @@ KEYS = ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_
 
 
 def _run_reference(monkeypatch, rank):
-    monkeypatch.setattr(bench, "CPU_SAMPLE_N", 300)
+    monkeypatch.setattr(bench, "CPU_SAMPLE_N", 200)
+    monkeypatch.setattr(bench, "REF_N", 300)
     buf = io.StringIO()
     with contextlib.redirect_stdout(buf):
         bench.reference_arm(argparse.Namespace(gpus=1, steps=1, warmup=0), rank)
@@ -35,7 +36,9 @@ def test_reference_arm_line(monkeypatch):
     assert d["value"] > 0 and d["higher_is_better"] is True and d["steps"] == 1 and d["warmup"] == 0
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["unit"] == d["unit"]
-    assert "N=300" in cb["sample"]
+    assert "N=300" in cb["sample"] and d["config"]["N"] == 300
+    sc = d["single_core"]
+    assert sc["cores"] == 1 and sc["value"] > 0 and "N=200" in sc["sample"]
     e = d["e2e"]
     assert e == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["workload"].startswith("large_n")

@@ -51,3 +51,17 @@ def test_two_gloo_replicas():
         assert p.exitcode == 0
     assert [o[1] for o in out] == [3.0, 3.0]          # max over ranks
     assert all(o[2] for o in out) and all(o[3] == 200 for o in out)
+
+
+def test_bare_gpus_flag_starts_its_ranks():
+    # `bench.py --gpus 2` without an outer launcher starts two ranks itself; on the reference arm rank 0
+    # alone prints its line and the other rank exits 0 without work
+    import json
+    import subprocess
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2",
+                        "--n", "200", "--steps", "1", "--warmup", "0"], capture_output=True, text=True, timeout=300,
+                       env=env, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1 and lines[0]["impl"] == "reference" and lines[0]["config"]["N"] == 200
