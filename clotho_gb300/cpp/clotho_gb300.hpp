@@ -52,6 +52,17 @@ struct Parameters {
     uint64_t seed = 1;
 };
 
+// The generation the engine is about to run.  Mutation::generateNewMutation(2N) is the first stage of the
+// reference's sequence that knows the generation's size and new-mutation count
+// (engine_batched_task.hpp:166-175): it records them here; the first stage that needs the device (the
+// free-space analysis of the parent) begins the generation on the device with them, and the last stage
+// (fitness, :213) ends it.  The reference swaps its parent and child spaces by pointer (:164); the device
+// swaps its buffers when the generation begins.
+struct StepState {
+    bool pending = false, begun = false;
+    uint32_t N = 0, M = 0;
+};
+
 // Owns one resident population (clotho_ctx).
 class Context {
 public:
@@ -88,19 +99,177 @@ public:
         check(clotho_get_info(ctx_, &i), ctx_, "clotho_get_info");
         return i;
     }
+    StepState& step() { return step_; }
 
 private:
     Parameters p_;
     clotho_ctx* ctx_ = nullptr;
+    StepState step_;
+};
+
+// ---- The spaces.  The reference passes its population, allele and trait spaces to every policy by raw
+// pointer (population_space_row, AlleleSpace, trait_space_vector: engine_batched_task.hpp:84-95).  Here
+// they live on the device, inside one Context; these types are the host-side views the policies take, with
+// the reference's member names.  Host copies are read back on demand and dropped when the device state
+// changes.
+
+inline void begin_pending(Context* c) {
+    StepState& st = c->step();
+    if (st.begun) return;
+    if (!st.pending) throw Error("no generation pending: Mutation::generateNewMutation comes first");
+    check(clotho_begin_generation(c->get(), st.N, st.M), c->get(), "clotho_begin_generation");
+    st.begun = true;
+    st.pending = false;
+}
+inline void end_begun(Context* c) {
+    StepState& st = c->step();
+    if (!st.begun) return;
+    check(clotho_end_generation(c->get()), c->get(), "clotho_end_generation");
+    st.begun = false;
+}
+
+// population_space_row<uint64_t, double> (population_space_row_block.hpp:25-260): row i is haploid genome
+// i, individual j owns rows 2j and 2j+1.  Two views (the parent and child roles the engine swaps by
+// pointer) share one Context; between generations both read the rows of the last generation.
+class PopulationSpaceGPU {
+public:
+    typedef uint64_t block_type;
+    typedef double weight_type;
+    typedef const block_type* genome_iterator;
+
+    explicit PopulationSpaceGPU(Context* ctx) : ctx_(ctx) {}
+
+    Context* context() const { return ctx_; }
+
+    // grow(I, A, T) (:64-72): the device sizes the child itself (the same child_max_alleles rule,
+    // :287-301, is applied on the device); this checks that the sizes fit the context's capacities.
+    void grow(unsigned I, unsigned A, unsigned T) {
+        const Parameters& p = ctx_->params();
+        if (I > p.max_individuals || A > p.max_alleles || T != p.traits)
+            throw Error("grow: the population exceeds the context's capacities");
+    }
+    // remove_fixed_allele (:127-147): the free-space analysis clears fixed columns on the device (the
+    // generation kernel masks them out of every parent word), so nothing is left to do here.
+    void remove_fixed_allele(unsigned /*index*/) {}
+
+    unsigned getMaxBlocks() const { return ctx_->info().W; }                       // :94-101
+    unsigned getMaxAlleles() const { return ctx_->info().A; }
+    unsigned haploid_genome_count() const { return 2 * ctx_->info().N; }
+    unsigned getIndividualCount() const { return ctx_->info().N; }
+    unsigned getTraitCount() const { return ctx_->params().traits; }
+
+    // begin_genome / end_genome (:176-188): the words of row i, from a host copy of the current rows
+    genome_iterator begin_genome(unsigned i) { return rows().data() + (size_t)i * width_; }
+    genome_iterator end_genome(unsigned i) { return begin_genome(i) + width_; }
+    void invalidate() { rows_.clear(); }
+
+private:
+    const std::vector<block_type>& rows() {
+        if (rows_.empty()) {
+            const clotho_info i = ctx_->info();
+            width_ = i.W;
+            rows_.assign((size_t)2 * i.N * i.W, 0);
+            if (!rows_.empty())
+                check(clotho_get_rows(ctx_->get(), rows_.data(), rows_.size()), ctx_->get(), "clotho_get_rows");
+        }
+        return rows_;
+    }
+    Context* ctx_;
+    std::vector<block_type> rows_;
+    unsigned width_ = 0;
+};
+
+// AlleleSpace<double, unsigned> (allele_space_vector.hpp:31-227): positions and ages by slot.
+class AlleleSpaceGPU {
+public:
+    typedef double position_type;
+    explicit AlleleSpaceGPU(Context* ctx) : ctx_(ctx) {}
+    size_t size() const { return ctx_->info().A; }
+    // grow (:115-137): slots appended by a mutation are added by the device
+    void grow() {}
+    position_type getPositionAt(size_t i) {
+        load();
+        return pos_.at(i);
+    }
+    unsigned getAgeAt(size_t i) {
+        load();
+        return age_.at(i);
+    }
+    void invalidate() { pos_.clear(); }
+
+private:
+    void load() {
+        if (!pos_.empty()) return;
+        const unsigned A = ctx_->info().A, T = ctx_->params().traits;
+        pos_.assign(A, 0.0);
+        age_.assign(A, 0);
+        std::vector<float> eff((size_t)A * T);
+        if (A) check(clotho_get_alleles(ctx_->get(), pos_.data(), age_.data(), eff.data()), ctx_->get(),
+                     "clotho_get_alleles");
+    }
+    Context* ctx_;
+    std::vector<double> pos_;
+    std::vector<uint32_t> age_;
+};
+
+// trait_space_vector<double> (trait_space_vector.hpp:26-198): T effects per slot.
+class TraitSpaceGPU {
+public:
+    typedef float weight_type;
+    typedef std::vector<float>::const_iterator iterator;
+    explicit TraitSpaceGPU(Context* ctx) : ctx_(ctx) {}
+    unsigned trait_count() const { return ctx_->params().traits; }
+    size_t size() const { return ctx_->info().A; }
+    void grow() {}  // the device writes the effects of appended slots
+    // isAllNeutral: every effect zero (the engine then takes the constant phenotype, :205-211)
+    bool isAllNeutral() {
+        load();
+        return std::all_of(w_.begin(), w_.end(), [](float x) { return x == 0.0f; });
+    }
+    iterator begin(size_t slot) {
+        load();
+        return w_.begin() + slot * trait_count();
+    }
+    iterator end(size_t slot) { return begin(slot) + trait_count(); }
+    void invalidate() { loaded_ = false; }
+
+private:
+    void load() {
+        if (loaded_) return;
+        const unsigned A = ctx_->info().A, T = trait_count();
+        std::vector<double> pos(A);
+        std::vector<uint32_t> age(A);
+        w_.assign((size_t)A * T, 0.0f);
+        if (A) check(clotho_get_alleles(ctx_->get(), pos.data(), age.data(), w_.data()), ctx_->get(),
+                     "clotho_get_alleles");
+        loaded_ = true;
+    }
+    Context* ctx_;
+    std::vector<float> w_;
+    bool loaded_ = false;
 };
 
 // ---- FreeSpaceAnalyzerMT<population_space_row> (free_space_mt_population_space_row_interlaced.hpp:41-89)
-// with the free_space_details accessors (free_space_details.hpp:193-277).
+// with the free_space_details accessors (free_space_details.hpp:193-277).  The analysis of the parent,
+// the removal of its fixed alleles and the fixed-allele table (Engine::updateFixedAlleles,
+// engine_batched_task.hpp:303-345) run on the device in one call.
 class FreeSpaceGPU {
 public:
     typedef uint32_t size_type;
     typedef std::vector<size_type>::const_iterator iterator;
 
+    template <class PoolType>
+    void operator()(PopulationSpaceGPU* ss, PoolType&) {
+        begin_pending(ss->context());
+        uint32_t c[3];
+        check(clotho_free_space(ss->context()->get(), c), ss->context()->get(), "clotho_free_space");
+        fixed_ = c[0];
+        lost_ = c[1];
+        idx_.assign(c[2], 0);
+        if (c[2]) check(clotho_get_free(ss->context()->get(), idx_.data()), ss->context()->get(), "clotho_get_free");
+        width_ = ss->context()->info().A;
+    }
+    // the same analysis through a bare Context (the fused engine's bookkeeping)
     template <class PoolType>
     void operator()(Context* ss, PoolType&) {
         uint32_t c[3];
@@ -127,16 +296,70 @@ private:
     size_type fixed_ = 0, lost_ = 0, width_ = 0;
 };
 
+class PhenotypeGPU;
+
+// ---- GeneralFitness (general_fitness.hpp:101-276): one fitness value per individual, the toolkit metric
+// applied on the device; begin()/end() iterate a host copy.
+class FitnessGPU {
+public:
+    typedef double fitness_type;
+    typedef std::vector<double>::const_iterator const_iterator;
+
+    FitnessGPU() = default;
+    explicit FitnessGPU(Context* ctx) : ctx_(ctx) {}
+    void bind(Context* ctx) { ctx_ = ctx; }
+    Context* context() const { return ctx_; }
+
+    // GeneralFitness::operator()(phenos) (:101-119)
+    inline void operator()(const PhenotypeGPU& phenos);
+    void operator()(Context* pop) {
+        check(clotho_fitness(pop->get()), pop->get(), "clotho_fitness");
+        load(pop);
+    }
+    // resize(N) (:238-243): new entries are 1.0
+    void resize(unsigned N) {
+        while (f_.size() < N) f_.push_back(1.0);
+    }
+    unsigned individual_count() const { return (unsigned)f_.size(); }
+    unsigned size() const { return (unsigned)f_.size(); }
+    const_iterator begin() const { return f_.begin(); }
+    const_iterator end() const { return f_.end(); }
+    const std::vector<double>& values() const { return f_; }
+    std::vector<double> values(Context* pop) const {  // the current population's fitness, read back
+        clotho_info i = pop->info();
+        std::vector<double> f(i.N);
+        if (i.N) check(clotho_get_fitness(pop->get(), f.data()), pop->get(), "clotho_get_fitness");
+        return f;
+    }
+    void load(Context* pop) { f_ = values(pop); }
+
+private:
+    Context* ctx_ = nullptr;
+    std::vector<double> f_;
+};
+
 // ---- SelectionGenerator<RNG, fitness_selection<GeneralFitness>>
-// (general_fitness_selection_generator.hpp:45-113): N (id0,id1) pairs,
-// uniform when every fitness is equal, else fitness-proportional.
+// (general_fitness_selection_generator.hpp:45-113): N (id0,id1) pairs, uniform when every fitness is equal,
+// else fitness-proportional.  Host draws (the default) follow the reference with the caller's RNG; with
+// device draws the pairs come from the device's FP64 prefix sum of fitness and Philox uniforms
+// (clotho_select), which needs the generation begun on the device.
 template <class RNG>
 class SelectionGPU {
 public:
     typedef std::vector<std::pair<uint32_t, uint32_t>> mate_pair_vector;
 
-    explicit SelectionGPU(RNG* rng) : rng_(rng) {}
+    explicit SelectionGPU(RNG* rng, bool device_draws = false) : rng_(rng), device_(device_draws) {}
 
+    void update(const FitnessGPU& fit, unsigned N) {
+        if (device_ && fit.context()) {
+            std::vector<uint32_t> ids(2 * (size_t)N);
+            check(clotho_select(fit.context()->get(), ids.data()), fit.context()->get(), "clotho_select");
+            pairs_.clear();
+            for (unsigned k = 0; k < N; ++k) pairs_.emplace_back(ids[2 * k], ids[2 * k + 1]);
+            return;
+        }
+        update(fit.values(), N);
+    }
     void update(const std::vector<double>& fit, unsigned N) {
         pairs_.clear();
         const size_t M = fit.size();
@@ -156,22 +379,30 @@ public:
             }
         }
     }
+    bool device_draws() const { return device_; }
     const mate_pair_vector& getMatePairs() const { return pairs_; }
     unsigned individual_count() const { return (unsigned)pairs_.size(); }
 
 private:
     RNG* rng_;
+    bool device_;
     mate_pair_vector pairs_;
 };
 
-// ---- BatchCrossoverMTWE (batch_crossover_mtwe.hpp:51-145): the event pool,
-// lookup and bias pool are drawn on the host in the reference's order; the
-// splice runs on the device.
+// ---- BatchCrossoverMTWE (batch_crossover_mtwe.hpp:51-145): the event pool, lookup and bias pool are drawn
+// on the host in the reference's order; the splice runs on the device.
 template <class RNG>
 class CrossoverGPU {
 public:
     CrossoverGPU(RNG* rng, double rho, double bias) : rng_(rng), rho_(rho), bias_(bias) {}
 
+    // operator()(parents, parental, offspring, alleles, pool) (:51-55)
+    template <class Selection, class PoolType>
+    void operator()(const Selection& parents, PopulationSpaceGPU* /*parental*/, PopulationSpaceGPU* offspring,
+                    AlleleSpaceGPU* /*alleles*/, PoolType& pool) {
+        (*this)(parents, (Context*)nullptr, offspring->context(), pool);
+        offspring->invalidate();
+    }
     template <class Selection, class PoolType>
     void operator()(const Selection& parents, Context* /*parental*/, Context* offspring, PoolType&) {
         const size_t S = 2 * parents.individual_count();
@@ -214,19 +445,42 @@ private:
     std::vector<uint8_t> swap_;
 };
 
-// ---- BatchMutationMT (batch_mutation_mt.hpp:57-81) with the allele and trait
-// generators: per mutation target row, position, then per trait neutral draw
-// and Normal effect.
+// ---- BatchMutationMT (batch_mutation_mt.hpp:57-81) with the allele and trait generators: per mutation the
+// target row, the position, then per trait the neutral draw and the Normal effect.  The free list, slot reuse
+// and appended slots (:69-80) are applied on the device from its own analysis.
 template <class RNG>
 class MutationGPU {
 public:
-    MutationGPU(RNG* rng, const Parameters& p) : rng_(rng), p_(p) {}
+    // pop: the population whose coming generation generateNewMutation announces (may be null)
+    MutationGPU(RNG* rng, const Parameters& p, Context* pop = nullptr) : rng_(rng), p_(p), pop_(pop) {}
 
-    uint32_t generateNewMutation(unsigned N_hap) {  // mutation_allocator.hpp:41-47
+    // generateNewMutation (:57-59, mutation_allocator.hpp:41-47); also records the coming generation
+    uint32_t generateNewMutation(unsigned N_hap) {
         std::poisson_distribution<uint32_t> d(p_.mu * N_hap);
-        return p_.mu > 0 ? d(*rng_) : 0u;
+        const uint32_t M = p_.mu > 0 ? d(*rng_) : 0u;
+        if (pop_) {
+            StepState& st = pop_->step();
+            if (st.begun) throw Error("a generation is still open on the device");
+            st.pending = true;
+            st.N = N_hap / 2;
+            st.M = M;
+        }
+        return M;
     }
 
+    // operator()(pop, alleles, traits, free_space, N, age, pool[, TC]) (:61-81)
+    template <class PoolType>
+    void operator()(PopulationSpaceGPU* pop, AlleleSpaceGPU* alleles, TraitSpaceGPU* traits, FreeSpaceGPU* free_space,
+                    unsigned M, unsigned age, PoolType& pool, unsigned TC = 1) {
+        (void)free_space;
+        (void)TC;  // the reference forces one mutation task (engine_batched_task.hpp:202)
+        const clotho_info i = pop->context()->info();
+        if (age != i.generation) throw Error("mutation age differs from the device's generation");
+        (*this)(pop->context(), M, 2 * i.N, pool);
+        pop->invalidate();
+        alleles->invalidate();
+        traits->invalidate();
+    }
     template <class PoolType>
     void operator()(Context* pop, unsigned M, unsigned S, PoolType&) {
         std::uniform_int_distribution<uint32_t> seq(0, S ? S - 1 : 0);
@@ -248,37 +502,76 @@ public:
 private:
     RNG* rng_;
     Parameters p_;
+    Context* pop_;
     std::vector<uint32_t> seq_;
     std::vector<double> pos_;
     std::vector<float> eff_;
 };
 
-// ---- BatchPhenotypeMT<population_space_row> (batch_phenotype_mt_population_space_row.hpp:62-104)
+// ---- BatchPhenotypeMT<population_space_row> (batch_phenotype_mt_population_space_row.hpp:48-104).  The
+// per-individual phenotype is a T-vector (individual_count() is N; the reference's returns T*N, which makes
+// its multi-trait fitness abort: a quirk not followed).
 class PhenotypeGPU {
 public:
+    typedef std::vector<double>::const_iterator phenotype_iterator;
+
+    // operator()(parent, child, traits, pool) (:62-72)
+    template <class PoolType>
+    void operator()(PopulationSpaceGPU* /*parent*/, PopulationSpaceGPU* pop, TraitSpaceGPU* traits, PoolType&) {
+        ctx_ = pop->context();
+        trait_count_ = traits->trait_count();
+        check(clotho_phenotype(ctx_->get()), ctx_->get(), "clotho_phenotype");
+        z_.clear();
+    }
     template <class PoolType>
     void operator()(Context* /*parent*/, Context* pop, PoolType&) {
+        ctx_ = pop;
+        trait_count_ = pop->params().traits;
         check(clotho_phenotype(pop->get()), pop->get(), "clotho_phenotype");
+        z_.clear();
+    }
+    // constant_phenotype(pop, traits) (:48-59): every effect is zero, so the device's fitness stage sees
+    // the constant phenotype 1.0 (engine_batched_task.hpp:207-211)
+    void constant_phenotype(PopulationSpaceGPU* pop, TraitSpaceGPU* traits) {
+        ctx_ = pop->context();
+        trait_count_ = traits->trait_count();
+        check(clotho_phenotype(ctx_->get()), ctx_->get(), "clotho_phenotype");
+        z_.clear();
+    }
+    Context* context() const { return ctx_; }
+    unsigned individual_count() const { return ctx_ ? ctx_->info().N : 0u; }
+    unsigned trait_count() const { return trait_count_; }
+    // begin/end_individual_phenotype(i) (:86-92): individual i's T values, from a host copy read after the
+    // fitness stage (the device fills the per-individual values there)
+    phenotype_iterator begin_individual_phenotype(unsigned i) { return values().begin() + (size_t)i * trait_count_; }
+    phenotype_iterator end_individual_phenotype(unsigned i) { return begin_individual_phenotype(i) + trait_count_; }
+    const std::vector<double>& values() {
+        if (z_.empty() && ctx_) z_ = phenotypes(ctx_);
+        return z_;
     }
     std::vector<double> phenotypes(Context* pop) const {
         clotho_info i = pop->info();
         std::vector<double> z((size_t)i.N * pop->params().traits);
-        check(clotho_get_phenotypes(pop->get(), z.data()), pop->get(), "clotho_get_phenotypes");
+        if (!z.empty()) check(clotho_get_phenotypes(pop->get(), z.data()), pop->get(), "clotho_get_phenotypes");
         return z;
     }
+    void invalidate() { z_.clear(); }
+
+private:
+    Context* ctx_ = nullptr;
+    unsigned trait_count_ = 0;
+    std::vector<double> z_;
 };
 
-// ---- GeneralFitness (general_fitness.hpp:101-119) with the toolkit metric.
-class FitnessGPU {
-public:
-    void operator()(Context* pop) { check(clotho_fitness(pop->get()), pop->get(), "clotho_fitness"); }
-    std::vector<double> values(Context* pop) const {
-        clotho_info i = pop->info();
-        std::vector<double> f(i.N);
-        check(clotho_get_fitness(pop->get(), f.data()), pop->get(), "clotho_get_fitness");
-        return f;
-    }
-};
+// the last stage of the reference's sequence (:213): also ends a generation begun on the device
+inline void FitnessGPU::operator()(const PhenotypeGPU& phenos) {
+    Context* c = phenos.context() ? phenos.context() : ctx_;
+    if (!c) throw Error("fitness: no population");
+    ctx_ = c;
+    check(clotho_fitness(c->get()), c->get(), "clotho_fitness");
+    end_begun(c);
+    load(c);
+}
 
 // ---- population growth: the reference's runtime plugins and their registry
 // (population_growth_toolkit.hpp:27-53).  A model maps (current N, generation)
@@ -405,75 +698,41 @@ unsigned generations_from(const Tree& config) {
 }
 
 // ---- Engine<...> restated on the device (engine_batched_task.hpp:110-223).
-// staged = true drives the policies one by one; false uses the fused call.
+// staged = true drives the policies one by one with the reference's member signatures; false uses the
+// fused call with the same host draws (same RNG, same order), so both give the same genomes.
 template <class RNG = std::mt19937_64>
 class EngineGB300 {
 public:
-    EngineGB300(RNG* rng, const Parameters& p)
-        : rng_(rng), pop_(p), sel_(rng), xover_(rng, p.rho, p.bias), mut_(rng, p), N_(p.max_individuals),
-          fit_(p.max_individuals, 1.0) {  // GeneralFitness::resize fills 1.0 (general_fitness.hpp:230-235)
-        check(clotho_init(pop_.get(), N_), pop_.get(), "clotho_init");
-    }
+    typedef PopulationSpaceGPU sequence_space_type;
+    typedef AlleleSpaceGPU allele_type;
+    typedef TraitSpaceGPU trait_space_type;
+    typedef FreeSpaceGPU free_space_type;
+    typedef SelectionGPU<RNG> selection_type;
+    typedef CrossoverGPU<RNG> crossover_type;
+    typedef MutationGPU<RNG> mutation_type;
+    typedef PhenotypeGPU phenotype_eval_type;
+    typedef FitnessGPU fitness_type;
 
-    // With a growth model the initial size is growth(0, 0) (Engine::init,
-    // engine_batched_task.hpp:143-161) and every generation's size follows it.
-    EngineGB300(RNG* rng, const Parameters& p, std::shared_ptr<PopulationGrowth> growth)
-        : rng_(rng), pop_(p), sel_(rng), xover_(rng, p.rho, p.bias), mut_(rng, p), N_(p.max_individuals),
-          growth_(std::move(growth)) {
+    EngineGB300(RNG* rng, const Parameters& p, std::shared_ptr<PopulationGrowth> growth = nullptr,
+                bool device_selection = false)
+        : rng_(rng), pop_(p), pop0_(&pop_), pop1_(&pop_), parent_(&pop0_), child_(&pop1_), alleles_(&pop_),
+          traits_(&pop_), sel_(rng, device_selection), xover_(rng, p.rho, p.bias), mut_(rng, p, &pop_),
+          N_(p.max_individuals), growth_(std::move(growth)) {
+        // Engine::init (:143-161): the initial size is growth(0, 0) with a growth model
         if (growth_) N_ = (*growth_)(0u, 0u);
         if (N_ > p.max_individuals) throw Error("growth: initial size exceeds max_individuals");
-        fit_.assign(N_, 1.0);
+        fit_.bind(&pop_);
+        fit_.resize(N_);  // GeneralFitness::resize fills 1.0 (general_fitness.hpp:238-243)
         check(clotho_init(pop_.get(), N_), pop_.get(), "clotho_init");
     }
 
     void simulate(bool staged = false) {
         const auto t0 = std::chrono::steady_clock::now();
-        if (growth_) {  // size of this generation from the current one (engine_batched_task.hpp:167-170)
-            N_ = (*growth_)(N_, pop_.info().generation);
-            if (N_ > pop_.params().max_individuals) throw Error("growth: size exceeds max_individuals");
-        }
-        const unsigned N = N_;
-        const uint32_t M = mut_.generateNewMutation(2 * N);
         if (staged) {
-            int pool = 0;
-            check(clotho_begin_generation(pop_.get(), N, M), pop_.get(), "clotho_begin_generation");
-            free_(&pop_, pool);
-            sel_.update(fit_, N);
-            xover_(sel_, &pop_, &pop_, pool);
-            mut_(&pop_, M, 2 * N, pool);
-            pheno_(&pop_, &pop_, pool);
-            fitness_(&pop_);
-            check(clotho_end_generation(pop_.get()), pop_.get(), "clotho_end_generation");
+            simulate_staged();
         } else {
-            sel_.update(fit_, N);
-            xover_.draw(2 * (size_t)N);
-            std::vector<uint32_t> pairs;
-            pairs.reserve(2 * (size_t)N);
-            for (const auto& pr : sel_.getMatePairs()) {
-                pairs.push_back(pr.first);
-                pairs.push_back(pr.second);
-            }
-            int pool = 0;
-            (void)pool;
-            std::uniform_int_distribution<uint32_t> seq(0, 2 * N - 1);
-            std::uniform_real_distribution<double> pos(0.0, 1.0);
-            std::bernoulli_distribution neutral(pop_.params().p_neutral);
-            std::normal_distribution<double> w(pop_.params().eff_mean, pop_.params().eff_sigma);
-            const unsigned T = pop_.params().traits;
-            std::vector<uint32_t> ms(M);
-            std::vector<double> mp(M);
-            std::vector<float> me((size_t)M * T, 0.0f);
-            for (uint32_t i = 0; i < M; ++i) {
-                ms[i] = seq(*rng_);
-                mp[i] = pos(*rng_);
-                for (unsigned t = 0; t < T; ++t)
-                    if (!neutral(*rng_)) me[(size_t)i * T + t] = (float)w(*rng_);
-            }
-            clotho_gen_tape tape{N, M, pairs.data(), xover_.bias().data(), xover_.lookup().data(),
-                                 xover_.events().data(), ms.data(), mp.data(), me.data()};
-            check(clotho_generation_tape(pop_.get(), &tape), pop_.get(), "clotho_generation_tape");
+            simulate_fused();
         }
-        fit_ = fitness_.values(&pop_);
         const auto t1 = std::chrono::steady_clock::now();
         sim_times_.push_back(std::chrono::duration<double>(t1 - t0).count());
         clotho_info i = pop_.info();
@@ -483,6 +742,9 @@ public:
     }
 
     Context& population() { return pop_; }
+    sequence_space_type* getChildPopulation() const { return child_; }
+    sequence_space_type* getParentPopulation() const { return parent_; }
+    const fitness_type& fitness() const { return fit_; }
 
     // getPerformanceResults (engine_batched_task.hpp:233-242) as JSON
     std::string performance_json() const {
@@ -497,17 +759,106 @@ public:
     }
 
 private:
+    struct Pool {
+        unsigned pool_size() const { return 0u; }  // the master thread alone (thread_count_parameter.hpp:22)
+    };
+
+    // the size of the coming generation (engine_batched_task.hpp:167-170)
+    unsigned next_size() {
+        unsigned pN = N_;
+        if (growth_) {
+            pN = (*growth_)(N_, pop_.info().generation);
+            if (pN > pop_.params().max_individuals) throw Error("growth: size exceeds max_individuals");
+        }
+        return pN;
+    }
+
+    // Engine::simulate (engine_batched_task.hpp:163-223), stage by stage
+    void simulate_staged() {
+        std::swap(child_, parent_);                                   // :164
+        const unsigned pN = next_size();                              // :166-170
+        const uint32_t pM = mut_.generateNewMutation(2 * pN);         // :175
+        const uint32_t free_count = updateFixedAlleles(parent_);      // :178
+        const size_t all_size = child_max_alleles(alleles_.size(), free_count, pM);  // :182
+        child_->grow(pN, (unsigned)all_size, traits_.trait_count());  // :192
+        sel_.update(fit_, pN);                                        // :195
+        xover_(sel_, parent_, child_, &alleles_, pool_);              // :198
+        mut_(child_, &alleles_, &traits_, &free_, pM, pop_.info().generation, pool_, 1);  // :202
+        if (!traits_.isAllNeutral()) {                                // :205-211
+            pheno_(parent_, child_, &traits_, pool_);
+        } else {
+            pheno_.constant_phenotype(child_, &traits_);
+        }
+        fit_(pheno_);                                                 // :213 (ends the device generation)
+        parent_->invalidate();
+        child_->invalidate();
+        N_ = pN;
+    }
+
+    // Engine::updateFixedAlleles (:303-345): the analysis removes the fixed alleles and records them on the
+    // device; the loop over fixed indices is kept for the reference's call shape
+    uint32_t updateFixedAlleles(sequence_space_type* ss) {
+        free_(ss, pool_);
+        for (auto it = free_.fixed_begin(); it != free_.fixed_end(); ++it) ss->remove_fixed_allele(*it);
+        return free_.free_size();
+    }
+    // child_max_alleles (:287-301)
+    static size_t child_max_alleles(size_t N_parent, size_t F_parent, size_t M_child) {
+        return F_parent >= M_child ? N_parent : N_parent + (M_child - F_parent);
+    }
+
+    // the fused call: the same host draws in the same order, one tape call
+    void simulate_fused() {
+        const unsigned N = next_size();
+        const uint32_t M = mut_.generateNewMutation(2 * N);
+        pop_.step().pending = false;  // the tape call below runs the whole generation
+        sel_.update(fit_.values(), N);
+        xover_.draw(2 * (size_t)N);
+        std::vector<uint32_t> pairs;
+        pairs.reserve(2 * (size_t)N);
+        for (const auto& pr : sel_.getMatePairs()) {
+            pairs.push_back(pr.first);
+            pairs.push_back(pr.second);
+        }
+        std::uniform_int_distribution<uint32_t> seq(0, 2 * N - 1);
+        std::uniform_real_distribution<double> pos(0.0, 1.0);
+        std::bernoulli_distribution neutral(pop_.params().p_neutral);
+        std::normal_distribution<double> w(pop_.params().eff_mean, pop_.params().eff_sigma);
+        const unsigned T = pop_.params().traits;
+        std::vector<uint32_t> ms(M);
+        std::vector<double> mp(M);
+        std::vector<float> me((size_t)M * T, 0.0f);
+        for (uint32_t i = 0; i < M; ++i) {
+            ms[i] = seq(*rng_);
+            mp[i] = pos(*rng_);
+            for (unsigned t = 0; t < T; ++t)
+                if (!neutral(*rng_)) me[(size_t)i * T + t] = (float)w(*rng_);
+        }
+        clotho_gen_tape tape{N, M, pairs.data(), xover_.bias().data(), xover_.lookup().data(),
+                             xover_.events().data(), ms.data(), mp.data(), me.data()};
+        check(clotho_generation_tape(pop_.get(), &tape), pop_.get(), "clotho_generation_tape");
+        fit_.load(&pop_);
+        std::swap(child_, parent_);
+        child_->invalidate();
+        parent_->invalidate();
+        N_ = N;
+    }
+
     RNG* rng_;
     Context pop_;
+    PopulationSpaceGPU pop0_, pop1_;
+    PopulationSpaceGPU *parent_, *child_;
+    AlleleSpaceGPU alleles_;
+    TraitSpaceGPU traits_;
     FreeSpaceGPU free_;
     SelectionGPU<RNG> sel_;
     CrossoverGPU<RNG> xover_;
     MutationGPU<RNG> mut_;
     PhenotypeGPU pheno_;
-    FitnessGPU fitness_;
+    FitnessGPU fit_;
+    Pool pool_;
     unsigned N_;
     std::shared_ptr<PopulationGrowth> growth_;
-    std::vector<double> fit_;
     std::vector<double> sim_times_;
     std::vector<uint32_t> free_sizes_, var_sizes_, fixed_sizes_;
 };

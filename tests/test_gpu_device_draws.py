@@ -134,7 +134,7 @@ def test_selection_with_zero_total_fitness_is_uniform_and_flagged():
     pop.close()
 
 
-def test_parent_counts_follow_fitness_under_strong_selection():
+def test_parent_counts_follow_fitness_under_strong_selection(capsys):
     from scipy import stats
     rng = np.random.default_rng(2026)
     N, seed = 20_000, 31337
@@ -154,8 +154,9 @@ def test_parent_counts_follow_fitness_under_strong_selection():
     chi2 = float(np.sum((o_b - e_b) ** 2 / e_b))
     p = float(stats.chi2.sf(chi2, len(e_b) - 1))
     top = order[-N // 10:]
-    print(f"selection chi2 = {chi2:.1f} over {len(e_b) - 1} dof, p = {p:.3f}; top decile drew "
-          f"{obs[top].sum():.0f} of {2 * N} parents (expected {expected[top].sum():.0f})")
+    with capsys.disabled():
+        print(f"\nselection chi2 = {chi2:.1f} over {len(e_b) - 1} dof, p = {p:.3f}; top decile drew "
+              f"{obs[top].sum():.0f} of {2 * N} parents (expected {expected[top].sum():.0f})")
     assert p > 1e-4
     assert abs(obs[top].sum() - expected[top].sum()) < 5.0 * math.sqrt(expected[top].sum())
 
@@ -260,11 +261,15 @@ def spectrum_stats(rows, A, fit):
     return sfs, int(seg.sum()), float(np.sum(2.0 * f * (1.0 - f))), float(np.mean(fit))
 
 
-def test_device_runs_match_oracle_runs_in_distribution():
+def test_device_runs_match_oracle_runs_in_distribution(capsys):
     # the bench workload's shape (four traits, reference gaussian metric, rho=5, pre-seeded 1/i load)
     # at N=1,000 with mu=0.01 so that 20 new alleles arrive each generation
+    # Bound: each statistic's replicate means within 4.5 standard errors.  The nine statistics are
+    # correlated (they follow the same allele trajectories), so single bins wander together: arms that
+    # draw from the same law (two seed sets of either generator) differed by up to 2.8 standard errors.
+    # Exact agreement is what the replays above establish; this guards the laws themselves.
     w = workloads.LARGE_N
-    N, mu, G, R = 1000, 0.01, 60, 24
+    N, mu, G, R = 1000, 0.01, 60, 48
     S = 2 * N
     rng = np.random.default_rng(99)
     A0 = 330  # ~ theta * H(S-1) with theta = 4 N mu = 40
@@ -304,11 +309,12 @@ def test_device_runs_match_oracle_runs_in_distribution():
         b = np.array([d[k] for d in orc], np.float64)
         se = math.sqrt(a.var(ddof=1) / R + b.var(ddof=1) / R)
         lines.append(f"{name}: device {a.mean():.4g} oracle {b.mean():.4g} (se {se:.3g})")
-        assert abs(a.mean() - b.mean()) <= 4.0 * se + 1e-12 * abs(b.mean()), lines[-1]
+        assert abs(a.mean() - b.mean()) <= 4.5 * se + 1e-12 * abs(b.mean()), lines[-1]
     sa = np.array([d[0] for d in dev], np.float64)
     sb = np.array([d[0] for d in orc], np.float64)
     for j in range(5):  # carrier counts 1, 2-3, 4-7, 8-15, 16-31
         se = math.sqrt(sa[:, j].var(ddof=1) / R + sb[:, j].var(ddof=1) / R)
         lines.append(f"sfs bin {j}: device {sa[:, j].mean():.2f} oracle {sb[:, j].mean():.2f} (se {se:.2f})")
-        assert abs(sa[:, j].mean() - sb[:, j].mean()) <= 4.0 * se + 0.5, lines[-1]
-    print("device-drawn vs oracle runs (N=1,000, G=60, 24 replicates each):\n  " + "\n  ".join(lines))
+        assert abs(sa[:, j].mean() - sb[:, j].mean()) <= 4.5 * se, lines[-1]
+    with capsys.disabled():
+        print("\ndevice-drawn vs oracle runs (N=1,000, G=60, 48 replicates each):\n  " + "\n  ".join(lines))
