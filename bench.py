@@ -61,6 +61,7 @@ def parse():
     p.add_argument("--phase-clocks", action="store_true",
                    help="print the generation kernel's per-phase cycle breakdown (profiling build) and exit")
     p.add_argument("--no-batched", action="store_true", help="skip the batched and serving measurements")
+    p.add_argument("--batched-only", action="store_true", help="only the batched and serving measurements")
     return p.parse_args()
 
 
@@ -223,62 +224,98 @@ def run_cpu_oracle(w, N, steps, warmup, threads):
     return 2.0 * N * steps / dt, dt, info, stages
 
 
-def batched_and_serving():
-    """Batched replicates and continuous-batching serving against the plain
-    engine one job at a time, on scaled synthetic job mixes (the published
-    mixes need terabytes of bitsets; see the workload notes)."""
-    import numpy as np
-    import clotho_gb300 as cg
-    from clotho_gb300 import serving, autotune
-
-    # ---- batched: 256 populations, N log-U[1e3,2e4], mu U[1e-3,1e-2], rho U[0.1,5], T 1-4, G=100
-    jobs = serving.synthetic_jobs(256, rate=1e9, seed=11, N_range=(1_000, 20_000), G_range=(100, 100))
-    G = 100
-    b = cg.Batch([j.desc() for j in jobs])
+def compare_batched(cg, serving, autotune, N_range, G, n=256, seed=11):
+    """One batch of n populations against the same jobs one at a time, both arms timed alike: with set-up
+    (context creation, init, generations, teardown) and steady state (generations only).  The tuner's
+    choice is made on a separate batch of the same jobs (it is cached per bucket in use)."""
+    jobs = serving.synthetic_jobs(n, rate=1e9, seed=seed, N_range=N_range, G_range=(G, G))
+    descs = [j.desc() for j in jobs]
+    t0 = time.perf_counter()
+    bt = cg.Batch(descs)
+    bt.init()
+    tuned = autotune.tune(bt, gens_per_trial=2)
+    bt.close()
+    t_tune = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b = cg.Batch(descs)
     b.init()
-    tuned = autotune.tune(b, gens_per_trial=2)
-    b2 = cg.Batch([j.desc() for j in jobs])
-    b2.init()
-    b2.set_rows_per_item(tuned)
-    b2.sync()
-    t0 = time.perf_counter()
-    b2.run(G)
-    b2.sync()
-    t_batched = time.perf_counter() - t0
-    errs = sum(1 for i in range(len(jobs)) if b2.info(i)["device_error"])
+    b.set_tuning(**tuned)
+    b.sync()
+    t1 = time.perf_counter()
+    b.run(G)
+    b.sync()
+    t2 = time.perf_counter()
+    errs = sum(1 for i in range(len(jobs)) if b.info(i)["device_error"])
+    footprint = b.footprint
     b.close()
-    b2.close()
-    # plain: the same jobs one at a time
-    sample = jobs
-    t0 = time.perf_counter()
-    for j in sample:
+    t3 = time.perf_counter()
+    b_setup, b_steady = t3 - t0, t2 - t1
+    p_setup = p_steady = 0.0
+    for j in jobs:
         d = j.desc()
+        t0 = time.perf_counter()
         pop = cg.Population(j.N, j.max_alleles(), j.T, mu=j.mu, rho=j.rho, fitness=j.fitness,
                             fit_param=j.fit_param, p_neutral=j.p_neutral, seed=j.seed, max_events=d.max_events,
                             max_mutations=d.max_mutations, max_fixed=d.max_fixed)
         pop.init(j.N)
+        pop.sync()
+        t1 = time.perf_counter()
         pop.run_philox(j.N, G)
         pop.sync()
+        t2 = time.perf_counter()
         pop.close()
-    t_plain = (time.perf_counter() - t0) / len(sample) * len(jobs)
-    batched = {"workload": "256 populations, N log-U[1e3,2e4], mu U[1e-3,1e-2], rho U[0.1,5], T 1-4, G=100",
-               "jobs_per_s": len(jobs) / t_batched, "plain_jobs_per_s": len(jobs) / t_plain,
-               "speedup": t_plain / t_batched, "rows_per_item": tuned, "device_errors": errs,
-               "plain_note": "plain = the same 256 jobs run one at a time through clotho_run_philox"}
+        t3 = time.perf_counter()
+        p_setup += t3 - t0
+        p_steady += t2 - t1
+    return {
+        "with_setup": {"jobs_per_s": n / b_setup, "plain_jobs_per_s": n / p_setup, "speedup": p_setup / b_setup,
+                       "note": "batched: Batch creation, init, generations, teardown; plain: Population creation, "
+                               "init, generations, teardown for every job"},
+        "steady": {"jobs_per_s": n / b_steady, "plain_jobs_per_s": n / p_steady, "speedup": p_steady / b_steady,
+                   "note": "generations only, in both arms"},
+        "jobs_per_s": n / b_setup, "plain_jobs_per_s": n / p_setup, "speedup": p_setup / b_setup,
+        "tuning": tuned, "autotune_s": t_tune, "device_errors": errs, "footprint_gb": footprint / 1e9}
 
-    # ---- serving: open-loop Poisson arrivals, both arms on the same job list
-    # arrivals faster than either arm can serve, so jobs/s measures capacity, not the arrival rate
-    sjobs = serving.synthetic_jobs(400, rate=1000.0, seed=21, N_range=(1_000, 20_000), G_range=(20, 100))
+
+def batched_and_serving():
+    """Batched populations and continuous-batching serving against the plain engine one job at a time, on
+    synthetic job mixes shaped like the batched and serving configurations (named deviations in `workload`),
+    with both arms timed alike."""
+    import clotho_gb300 as cg
+    from clotho_gb300 import serving, autotune
+
+    batched = compare_batched(cg, serving, autotune, N_range=(1_000, 200_000), G=100)
+    batched["workload"] = (
+        f"256 populations, N log-U[1e3,2e5], mu U[1e-3,1e-2], rho U[0.1,5], T 1-4, G=100, all resident "
+        f"({batched.pop('footprint_gb'):.0f} GB). Deviations from the batched configuration: mu (stated U[0.01,1.0]; "
+        "at N=2e5 that is up to 6e6 allele slots, ~590 GB for one population) and G (stated 1,000; 100 keeps both "
+        "arms within a minute). Large populations fill the GPU on their own, so batching gains little on them")
+    small = compare_batched(cg, serving, autotune, N_range=(1_000, 20_000), G=100)
+    small["workload"] = (f"256 populations, N log-U[1e3,2e4], mu U[1e-3,1e-2], rho U[0.1,5], T 1-4, G=100 "
+                         f"({small.pop('footprint_gb'):.0f} GB): small populations, where one-at-a-time runs are "
+                         "bound by launches and set-up")
+    batched["small_populations"] = small
+
+    # ---- serving: open-loop Poisson arrivals at 20 jobs/s, both arms on the same job list
+    sjobs = serving.synthetic_jobs(200, rate=20.0, seed=21, N_range=(1_000, 10_000), G_range=(200, 2000))
     pjobs = [serving.Job(**{k: getattr(j, k) for k in ("id", "N", "mu", "rho", "T", "G", "seed", "arrival")})
              for j in sjobs]
     srv = serving.Server(budget_bytes=64 << 30, max_slots=256)
     s_srv = srv.run_open_loop(sjobs)
-    s_plain = serving.run_plain(pjobs)
+    s_plain = serving.run_plain(pjobs)      # busy from the first arrival on: its jobs/s is its capacity
+    cjobs = [serving.Job(**{k: getattr(j, k) for k in ("id", "N", "mu", "rho", "T", "G", "seed")}, arrival=0.0)
+             for j in sjobs]
+    cap = serving.Server(budget_bytes=64 << 30, max_slots=256).run_open_loop(cjobs)
     same = sum(1 for j, p in zip(sorted(srv.finished, key=lambda x: x.id), pjobs)
                if j.result["sfs"] == p.result["sfs"] and j.result["mean_fitness"] == p.result["mean_fitness"])
-    serve = {"workload": "400 jobs, Poisson arrivals 1000/s, N log-U[1e3,2e4], G U[20,100], mu U[1e-3,1e-2], "
-                         "rho U[0.1,5], T 1-4",
+    serve = {"workload": ("200 jobs arriving as a Poisson stream at 20 jobs/s (the serving configuration's rate), "
+                          "G U[200,2000] (as stated), N log-U[1e3,1e4] (stated 1e3-5e5: one 5e5 job of 2,000 "
+                          "generations takes ~15 s on the plain engine, the whole run a few hours), mu U[1e-3,1e-2] "
+                          "(unstated), rho U[0.1,5], T 1-4; latency = completion - arrival"),
              "served": s_srv, "plain": s_plain, "speedup_jobs_per_s": s_srv["jobs_per_s"] / s_plain["jobs_per_s"],
+             "served_capacity": {**cap, "note": "the same jobs all arriving at once: the served loop's capacity "
+                                 "(at 20 jobs/s it is bound by the arrivals; the plain engine is saturated there)"},
+             "capacity_speedup": cap["jobs_per_s"] / s_plain["jobs_per_s"],
              "identical_results": same}
     return batched, serve
 
@@ -366,10 +403,10 @@ def batch_kernels(cg, warmup, steps):
     """The batched measurement's 256 populations (the same job list and tuned-size items), stepped eagerly
     one generation at a time, for launch lists of a batched step."""
     from clotho_gb300 import serving
-    jobs = serving.synthetic_jobs(256, rate=1e9, seed=11, N_range=(1_000, 20_000), G_range=(100, 100))
+    jobs = serving.synthetic_jobs(256, rate=1e9, seed=11, N_range=(1_000, 200_000), G_range=(100, 100))
     b = cg.Batch([j.desc() for j in jobs])
     b.init()
-    b.set_rows_per_item(1024)
+    b.set_tuning(rows_per_item=1024)
     for _ in range(warmup + steps):
         b.step()
     b.sync()
@@ -416,6 +453,10 @@ def main():
 
     if args.batch_kernels:
         print(json.dumps(batch_kernels(cg, args.warmup, args.steps)))
+        return
+    if args.batched_only:
+        batched, serve = batched_and_serving()
+        print(json.dumps({"batched": batched, "serving": serve}))
         return
 
     w = LARGE_N

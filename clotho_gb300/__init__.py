@@ -224,6 +224,11 @@ class Population:
         self._ck(self.L.clotho_info_wait(self.h, ticket, C.byref(i)), "info_wait")
         return {n: getattr(i, n) for n, _ in capi.Info._fields_}
 
+    def set_tuning(self, rows_per_item: int = 0, narrow_build: int = 1, row_blocks_per_sm: int = 0):
+        """Launch shapes (clotho_gb300.autotune); no result depends on them."""
+        t = capi.Tuning(rows_per_item, narrow_build, row_blocks_per_sm)
+        self._ck(self.L.clotho_set_tuning(self.h, C.byref(t)), "set_tuning")
+
     def set_copy_wait_limit(self, rounds: int):
         """try_wait rounds a copy row's bulk copy may take before the STALL flag is raised (0: default)."""
         self._ck(self.L.clotho_set_copy_wait_limit(self.h, rounds), "set_copy_wait_limit")
@@ -499,6 +504,16 @@ class Batch:
 
     def set_rows_per_item(self, rows: int):
         self._ck(self.L.clotho_set_rows_per_item(self.h, rows), "set_rows_per_item")
+
+    def set_tuning(self, rows_per_item: int = 0, narrow_build: int = 1, row_blocks_per_sm: int = 0):
+        """Launch shapes (clotho_gb300.autotune); no result depends on them."""
+        t = capi.Tuning(rows_per_item, narrow_build, row_blocks_per_sm)
+        self._ck(self.L.clotho_set_tuning(self.h, C.byref(t)), "set_tuning")
+
+    def tuning(self) -> dict:
+        t = capi.Tuning()
+        self._ck(self.L.clotho_get_tuning(self.h, C.byref(t)), "get_tuning")
+        return {n: getattr(t, n) for n, _ in capi.Tuning._fields_}
 
     def set_stream(self, stream=None):
         """Run on the caller's CUDA stream (integer handle); None returns to the context's own."""

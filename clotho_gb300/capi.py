@@ -16,6 +16,10 @@ u64 = C.c_uint64
 i32 = C.c_int32
 
 
+class Tuning(C.Structure):
+    _fields_ = [("rows_per_item", u32), ("narrow_build", u32), ("row_blocks_per_sm", u32)]
+
+
 class Desc(C.Structure):
     _fields_ = [
         ("max_individuals", u32), ("max_alleles", u32), ("traits", u32), ("max_events", u32),
@@ -113,6 +117,8 @@ SIGNATURES = {
     "clotho_batch_run_philox": (C.c_int, [vp, vp, u32]),
     "clotho_set_rows_per_item": (C.c_int, [vp, u32]),
     "clotho_set_copy_wait_limit": (C.c_int, [vp, u32]),
+    "clotho_set_tuning": (C.c_int, [vp, vp]),
+    "clotho_get_tuning": (C.c_int, [vp, vp]),
     "clotho_mem_info": (C.c_int, [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     "clotho_free_space_noalloc": (C.c_int, [vp, u32, u32, u32, vp, vp, vp]),
     "clotho_host_free": (C.c_int, [vp]),

@@ -121,6 +121,9 @@ struct clotho_ctx {
     bool in_step = false;
     uint32_t maxW = 0, maxS = 0, maxN = 0, maxNB = 0, maxA = 0;
     cudaError_t launch_err = cudaSuccess;  // a launch set-up failure, reported by the next check_launch
+    uint32_t ind_per_sm = 16;               // tuning (clotho_set_tuning)
+    bool narrow_ok = true;
+    uint32_t tuning_epoch = 0;              // part of every graph's key: a new tuning re-captures
 };
 
 namespace {
@@ -142,7 +145,12 @@ int fail(clotho_ctx* c, int code, const std::string& m) {
             return fail(ctx, CLOTHO_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-LaunchCfg cfg(clotho_ctx* ctx) { return LaunchCfg{ctx->stream, ctx->num_sms}; }
+LaunchCfg cfg(clotho_ctx* ctx) {
+    LaunchCfg L{ctx->stream, ctx->num_sms};
+    L.ind_per_sm = ctx->ind_per_sm;
+    L.narrow_ok = ctx->narrow_ok;
+    return L;
+}
 
 // A pinned slot for one step header; nullptr if pinned memory is unavailable.
 uint32_t* hdr_stage(clotho_ctx* ctx, uint32_t* slot) {
@@ -421,7 +429,8 @@ void enqueue_fused_step(clotho_ctx* ctx, uint32_t set, bool philox) {
 // Captures one fused device-drawn step as the context's graph, keyed by the sizes it serves (a graph
 // with the same key is reused).  Whatever fails between the start of the capture and the graph's
 // instantiation, the capture is ended and the partial graph discarded, so the stream stays usable.
-int capture_step_graph(clotho_ctx* ctx, const std::vector<uint32_t>& key) {
+int capture_step_graph(clotho_ctx* ctx, std::vector<uint32_t> key) {
+    key.push_back(ctx->tuning_epoch);
     if (ctx->graph && ctx->graph_key == key) return 0;
     if (ctx->graph) {
         cudaGraphExecDestroy(ctx->graph);
@@ -1696,6 +1705,31 @@ int clotho_set_copy_wait_limit(clotho_ctx* ctx, uint32_t rounds) {
     if (rounds > (1u << 30)) return fail(ctx, CLOTHO_E_ARG, "wait limit above 2^30 rounds");
     CK(cudaMemcpyAsync(&ctx->d_ctl->wait_limit, &rounds, sizeof(rounds), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int clotho_set_tuning(clotho_ctx* ctx, const clotho_tuning* t) {
+    if (!ctx || !t) return CLOTHO_E_ARG;
+    if (t->rows_per_item > 65536 || t->row_blocks_per_sm > 64 || t->narrow_build > 1)
+        return fail(ctx, CLOTHO_E_ARG, "tuning value out of range");
+    if (t->rows_per_item) {
+        int rc = clotho_set_rows_per_item(ctx, t->rows_per_item);
+        if (rc) return rc;
+    }
+    ctx->ind_per_sm = t->row_blocks_per_sm ? t->row_blocks_per_sm : 16u;
+    ctx->narrow_ok = t->narrow_build != 0u;
+    ctx->tuning_epoch += 1;  // graphs captured under the old launch shapes are not replayed
+    return 0;
+}
+
+int clotho_get_tuning(clotho_ctx* ctx, clotho_tuning* t) {
+    if (!ctx || !t) return CLOTHO_E_ARG;
+    uint32_t rpi = 0;
+    CK(cudaMemcpyAsync(&rpi, &ctx->d_ctl->rows_per_item, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    t->rows_per_item = rpi;
+    t->narrow_build = ctx->narrow_ok ? 1u : 0u;
+    t->row_blocks_per_sm = ctx->ind_per_sm;
     return 0;
 }
 

@@ -256,6 +256,8 @@ namespace clotho {
 struct LaunchCfg {
     cudaStream_t stream;
     int num_sms;
+    uint32_t ind_per_sm = 16;     // blocks per SM of the per-individual kernels (selection, fitness)
+    bool narrow_ok = true;        // the narrow build of k_generation may run when every row fits it
 };
 
 // Population-parallel launches: blockIdx.z walks the populations, so small

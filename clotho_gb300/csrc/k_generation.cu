@@ -1406,7 +1406,7 @@ cudaError_t launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t n
         gacc ? 0 : (3ull + (suf ? kWarps : 0u)) * maxW * sizeof(uint64_t) + (suf ? kWarps * sizeof(WarpSmem) : 0);
     // profile 2: the suffix-table kernel's build with phase clocks; rows of at most
     // 128 words: its narrow build (copy rows by direct loads)
-    const bool narrow = maxW <= 64u * kDirectCopyChunks;
+    const bool narrow = L.narrow_ok && maxW <= 64u * kDirectCopyChunks;
     const int si = suf ? (profile == 2 ? (narrow ? 4 : 2) : narrow ? 3 : 1) : 0;
     const void* fns[5] = {(const void*)k_generation<false, false, false>, (const void*)k_generation<true, false, false>,
                           (const void*)k_generation<true, true, false>, (const void*)k_generation<true, false, true>,

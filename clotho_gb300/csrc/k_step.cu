@@ -413,7 +413,7 @@ __global__ void k_select_philox(const PopDev* __restrict__ pops, uint32_t npops)
     }
 }
 void launch_select_philox(const LaunchCfg& L, const PopDev* pops, uint32_t npops) {
-    k_select_philox<<<pop_grid(npops, L.num_sms * 2u, L.num_sms, 16), 256, 0, L.stream>>>(pops, npops);
+    k_select_philox<<<pop_grid(npops, L.num_sms * 2u, L.num_sms, L.ind_per_sm), 256, 0, L.stream>>>(pops, npops);
 }
 
 // ---------------------------------------------------------------------------
@@ -461,7 +461,7 @@ __global__ void k_individuals(const PopDev* __restrict__ pops, uint32_t npops) {
     }
 }
 void launch_individuals(const LaunchCfg& L, const PopDev* pops, uint32_t npops) {
-    k_individuals<<<pop_grid(npops, L.num_sms * 2u, L.num_sms, 16), 256, 0, L.stream>>>(pops, npops);
+    k_individuals<<<pop_grid(npops, L.num_sms * 2u, L.num_sms, L.ind_per_sm), 256, 0, L.stream>>>(pops, npops);
 }
 
 // ---------------------------------------------------------------------------

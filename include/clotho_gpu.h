@@ -349,6 +349,25 @@ int  clotho_set_copy_wait_limit(clotho_ctx *ctx, uint32_t rounds);
  * batched contexts; a single-population context has its warps claim one row
  * at a time and ignores it). */
 int  clotho_set_rows_per_item(clotho_ctx *ctx, uint32_t rows);
+/* Launch shapes chosen by an autotuner (clotho_gb300/autotune.py).  None
+ * changes a result: the kernels are deterministic in every shape.
+ *   rows_per_item      rows per scheduling item of the generation kernel in
+ *                      batched contexts (0 = keep the current value)
+ *   narrow_build       1 = run the generation kernel's narrow build when every
+ *                      row is at most 128 words (the default), 0 = always the
+ *                      wide build
+ *   row_blocks_per_sm  blocks per SM of the per-individual kernels of a step
+ *                      (parent sampling; phenotype and fitness); 0 = the
+ *                      default, 16
+ * No reference counterpart: the reference's work partition is its thread
+ * pool's fixed batches (thread_pool.hpp:31-139). */
+typedef struct clotho_tuning {
+    uint32_t rows_per_item;
+    uint32_t narrow_build;
+    uint32_t row_blocks_per_sm;
+} clotho_tuning;
+int  clotho_set_tuning(clotho_ctx *ctx, const clotho_tuning *t);
+int  clotho_get_tuning(clotho_ctx *ctx, clotho_tuning *t);
 /* Free and total device memory (admission control). */
 int  clotho_mem_info(size_t *free_bytes, size_t *total_bytes);
 

@@ -103,24 +103,36 @@ def test_interval_and_suffix_classifiers_agree():
     assert abs(bs["mean_fitness"] / st["mean_fitness"] - 1.0) < 1e-9
 
 
-def test_rows_per_item_does_not_change_results():
+@pytest.mark.parametrize("cap", [8192, 1 << 14])
+def test_launch_shapes_do_not_change_results(cap):
+    # every tuning knob (rows per item, the narrow build where rows are at most 128 words, blocks per SM of
+    # the per-individual kernels) gives bit-identical rows, statistics and mean fitness; at 8,192 slots
+    # the narrow build runs unless switched off
     G = 6
     outs = []
-    for rpi in (64, 1024):
-        b = cg.Batch([desc_of(s) for s in SPECS[:3]])
+    for rpi, narrow, blocks in ((64, 1, 16), (1024, 0, 4), (256, 1, 24), (512, 0, 8)):
+        b = cg.Batch([cg.make_desc(s["N"], cap, s["T"], p_neutral=0.3,
+                                   **{k: v for k, v in s.items() if k not in ("N", "T")}) for s in SPECS[:3]])
         b.init()
-        b.set_rows_per_item(rpi)
+        b.set_tuning(rows_per_item=rpi, narrow_build=narrow, row_blocks_per_sm=blocks)
+        assert b.tuning() == {"rows_per_item": rpi, "narrow_build": narrow, "row_blocks_per_sm": blocks}
         b.run(G)
-        outs.append([b.rows(i) for i in range(3)])
-    for a, c in zip(*outs):
-        assert np.array_equal(a, c)
+        outs.append([(b.rows(i), b.stats(i, 64), b.info(i)) for i in range(3)])
+        b.close()
+    for other in outs[1:]:
+        for (ra, sa, ia), (rb, sb, ib) in zip(outs[0], other):
+            assert ia["device_error"] == 0 and ib["device_error"] == 0
+            assert np.array_equal(ra, rb)
+            assert np.array_equal(sa["sfs"], sb["sfs"]) and sa["mean_fitness"] == sb["mean_fitness"]
 
 
 def test_autotuner_picks_a_candidate(tmp_path):
     b = cg.Batch([desc_of(s) for s in SPECS])
     b.init()
     best = autotune.tune(b, gens_per_trial=1, cache_path=str(tmp_path / "tune.json"))
-    assert best in autotune.CANDIDATES
+    assert set(best) == set(autotune.DEFAULT)
+    assert all(best[k] in v for k, v in autotune.CANDIDATES.items())
+    assert b.tuning() == best
     assert autotune.tune(b, cache_path=str(tmp_path / "tune.json")) == best  # cached
 
 

@@ -2,10 +2,11 @@
 batch: admission under the byte budget and the slot limit, retirement by
 index from the highest down (every job gets its own population's result),
 chunked stepping that never runs a job past its generation count, and the
-error for a job larger than the whole budget; and the autotuner's choice of
-rows per item and its cache.  The footprint of each job comes from the real
+error for a job larger than the whole budget; and the autotuner's search over
+launch shapes and its cache.  The footprint of each job comes from the real
 library (`clotho_footprint_for` needs no GPU)."""
 import itertools
+import math
 
 import numpy as np
 import pytest
@@ -120,19 +121,21 @@ def test_summary_percentiles():
 
 
 class TimedBatch:
-    """Stand-in with a per-grain step cost (ms), for the autotuner."""
+    """Stand-in with a step cost (ms) per launch-shape configuration, for the autotuner."""
 
     def __init__(self, cost, N=(1000, 2000), A=4096):
         self.cost, self.N = cost, list(N)
         self.descs = [cg.make_desc(n, A) for n in N]
-        self.rpi, self.steps, self.ms = None, 0, 0.0
+        self.cfg, self.steps, self.ms, self.trials = None, 0, 0.0, []
 
-    def set_rows_per_item(self, r):
-        self.rpi = r
+    def set_tuning(self, rows_per_item=0, narrow_build=1, row_blocks_per_sm=0):
+        self.cfg = {"rows_per_item": rows_per_item, "narrow_build": narrow_build,
+                    "row_blocks_per_sm": row_blocks_per_sm}
+        self.trials.append(dict(self.cfg))
 
     def step(self):
         self.steps += 1
-        self.ms += self.cost[self.rpi]
+        self.ms += self.cost(self.cfg)
 
     def sync(self):
         pass
@@ -144,15 +147,25 @@ class TimedBatch:
         return self.ms
 
 
-def test_autotuner_keeps_the_fastest_grain_and_caches_it(tmp_path):
-    cost = {64: 5.0, 128: 3.0, 256: 1.5, 512: 2.0, 1024: 4.0}
-    b = TimedBatch(cost)
+def _cost(best):
+    # separable cost with its minimum at `best`
+    return lambda c: 1.0 + sum(abs(math.log2(c[k] + 1) - math.log2(best[k] + 1)) for k in best)
+
+
+def test_autotuner_finds_the_fastest_shapes_and_caches_them(tmp_path):
+    best = {"rows_per_item": 256, "narrow_build": 0, "row_blocks_per_sm": 8}
+    b = TimedBatch(_cost(best))
     path = str(tmp_path / "sub" / "tune.json")
-    assert autotune.tune(b, gens_per_trial=2, cache_path=path) == 256 and b.rpi == 256
-    assert b.steps == 3 * len(autotune.CANDIDATES)
-    b2 = TimedBatch({k: 1.0 for k in cost})  # a cache hit runs nothing
-    assert autotune.tune(b2, cache_path=path) == 256 and b2.rpi == 256 and b2.steps == 0
-    # another bucket (wider rows) is tuned afresh
-    b3 = TimedBatch({64: 1.0, 128: 2.0, 256: 3.0, 512: 4.0, 1024: 5.0}, A=1 << 20)
+    assert autotune.tune(b, gens_per_trial=2, cache_path=path) == best and b.cfg == best
+    n_trials = sum(len(v) for v in autotune.CANDIDATES.values())
+    assert b.steps == 3 * n_trials                    # a warm-up and two timed steps per candidate
+    b2 = TimedBatch(lambda c: 1.0)                     # a cache hit runs nothing
+    assert autotune.tune(b2, cache_path=path) == best and b2.cfg == best and b2.steps == 0
+    # another bucket (wider rows): the narrow build cannot run there, so that knob is not searched
+    best3 = {"rows_per_item": 64, "narrow_build": 1, "row_blocks_per_sm": 24}
+    b3 = TimedBatch(_cost(best3), A=1 << 20)
     assert autotune.bucket(b3) != autotune.bucket(b)
-    assert autotune.tune(b3, cache_path=path) == 64
+    got = autotune.tune(b3, cache_path=path)
+    assert got == best3
+    assert all(t["narrow_build"] == 1 for t in b3.trials)
+    assert b3.steps == 3 * (n_trials - len(autotune.CANDIDATES["narrow_build"]))
