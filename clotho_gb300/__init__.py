@@ -229,6 +229,11 @@ class Population:
         t = capi.Tuning(rows_per_item, narrow_build, row_blocks_per_sm)
         self._ck(self.L.clotho_set_tuning(self.h, C.byref(t)), "set_tuning")
 
+    def count_columns(self, enable: bool = True):
+        """Count every allele slot's carriers inside each later fused generation step, so stats() reads the
+        counts instead of making a pass over the rows."""
+        self._ck(self.L.clotho_pop_count_columns(self.h, 0, 1 if enable else 0), "count_columns")
+
     def set_copy_wait_limit(self, rounds: int):
         """try_wait rounds a copy row's bulk copy may take before the STALL flag is raised (0: default)."""
         self._ck(self.L.clotho_set_copy_wait_limit(self.h, rounds), "set_copy_wait_limit")
@@ -509,6 +514,10 @@ class Batch:
         """Launch shapes (clotho_gb300.autotune); no result depends on them."""
         t = capi.Tuning(rows_per_item, narrow_build, row_blocks_per_sm)
         self._ck(self.L.clotho_set_tuning(self.h, C.byref(t)), "set_tuning")
+
+    def count_columns(self, i: int, enable: bool = True):
+        """Population i counts its allele slots' carriers inside each later step (stats() then reads them)."""
+        self._ck(self.L.clotho_pop_count_columns(self.h, i, 1 if enable else 0), "pop_count_columns")
 
     def tuning(self) -> dict:
         t = capi.Tuning()

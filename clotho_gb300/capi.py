@@ -118,6 +118,7 @@ SIGNATURES = {
     "clotho_set_rows_per_item": (C.c_int, [vp, u32]),
     "clotho_set_copy_wait_limit": (C.c_int, [vp, u32]),
     "clotho_set_tuning": (C.c_int, [vp, vp]),
+    "clotho_pop_count_columns": (C.c_int, [vp, u32, C.c_int]),
     "clotho_get_tuning": (C.c_int, [vp, vp]),
     "clotho_mem_info": (C.c_int, [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     "clotho_free_space_noalloc": (C.c_int, [vp, u32, u32, u32, vp, vp, vp]),

@@ -19,6 +19,7 @@ namespace {
 
 struct PopHost {
     clotho_desc desc{};
+    bool counting = false;    // asked for fused column counts (clotho_pop_count_columns)
     PopDev dev[3]{};          // tape set 0, tape set 1, device-drawn (Philox)
     void* arena = nullptr;          // every device table of the population, one pool block
     size_t bytes = 0;
@@ -72,6 +73,7 @@ std::vector<size_t> sizes_of(const Geometry& g) {
         A <= kSufMaxSlots ? g.EVcap * 4ull : 0,                   // plan_cr
         A <= kSufMaxSlots ? S * 8 : 0,                            // plan_mut
         A <= kSufMaxSlots ? S * 32 : 0,                           // plan_z
+        A * 4,                                                    // colcnt
         sizeof(DevStatus),
         // two tape sets: pairs, swap, ev_off, ev_pos, mut_seq, mut_pos, mut_eff
         S * 4, S, (S + 1) * 4, g.EVcap * 8ull, g.Mcap * 4ull, g.Mcap * 8ull, g.Mcap * T * 4ull,
@@ -124,6 +126,7 @@ struct clotho_ctx {
     uint32_t ind_per_sm = 16;               // tuning (clotho_set_tuning)
     bool narrow_ok = true;
     uint32_t tuning_epoch = 0;              // part of every graph's key: a new tuning re-captures
+    uint32_t counting = 0;                  // populations that asked for fused column counts
 };
 
 namespace {
@@ -248,6 +251,7 @@ int alloc_pop(clotho_ctx* ctx, const clotho_desc& d, PopHost** out) {
     b.ord_cur = (uint32_t*)ptr[k++]; b.ord_pos = (uint32_t*)ptr[k++];
     b.plan_go = (uint32_t*)ptr[k++]; b.plan_cr = (uint32_t*)ptr[k++];
     b.plan_mut = (uint2*)ptr[k++]; b.plan_z = (double*)ptr[k++];
+    b.colcnt = (uint32_t*)ptr[k++];
     b.st = (DevStatus*)ptr[k++];
     b.Scap = g.Scap; b.Ncap = g.Ncap; b.Wcap = g.Wcap; b.Acap = g.Aslots; b.Mcap = g.Mcap;
     b.EVcap = g.EVcap; b.FXcap = g.FXcap; b.T = g.T; b.NB = g.NB;
@@ -340,6 +344,13 @@ int prof_collect(clotho_ctx* ctx) {
     return 0;
 }
 
+// The fused step's generation kernel counts columns (its counting build) when a population asked and the
+// counters fit in shared memory; k_fs_finalize of the same step zeroes those counts and marks them valid.
+bool count_on(clotho_ctx* ctx, uint32_t fuse) {
+    return ctx->counting > 0 && (fuse & kFuseFs) && !(ctx->profiling && ctx->phase_clocks) &&
+           generation_counts_fit(ctx->maxW, ctx->maxA);
+}
+
 void launch_gen(clotho_ctx* ctx, const PopDev* pops, uint32_t npops, uint32_t fuse) {
     if (ctx->maxA <= kSufMaxSlots) {  // per-row crossover plans of the suffix-table classifier
         launch_plan(cfg(ctx), pops, npops, ctx->maxS);
@@ -347,7 +358,7 @@ void launch_gen(clotho_ctx* ctx, const PopDev* pops, uint32_t npops, uint32_t fu
     }
     prof_begin(ctx);
     const cudaError_t e = launch_generation(cfg(ctx), pops, npops, ctx->d_ctl, ctx->maxW, ctx->maxA, fuse,
-                                            ctx->profiling ? (ctx->phase_clocks ? 2 : 1) : 0);
+                                            ctx->profiling ? (ctx->phase_clocks ? 2 : 1) : 0, count_on(ctx, fuse));
     if (e != cudaSuccess && ctx->launch_err == cudaSuccess) ctx->launch_err = e;
     prof_end(ctx);
     ctx->launches += 1;
@@ -411,7 +422,7 @@ void enqueue_fused_step(clotho_ctx* ctx, uint32_t set, bool philox) {
     launch_begin(L, pops, n, ctx->d_hdr[set], ctx->d_ctl);
     ensure_parent_acc(ctx, pops, n);
     if (philox) launch_mut_counts_philox(L, pops, n, ctx->maxS);
-    launch_fs_finalize(L, pops, n);
+    launch_fs_finalize(L, pops, n, count_on(ctx, kFuseMut | kFusePheno | kFuseFs));
     if (!philox) launch_mut_csr_tape(L, pops, n, ctx->maxS);
     launch_mut_resolve(L, pops, n);
     launch_ranks(L, pops, n, ctx->maxNB, ctx->maxW, ctx->maxA <= kSufMaxSlots);
@@ -629,6 +640,7 @@ static int init_pop(clotho_ctx* ctx, uint32_t idx, uint32_t N0) {
     s.gen = 1;
     s.cur = 0;
     s.N = N0;
+    s.count_cols = p->counting ? 1u : 0u;
     s.fit_const = 1;
     s.fit_total = (double)N0;
     s.all_neutral = 1;
@@ -671,6 +683,7 @@ static int start_population(clotho_ctx* ctx, uint32_t N, uint32_t A, const doubl
     s.cur = 0;
     s.N = N;
     s.A = A;
+    s.count_cols = p->counting ? 1u : 0u;
     s.W = ref_width(A);
     s.nz_eff = nz;
     s.fit_const = 1;
@@ -1148,17 +1161,22 @@ static int stats_of(clotho_ctx* ctx, uint32_t idx, clotho_stats* out, uint32_t* 
     const PopDev& D = p->dev[0];
     const uint32_t A = s.A, S = 2 * s.N;
     std::vector<uint32_t> counts(std::max<size_t>(1, (size_t)s.W * 64), 0);
-    // scratch column counts from the context's pool: stream-ordered, no device-wide synchronisation
-    uint32_t* d_counts = nullptr;
-    CK(pool_alloc(ctx, &d_counts, counts.size() * 4));
-    CK(cudaMemsetAsync(d_counts, 0, counts.size() * 4, ctx->stream));
-    if (S && s.W) launch_stats(cfg(ctx), ctx->d_pops[0], idx, d_counts, s.W);
-    CK(cudaMemcpyAsync(counts.data(), d_counts, counts.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaFreeAsync(d_counts, ctx->stream));
+    if (s.cols_valid) {
+        // the last fused step counted the columns of these rows: no pass over the rows
+        if (A) CK(cudaMemcpyAsync(counts.data(), D.colcnt, (size_t)A * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    } else {
+        // scratch column counts from the context's pool: stream-ordered, no device-wide synchronisation
+        uint32_t* d_counts = nullptr;
+        CK(pool_alloc(ctx, &d_counts, counts.size() * 4));
+        CK(cudaMemsetAsync(d_counts, 0, counts.size() * 4, ctx->stream));
+        if (S && s.W) launch_stats(cfg(ctx), ctx->d_pops[0], idx, d_counts, s.W);
+        CK(cudaMemcpyAsync(counts.data(), d_counts, counts.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaFreeAsync(d_counts, ctx->stream));
+        ctx->launches += 1;
+    }
     std::vector<double> zi((size_t)s.N * 4);
     if (s.N) CK(cudaMemcpyAsync(zi.data(), D.zi, (size_t)s.N * 32, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    ctx->launches += 1;
     *out = clotho_stats{};
     if (sfs)
         for (uint32_t k = 0; k < sfs_len; ++k) sfs[k] = 0;
@@ -1341,7 +1359,7 @@ int clotho_snapshot(clotho_ctx* ctx, void* dst, size_t len) {
     char* b = static_cast<char*>(dst);
     SnapHeader h{};
     std::memcpy(h.magic, kSnapMagic, 8);
-    h.version = 1;
+    h.version = 2;
     h.header_bytes = sizeof(SnapHeader);
     h.desc = p->desc;
     h.st = st;
@@ -1381,11 +1399,11 @@ int clotho_restore(clotho_ctx* ctx, const void* src, size_t len) {
     if (len < sizeof(SnapHeader)) return fail(ctx, CLOTHO_E_ARG, "not a snapshot (too short)");
     SnapHeader h;
     std::memcpy(&h, src, sizeof(h));
-    if (std::memcmp(h.magic, kSnapMagic, 8) != 0 || h.version != 1 || h.header_bytes != sizeof(SnapHeader))
+    if (std::memcmp(h.magic, kSnapMagic, 8) != 0 || h.version != 2 || h.header_bytes != sizeof(SnapHeader))
         return fail(ctx, CLOTHO_E_ARG, "not a snapshot of this library version");
     PopHost* p = ctx->pops[0];
     const PopDev& D = p->dev[0];
-    const DevStatus st = h.st;
+    DevStatus st = h.st;
     if (st.cur > 1u || st.W != ref_width(st.A)) return fail(ctx, CLOTHO_E_ARG, "snapshot status is inconsistent");
     const SnapLayout L = snap_layout(st, D.T);
     if (h.total_bytes != L.total || len < L.total) return fail(ctx, CLOTHO_E_ARG, "snapshot truncated");
@@ -1436,6 +1454,8 @@ int clotho_restore(clotho_ctx* ctx, const void* src, size_t len) {
     }
     int rc = init_pop(ctx, 0, st.N);  // zeroed tables and counters
     if (rc) return rc;
+    st.count_cols = ctx->pops[0]->counting ? 1u : 0u;  // the context's own choice, not the snapshot's
+    st.cols_valid = 0u;
     cudaStream_t s = ctx->stream;
     CK(cudaMemcpyAsync(D.st, &st, sizeof(DevStatus), cudaMemcpyHostToDevice, s));
     if (S * st.W)
@@ -1590,9 +1610,27 @@ int clotho_pop_remove(clotho_ctx* ctx, uint32_t index) {
     if (!ctx || index >= ctx->pops.size()) return fail(ctx, CLOTHO_E_ARG, "no such population");
     CK(cudaStreamSynchronize(ctx->copy_stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->pops[index]->counting) {
+        ctx->counting -= 1;
+        ctx->tuning_epoch += 1;  // the step's kernels change when the last counting population leaves
+    }
     free_pop(ctx, ctx->pops[index]);
     ctx->pops.erase(ctx->pops.begin() + index);
     return sync_pop_arrays(ctx, index);
+}
+
+int clotho_pop_count_columns(clotho_ctx* ctx, uint32_t index, int enable) {
+    if (!ctx || index >= ctx->pops.size()) return fail(ctx, CLOTHO_E_ARG, "no such population");
+    PopHost* p = ctx->pops[index];
+    const bool on = enable != 0;
+    if (p->counting == on) return 0;
+    const uint32_t v = on ? 1u : 0u;
+    CK(cudaMemcpyAsync(&p->dev[0].st->count_cols, &v, 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    p->counting = on;
+    ctx->counting += on ? 1u : (uint32_t)-1;
+    ctx->tuning_epoch += 1;  // a captured step re-captures with (or without) the counting build
+    return 0;
 }
 
 int clotho_pop_init(clotho_ctx* ctx, uint32_t index, uint32_t N0) { return init_pop(ctx, index, N0); }

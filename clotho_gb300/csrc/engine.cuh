@@ -49,6 +49,8 @@ struct DevStatus {
     uint32_t all_neutral;  // phenotype took the constant path
     uint32_t last_M;
     uint32_t ev_used;      // crossover-plan event entries allocated in the step in progress
+    uint32_t count_cols;   // the host asked for per-column counts of every fused step's child rows
+    uint32_t cols_valid;   // colcnt holds the column counts of the current child rows
     double   fit_total;    // sum of fitness of the current population
     double   fixsum[4];    // effect sums of the alleles fixed in this step's parent
 };
@@ -100,6 +102,7 @@ struct PopDev {
     uint32_t* plan_cr;     // [EVcap] correction ranks per planned event: first | count << 20 (with suf)
     uint2*    plan_mut;    // [Scap] new alleles of the planned row (processing order): CSR offset, count
     double*   plan_z;      // [Scap * 4] phenotype base of the planned row: z(base strand) - sum(fixed)
+    uint32_t* colcnt;      // [Acap] per-column counts of the child rows (counting steps)
     DevStatus* st;
     uint32_t Scap, Ncap, Wcap, Acap, Mcap, EVcap, FXcap, T;
     uint32_t NB, pad2;     // position buckets (power of two)
@@ -276,7 +279,9 @@ inline uint32_t blocks_for(uint64_t n, uint32_t per_block) {
 }
 // which: 0 = current child rows, 1 = parent rows of the step in progress
 void launch_fs_reduce(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxW, uint32_t which);
-void launch_fs_finalize(const LaunchCfg&, const PopDev* pops, uint32_t npops);
+// count_on: the step's generation kernel counts columns for the populations that asked (see
+// generation_counts_fit); their counts are zeroed here and marked valid
+void launch_fs_finalize(const LaunchCfg&, const PopDev* pops, uint32_t npops, bool count_on = false);
 void launch_begin(const LaunchCfg&, const PopDev* pops, uint32_t npops, const uint32_t* hdr,
                   WorkCtl* ctl);
 void launch_mut_csr_tape(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
@@ -284,7 +289,9 @@ void launch_mut_counts_philox(const LaunchCfg&, const PopDev* pops, uint32_t npo
 void launch_mut_resolve(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_select_philox(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 cudaError_t launch_generation(const LaunchCfg&, const PopDev* pops, uint32_t npops, WorkCtl* ctl,
-                              uint32_t maxW, uint32_t maxA, uint32_t fuse, int profile);
+                              uint32_t maxW, uint32_t maxA, uint32_t fuse, int profile, bool count_on = false);
+// whether the generation kernel's counting build fits this launch (suffix-table rows, counters in shared memory)
+bool generation_counts_fit(uint32_t maxW, uint32_t maxA);
 void launch_mut_scatter(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_phenotype(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_individuals(const LaunchCfg&, const PopDev* pops, uint32_t npops);

@@ -102,9 +102,14 @@ __device__ inline void padded_word(const PopDev& P, uint32_t w, uint32_t W, uint
     L = ~(P.accV[w] | ~valid);
 }
 
-__global__ void __launch_bounds__(1024) k_fs_finalize(const PopDev* __restrict__ pops) {
+__global__ void __launch_bounds__(1024) k_fs_finalize(const PopDev* __restrict__ pops, uint32_t count_on) {
     const PopDev& P = pops[blockIdx.x];
     DevStatus* st = P.st;
+    // column counts of this step's child rows, for the populations that asked: zeroed here, added by the
+    // generation kernel's counting build
+    const bool counting = count_on && st->count_cols != 0u;
+    if (counting)
+        for (uint32_t a = threadIdx.x; a < P.Acap; a += 1024u) P.colcnt[a] = 0u;
     __shared__ uint32_t s_warp[32];
     const uint32_t pA = st->pA, pW = st->pW, pS = 2u * st->pN, M = st->M;
     const uint32_t fx_base = st->fixed_total;
@@ -193,11 +198,12 @@ __global__ void __launch_bounds__(1024) k_fs_finalize(const PopDev* __restrict__
             st->A = Ac;
         }
         st->W = ref_width(st->A);
+        st->cols_valid = counting ? 1u : 0u;
     }
 }
 
-void launch_fs_finalize(const LaunchCfg& L, const PopDev* pops, uint32_t npops) {
-    k_fs_finalize<<<npops, 1024, 0, L.stream>>>(pops);
+void launch_fs_finalize(const LaunchCfg& L, const PopDev* pops, uint32_t npops, bool count_on) {
+    k_fs_finalize<<<npops, 1024, 0, L.stream>>>(pops, count_on ? 1u : 0u);
 }
 
 }  // namespace clotho

@@ -156,6 +156,59 @@ __device__ __forceinline__ void fold_fs(uint64_t* sF, uint64_t* sV, uint32_t w, 
     if (x1 & ~v.y) atomicOr((unsigned long long*)&sV[w + 1u], (unsigned long long)x1);
 }
 
+// Per-column counts of the finished child words, bit-sliced: plane b (cnt + b * stride) holds bit b of every
+// column's count in the CTA since its last flush.  Adding a word is a ripple-carry increment of every column
+// whose bit is set; each step is an atomic XOR whose old value gives the carry, so adds from other warps
+// interleave exactly.  Up to 2^kCountPlanes - 1 rows between flushes.
+constexpr uint32_t kCountPlanes = 16;
+
+__device__ __forceinline__ void count_add(uint64_t* cnt, uint32_t stride, uint32_t w, uint64_t x0, uint64_t x1) {
+    unsigned long long c0 = x0, c1 = x1;
+    for (uint32_t b = 0; b < kCountPlanes && (c0 | c1); ++b) {
+        unsigned long long* pl = reinterpret_cast<unsigned long long*>(cnt + (size_t)b * stride + w);
+        if (c0) c0 &= atomicXor(pl, c0);
+        if (c1) c1 &= atomicXor(pl + 1, c1);
+    }
+}
+
+// What the free-space epilogue folds a finished word pair into: the AND/OR accumulators and, in the
+// counting build, the column-count planes (cnt null otherwise, and the branch folds away).
+struct Fold {
+    uint64_t* F;
+    uint64_t* V;
+    uint64_t* cnt;
+    uint32_t stride;
+};
+__device__ __forceinline__ void fold(const Fold& fo, uint32_t w, uint64_t x0, uint64_t x1) {
+    fold_fs(fo.F, fo.V, w, x0, x1);
+    if (fo.cnt) count_add(fo.cnt, fo.stride, w, x0, x1);
+}
+constexpr uint32_t kCountMax = (1u << kCountPlanes) - 1u;   // rows a CTA may add between flushes
+
+// Adds the CTA's counters of words [0, W) to the population's column counts colcnt[0, A) and clears them.
+// The whole block calls it, after a barrier (every add is done) and before one (the planes are reused).
+__device__ __noinline__ void count_flush(uint64_t* planes, uint32_t stride, uint32_t W, uint32_t A,
+                                         uint32_t* __restrict__ colcnt) {
+    for (uint32_t w = threadIdx.x; w < W; w += blockDim.x) {
+        uint64_t pl[kCountPlanes];
+        uint64_t any = 0;
+#pragma unroll
+        for (uint32_t b = 0; b < kCountPlanes; ++b) {
+            pl[b] = planes[(size_t)b * stride + w];
+            planes[(size_t)b * stride + w] = 0ull;
+            any |= pl[b];
+        }
+        for (uint64_t m = any; m; m &= m - 1ull) {
+            const uint32_t j = (uint32_t)(__ffsll((long long)m) - 1);
+            uint32_t c = 0;
+#pragma unroll
+            for (uint32_t b = 0; b < kCountPlanes; ++b) c |= (uint32_t)((pl[b] >> j) & 1ull) << b;
+            const uint32_t slot = w * 64u + j;
+            if (slot < A) atomicAdd(colcnt + slot, c);
+        }
+    }
+}
+
 // XOR masks of the lane's two words (w, w+1) from the row's new alleles.
 // Called by the whole warp (the shuffles need every lane).
 __device__ __forceinline__ void mutation_masks(const PopDev& P, const DevStatus& st, const RowArgs& R, uint32_t w,
@@ -565,7 +618,7 @@ __device__ __forceinline__ void row_mutations(const PopDev& P, uint32_t M, const
 // the new alleles added; the bottom-strand registers of the crossover loop
 // hold more of the top strand here, six chunks ahead.
 __device__ __forceinline__ void row_body_copy(const PopDev& P, uint32_t M, const RowArgs& R, const uint64_t* sfix,
-                                              bool do_mut, bool do_fs, uint64_t* sF, uint64_t* sV) {
+                                              bool do_mut, bool do_fs, const Fold& fo) {
     const uint32_t lane = threadIdx.x & 31u;
     constexpr uint32_t D = 6;
     ulonglong2 t[D];
@@ -588,7 +641,7 @@ __device__ __forceinline__ void row_body_copy(const PopDev& P, uint32_t M, const
             if (w < R.Wp) fm = *reinterpret_cast<const ulonglong2*>(sfix + w);
             const uint64_t x0 = (cur.x & ~fm.x) ^ mx0, x1 = (cur.y & ~fm.y) ^ mx1;
             *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(x0, x1);
-            if (do_fs) fold_fs(sF, sV, w, x0, x1);
+            if (do_fs) fold(fo, w, x0, x1);
         }
     }
 }
@@ -600,8 +653,7 @@ __device__ __forceinline__ void row_body_copy(const PopDev& P, uint32_t M, const
 // a barrier and waiting for a bulk copy.  A separate build keeps the wide rows'
 // code as it is (even an untaken branch to this path slowed them 2%).
 __device__ __forceinline__ void row_body_copy_direct(const PopDev& P, uint32_t M, const RowArgs& R,
-                                                  const uint64_t* sfix, bool do_mut, bool do_fs, uint64_t* sF,
-                                                  uint64_t* sV) {
+                                                  const uint64_t* sfix, bool do_mut, bool do_fs, const Fold& fo) {
     const uint32_t lane = threadIdx.x & 31u;
     ulonglong2 t[kDirectCopyChunks];
 #pragma unroll
@@ -620,7 +672,7 @@ __device__ __forceinline__ void row_body_copy_direct(const PopDev& P, uint32_t M
                 w < R.Wp ? *reinterpret_cast<const ulonglong2*>(sfix + w) : make_ulonglong2(0, 0);
             const uint64_t x0 = (t[j].x & ~fm.x) ^ mx0, x1 = (t[j].y & ~fm.y) ^ mx1;
             *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(x0, x1);
-            if (do_fs) fold_fs(sF, sV, w, x0, x1);
+            if (do_fs) fold(fo, w, x0, x1);
         }
     }
     if (R.Wc > 64u * kDirectCopyChunks) {  // a child wider than its parent: the rest is new alleles only
@@ -630,7 +682,7 @@ __device__ __forceinline__ void row_body_copy_direct(const PopDev& P, uint32_t M
             if (do_mut && R.mc) row_mutations(P, M, R, w, mx0, mx1);
             if (w < R.Wc) {
                 *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(mx0, mx1);
-                if (do_fs) fold_fs(sF, sV, w, mx0, mx1);
+                if (do_fs) fold(fo, w, mx0, mx1);
             }
         }
     }
@@ -644,7 +696,7 @@ __device__ __forceinline__ void row_body_copy_direct(const PopDev& P, uint32_t M
 __device__ __forceinline__ bool row_body_copy_bulk(const PopDev& P, uint32_t M, const RowArgs& R,
                                                    const uint64_t* sfix, uint64_t* buf, unsigned long long* bar,
                                                    uint32_t& phase, const uint32_t* wait_limit, bool do_mut,
-                                                   bool do_fs, uint64_t* sF, uint64_t* sV) {
+                                                   bool do_fs, const Fold& fo) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t bytes = R.Wp * 8u;
     bool ok = true;
@@ -674,7 +726,7 @@ __device__ __forceinline__ bool row_body_copy_bulk(const PopDev& P, uint32_t M, 
             }
             const uint64_t x0 = (t.x & ~fm.x) ^ mx0, x1 = (t.y & ~fm.y) ^ mx1;
             *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(x0, x1);
-            if (do_fs) fold_fs(sF, sV, w, x0, x1);
+            if (do_fs) fold(fo, w, x0, x1);
         }
     }
     __syncwarp();
@@ -687,7 +739,7 @@ __device__ __forceinline__ bool row_body_copy_bulk(const PopDev& P, uint32_t M, 
 template <int MODE, bool PROF = false>
 __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const RowArgs& R, const uint64_t* sfix,
                                              uint64_t* mask, uint32_t* Q, bool inv, bool do_mut, bool gather,
-                                             bool do_fs, uint64_t* sF, uint64_t* sV, float (&d)[kMaxTraits],
+                                             bool do_fs, const Fold& fo, float (&d)[kMaxTraits],
                                              unsigned long long* gcyc = nullptr) {
     const uint32_t lane = threadIdx.x & 31u;
     constexpr bool xo = true;
@@ -740,7 +792,7 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
             x0 ^= mx0;
             x1 ^= mx1;
             *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(x0, x1);
-            if (do_fs) fold_fs(sF, sV, w, x0, x1);
+            if (do_fs) fold(fo, w, x0, x1);
         }
         t_a = t_b; b_a = b_b;
     }
@@ -757,10 +809,9 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
 }
 
 __device__ CLOTHO_COLD float4 row_body_events(const PopDev& P, uint32_t M, const RowArgs R, const uint64_t* sfix,
-                                               uint32_t* Q, bool do_mut, bool gather, bool do_fs, uint64_t* sF,
-                                               uint64_t* sV) {
+                                               uint32_t* Q, bool do_mut, bool gather, bool do_fs, const Fold& fo) {
     float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
-    row_body_suf<1>(P, M, R, sfix, nullptr, Q, false, do_mut, gather, do_fs, sF, sV, d);
+    row_body_suf<1>(P, M, R, sfix, nullptr, Q, false, do_mut, gather, do_fs, fo, d);
     return make_float4(d[0], d[1], d[2], d[3]);
 }
 
@@ -786,8 +837,8 @@ struct PhaseClk {
 template <bool PROF, bool NARROW>
 __device__ __forceinline__ bool gen_row_suf(const PopDev& P, const DevStatus& st, uint32_t v, const uint64_t* sfix,
                                             uint64_t* mask, WarpSmem& ws, uint32_t& phase,
-                                            const uint32_t* wait_limit, bool do_mut, bool do_ph, bool gather, bool do_fs, uint64_t* sF,
-                                            uint64_t* sV, PhaseClk& pc) {
+                                            const uint32_t* wait_limit, bool do_mut, bool do_ph, bool gather, bool do_fs,
+                                            const Fold& fo, PhaseClk& pc) {
     const uint32_t lane = threadIdx.x & 31u;
     const long long c0 = PROF ? clock64() : 0;
     long long c1 = 0, c2 = 0, c3 = 0;
@@ -816,15 +867,15 @@ __device__ __forceinline__ bool gen_row_suf(const PopDev& P, const DevStatus& st
     bool landed = true;
     if (PROF) c1 = clock64();
     if (flags & kPlanLong) {
-        add4(d, row_body_events(P, st.M, R, sfix, ws.q, do_mut, gather, do_fs, sF, sV));
+        add4(d, row_body_events(P, st.M, R, sfix, ws.q, do_mut, gather, do_fs, fo));
     } else if (E == 0) {
 #if CLOTHO_COPY_BULK
         if (NARROW)
-            row_body_copy_direct(P, st.M, R, sfix, do_mut, do_fs, sF, sV);
+            row_body_copy_direct(P, st.M, R, sfix, do_mut, do_fs, fo);
         else
-            landed = row_body_copy_bulk(P, st.M, R, sfix, mask, &ws.mbar, phase, wait_limit, do_mut, do_fs, sF, sV);
+            landed = row_body_copy_bulk(P, st.M, R, sfix, mask, &ws.mbar, phase, wait_limit, do_mut, do_fs, fo);
 #else
-        row_body_copy(P, st.M, R, sfix, do_mut, do_fs, sF, sV);
+        row_body_copy(P, st.M, R, sfix, do_mut, do_fs, fo);
 #endif
     } else {
         uint32_t* m32 = reinterpret_cast<uint32_t*>(mask);
@@ -914,7 +965,7 @@ __device__ __forceinline__ bool gen_row_suf(const PopDev& P, const DevStatus& st
         }
         __syncwarp();
         if (PROF) c2 = clock64();
-        row_body_suf<0, PROF>(P, st.M, R, sfix, mask, ws.q, inv, do_mut, gather, do_fs, sF, sV, d,
+        row_body_suf<0, PROF>(P, st.M, R, sfix, mask, ws.q, inv, do_mut, gather, do_fs, fo, d,
                               &pc.c[kPhXoGather]);
     }
     if (PROF) c3 = clock64();
@@ -1061,7 +1112,7 @@ enum XoKind : int { kXoCopy = 0, kXoIv4 = 4, kXoIv8 = 8, kXoFar = -1, kXoEvents 
 template <int KIND>
 __device__ __forceinline__ void row_body_iv(const PopDev& P, const DevStatus& st, const RowArgs& R,
                                             const uint64_t* sfix, const RowXo& X, uint32_t* Q, uint32_t* SM,
-                                            bool do_mut, bool gather, bool do_fs, uint64_t* sF, uint64_t* sV,
+                                            bool do_mut, bool gather, bool do_fs, const Fold& fo,
                                             float (&d)[kMaxTraits]) {
     const uint32_t lane = threadIdx.x & 31u;
     constexpr bool xo = (KIND != kXoCopy);
@@ -1113,7 +1164,7 @@ __device__ __forceinline__ void row_body_iv(const PopDev& P, const DevStatus& st
             x0 ^= mx0;
             x1 ^= mx1;
             *reinterpret_cast<ulonglong2*>(R.out + w) = make_ulonglong2(x0, x1);
-            if (do_fs) fold_fs(sF, sV, w, x0, x1);
+            if (do_fs) fold(fo, w, x0, x1);
         }
         t_a = t_b; b_a = b_b;
         t_b = t_c; b_b = b_c;
@@ -1123,7 +1174,7 @@ __device__ __forceinline__ void row_body_iv(const PopDev& P, const DevStatus& st
 // One offspring row, the whole warp (interval classifier).
 __device__ __forceinline__ void gen_row_iv(const PopDev& P, const DevStatus& st, uint32_t g, const uint64_t* sfix,
                                            uint2* s_iv, uint32_t* s_thr, uint32_t* Q, uint32_t* SM, bool do_mut,
-                                           bool do_ph, bool gather, bool do_fs, uint64_t* sF, uint64_t* sV) {
+                                           bool do_ph, bool gather, bool do_fs, const Fold& fo) {
     const uint32_t lane = threadIdx.x & 31u;
     RowArgs R;
     float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
@@ -1185,11 +1236,11 @@ __device__ __forceinline__ void gen_row_iv(const PopDev& P, const DevStatus& st,
         kind = kXoEvents;  // tape rows with very long event lists
     }
     switch (kind) {
-        case kXoCopy: row_body_iv<kXoCopy>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, sF, sV, d); break;
-        case kXoIv4: row_body_iv<kXoIv4>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, sF, sV, d); break;
-        case kXoIv8: row_body_iv<kXoIv8>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, sF, sV, d); break;
-        case kXoFar: row_body_iv<kXoFar>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, sF, sV, d); break;
-        default: row_body_iv<kXoEvents>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, sF, sV, d); break;
+        case kXoCopy: row_body_iv<kXoCopy>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, fo, d); break;
+        case kXoIv4: row_body_iv<kXoIv4>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, fo, d); break;
+        case kXoIv8: row_body_iv<kXoIv8>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, fo, d); break;
+        case kXoFar: row_body_iv<kXoFar>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, fo, d); break;
+        default: row_body_iv<kXoEvents>(P, st, R, sfix, X, Q, SM, do_mut, gather, do_fs, fo, d); break;
     }
     if (do_ph) row_phenotype(P, st, g, R, d);
 }
@@ -1202,7 +1253,10 @@ __device__ __forceinline__ void gen_row_iv(const PopDev& P, const DevStatus& st,
 // accumulators and the fixed mask is read from global memory.
 // PROF (suffix-table build only): per-phase cycle counters into ctl->phase.
 // NARROW (suffix-table build only): every row is at most 128 words.
-template <bool SUF, bool PROF, bool NARROW>
+// CNT (suffix-table builds, shared accumulators): per-column counts of the child rows of the populations
+// that asked (DevStatus::count_cols), in kCountPlanes bit-sliced planes after the WarpSmem array, flushed to
+// PopDev::colcnt when the block moves to another population and at the kernel's end.
+template <bool SUF, bool PROF, bool NARROW, bool CNT = false>
 __global__ void __launch_bounds__(kGenThreads, 1)
 k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restrict__ ctl, uint32_t fuse,
              int profile, uint32_t maxW, uint32_t gacc) {
@@ -1217,6 +1271,7 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     __shared__ uint32_t s_q[kIvWarps][kQueueCap];
     __shared__ uint32_t s_sm[kIvWarps][128];
     __shared__ uint32_t s_item, s_next;
+    __shared__ uint32_t s_crows;   // CNT, one population: rows the block has counted
     uint64_t* sF = s_dyn;
     uint64_t* sV = s_dyn + maxW;
     uint64_t* sfix = s_dyn + 2u * maxW;
@@ -1235,8 +1290,16 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
         __syncwarp();
     }
     const bool do_mut = (fuse & kFuseMut) != 0, do_ph = (fuse & kFusePheno) != 0, do_fs = (fuse & kFuseFs) != 0;
+    uint64_t* const cplanes =
+        CNT ? reinterpret_cast<uint64_t*>(reinterpret_cast<WarpSmem*>(s_dyn + (3u + kWarps) * maxW) + kWarps) : nullptr;
+    if (CNT) {
+        for (uint32_t i = threadIdx.x; i < kCountPlanes * maxW; i += blockDim.x) cplanes[i] = 0ull;
+        if (threadIdx.x == 0) s_crows = 0u;
+    }
     int cur_pop = -1;
-    uint32_t cur_W = 0;
+    uint32_t cur_W = 0, cur_A = 0;
+    bool cur_cnt = false;      // CNT: the block's current population counts columns
+    uint32_t crows = 0;        // CNT, batches: rows the block has counted since its last flush (block-uniform)
     uint64_t rows_done = 0, words_done = 0;
 
     if (npops == 1) {
@@ -1260,6 +1323,9 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
         const bool gather = do_ph && st.nz_eff != 0;
         const uint32_t S = 2u * st.N;
         const uint32_t Se = (S + 1u) >> 1;
+        cur_A = st.A;
+        cur_cnt = CNT && do_fs && !gacc && st.count_cols != 0u;
+        Fold fo{sF, sV, cur_cnt ? cplanes : nullptr, maxW};
         // the next claim is taken before the current rows run, so its
         // round trip to the counter is hidden behind them
         uint32_t claim = 0;
@@ -1271,15 +1337,24 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             const uint32_t k1 = min(S, k + kWarpChunk);
             for (uint32_t v = k; v < k1; ++v) {
                 const uint32_t g = v < Se ? 2u * v : 2u * (v - Se) + 1u;
+                if (CNT && fo.cnt) {  // a block counts at most kCountMax rows (one flush, at the end)
+                    uint32_t n = 0;
+                    if (lane == 0) n = atomicAdd(&s_crows, 1u);
+                    n = __shfl_sync(0xffffffffu, n, 0);
+                    if (n >= kCountMax) {
+                        if (lane == 0 && n == kCountMax) atomicAnd(&P.st->cols_valid, 0u);
+                        fo.cnt = nullptr;
+                    }
+                }
                 if (SUF) {
                     if (!gen_row_suf<PROF, NARROW>(P, st, v, sfix, mask, ws, bphase, wait_limit, do_mut, do_ph,
-                                                   gather, do_fs, sF, sV, pc)) {
+                                                   gather, do_fs, fo, pc)) {
                         ws.dead = 1u;
                         break;
                     }
                 } else
                     gen_row_iv(P, st, g, sfix, s_iv[warp], s_thr[warp], s_q[warp], s_sm[warp], do_mut, do_ph,
-                               gather, do_fs, sF, sV);
+                               gather, do_fs, fo);
                 if (profile && lane == 0) { rows_done += 1; words_done += st.W; }
             }
             if (SUF && ws.dead) break;  // no further row: the warp leaves the loop
@@ -1316,10 +1391,14 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
                     atomicAnd((unsigned long long*)&Q.accF[w], (unsigned long long)sF[w]);
                     atomicOr((unsigned long long*)&Q.accV[w], (unsigned long long)sV[w]);
                 }
+                if (CNT && cur_cnt) count_flush(cplanes, maxW, cur_W, cur_A, Q.colcnt);
             }
             __syncthreads();
             cur_pop = (int)p;
             cur_W = st.W;
+            cur_A = st.A;
+            cur_cnt = CNT && do_fs && st.count_cols != 0u;
+            crows = 0;
             if (do_fs)
                 for (uint32_t w = threadIdx.x; w < cur_W; w += blockDim.x) { sF[w] = ~0ull; sV[w] = 0ull; }
             for (uint32_t w = threadIdx.x; w < st.pW; w += blockDim.x) sfix[w] = P.fixmask[w];
@@ -1332,6 +1411,15 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
         const uint32_t r0 = (item - ctl->item_base[p]) * rpi;
         const uint32_t r1 = min(S, r0 + rpi);
         const uint32_t Se = (S + 1u) >> 1;
+        if (CNT && cur_cnt && !gacc) {  // block-uniform: flush before the counters could overflow
+            if (crows + (r1 - r0) > kCountMax) {
+                count_flush(cplanes, maxW, cur_W, cur_A, P.colcnt);
+                __syncthreads();
+                crows = 0;
+            }
+            crows += r1 - r0;
+        }
+        const Fold fo{sF, sV, (CNT && cur_cnt && !gacc) ? cplanes : nullptr, maxW};
         // narrow build: each warp claims its next row one ahead and fetches that row's plan entries into L1
         // behind the current row (narrow rows are bound by their chains of dependent loads)
         uint32_t kc = 0;
@@ -1365,11 +1453,11 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
                 // block's barriers
                 if (ws.dead) continue;
                 if (!gen_row_suf<PROF, NARROW>(P, st, v, sfix, mask, ws, bphase, wait_limit, do_mut, do_ph, gather,
-                                               do_fs, sF, sV, pc))
+                                               do_fs, fo, pc))
                     ws.dead = 1u;
             } else
                 gen_row_iv(P, st, g, sfix, s_iv[warp], s_thr[warp], s_q[warp], s_sm[warp], do_mut, do_ph, gather,
-                           do_fs, sF, sV);
+                           do_fs, fo);
             if (profile && lane == 0) { rows_done += 1; words_done += st.W; }
         }
         __syncthreads();
@@ -1381,6 +1469,7 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             atomicAnd((unsigned long long*)&Q.accF[w], (unsigned long long)sF[w]);
             atomicOr((unsigned long long*)&Q.accV[w], (unsigned long long)sV[w]);
         }
+        if (CNT && cur_cnt) count_flush(cplanes, maxW, cur_W, cur_A, Q.colcnt);
     }
     if (PROF && lane == 0) {
         pc.c[kPhWarpCyc] = (unsigned long long)(clock64() - c_start);
@@ -1397,25 +1486,39 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
 // The suffix-table classifier runs when every population has a table
 // (capacity <= kSufMaxSlots slots, so maxW <= 1,024 words).  Returns the error of
 // the shared-memory opt-in (the kernel is not launched then), else cudaSuccess.
+namespace {
+constexpr size_t kSmemLimit = 227u * 1024u;   // dynamic shared memory a block may opt into
+size_t suf_smem(uint32_t maxW, bool count) {
+    return (3ull + kWarps + (count ? kCountPlanes : 0u)) * maxW * sizeof(uint64_t) + kWarps * sizeof(WarpSmem);
+}
+}  // namespace
+
+bool generation_counts_fit(uint32_t maxW, uint32_t maxA) {
+    return maxA <= kSufMaxSlots && suf_smem(maxW, true) <= kSmemLimit;
+}
+
 cudaError_t launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, WorkCtl* ctl, uint32_t maxW,
-                              uint32_t maxA, uint32_t fuse, int profile) {
+                              uint32_t maxA, uint32_t fuse, int profile, bool count_on) {
     const bool suf = maxA <= kSufMaxSlots;
     // the interval classifier keeps 3.5 KB of static shared memory per warp
     const uint32_t gacc = (!suf && 3ull * maxW * sizeof(uint64_t) + kWarps * 3584u > 220u * 1024u) ? 1u : 0u;
-    const size_t smem =
-        gacc ? 0 : (3ull + (suf ? kWarps : 0u)) * maxW * sizeof(uint64_t) + (suf ? kWarps * sizeof(WarpSmem) : 0);
+    // the counting build: column counters in shared memory (the phase-clock builds do not count)
+    const bool cnt = count_on && profile != 2 && generation_counts_fit(maxW, maxA);
+    const size_t smem = gacc ? 0 : suf ? suf_smem(maxW, cnt) : 3ull * maxW * sizeof(uint64_t);
     // profile 2: the suffix-table kernel's build with phase clocks; rows of at most
     // 128 words: its narrow build (copy rows by direct loads)
     const bool narrow = L.narrow_ok && maxW <= 64u * kDirectCopyChunks;
-    const int si = suf ? (profile == 2 ? (narrow ? 4 : 2) : narrow ? 3 : 1) : 0;
-    const void* fns[5] = {(const void*)k_generation<false, false, false>, (const void*)k_generation<true, false, false>,
+    const int si = suf ? (profile == 2 ? (narrow ? 4 : 2) : cnt ? (narrow ? 6 : 5) : narrow ? 3 : 1) : 0;
+    const void* fns[7] = {(const void*)k_generation<false, false, false>, (const void*)k_generation<true, false, false>,
                           (const void*)k_generation<true, true, false>, (const void*)k_generation<true, false, true>,
-                          (const void*)k_generation<true, true, true>};
+                          (const void*)k_generation<true, true, true>,
+                          (const void*)k_generation<true, false, false, true>,
+                          (const void*)k_generation<true, false, true, true>};
     // static shared memory is above 48 KB on its own, so the opt-in attribute is always needed; it is a
     // property of the function on each device, so it is kept per device (host threads share the table)
     {
         static std::mutex mu;
-        static size_t configured[kMaxGenDevices][5] = {};
+        static size_t configured[kMaxGenDevices][7] = {};
         int dev = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e != cudaSuccess) return e;
@@ -1428,21 +1531,35 @@ cudaError_t launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t n
             c = smem > 0 ? smem : 1;
         }
     }
-    if (si == 4)
-        k_generation<true, true, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
-                                                                                  maxW, 0u);
-    else if (si == 3)
-        k_generation<true, false, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
-                                                                                   maxW, 0u);
-    else if (si == 2)
-        k_generation<true, true, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
-                                                                                   maxW, 0u);
-    else if (si == 1)
-        k_generation<true, false, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
-                                                                                    maxW, 0u);
-    else
-        k_generation<false, false, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
-                                                                                     maxW, gacc);
+    switch (si) {
+        case 6:
+            k_generation<true, false, true, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse,
+                                                                                              profile, maxW, 0u);
+            break;
+        case 5:
+            k_generation<true, false, false, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse,
+                                                                                               profile, maxW, 0u);
+            break;
+        case 4:
+            k_generation<true, true, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
+                                                                                      maxW, 0u);
+            break;
+        case 3:
+            k_generation<true, false, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
+                                                                                       maxW, 0u);
+            break;
+        case 2:
+            k_generation<true, true, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
+                                                                                       maxW, 0u);
+            break;
+        case 1:
+            k_generation<true, false, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse,
+                                                                                        profile, maxW, 0u);
+            break;
+        default:
+            k_generation<false, false, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse,
+                                                                                         profile, maxW, gacc);
+    }
     return cudaSuccess;
 }
 

@@ -5,7 +5,9 @@ admitted when a population slot is free and its bitset footprint fits the
 device budget; admitted jobs stay resident, and every step advances all of
 them by one device-drawn generation in one launch per stage.  Jobs that reach
 their generation count leave with their result (site-frequency spectrum,
-mean fitness, segregating sites), which frees memory for the queue.  Each
+mean fitness, segregating sites), which frees memory for the queue; their
+column counts are taken inside the generation kernel during their last chunk
+of generations, so the spectrum costs no extra pass over their rows.  Each
 job's draws depend only on its own seed and generation counter, so its
 result is the same alone and in the mix.
 
@@ -71,6 +73,7 @@ class Server:
         self.finished: list[Job] = []
         self.used = 0
         self.steps = 0
+        self.counting: set[int] = set()   # resident indices whose population counts its columns
 
     def submit(self, job: Job):
         self.queue.append(job)
@@ -102,6 +105,13 @@ class Server:
             self.batch.remove(i)
             self.used -= footprint_of(job.desc())
             self.finished.append(job)
+        # indices above a removed population shift down by one
+        shifted = set()
+        for c in self.counting:
+            if c in done_idx:
+                continue
+            shifted.add(c - sum(1 for d in done_idx if d < c))
+        self.counting = shifted
         for i, (job, g) in enumerate(self.resident):
             if i not in done_idx:
                 keep.append((job, g))
@@ -115,6 +125,12 @@ class Server:
         # chunk length retire inside it
         left = min(job.G - g for job, g in self.resident)
         k = max(1, min(left, 8))
+        # jobs that finish in this chunk count their columns inside its generations, so their SFS is
+        # read at retirement without another pass over the rows
+        for i, (job, g) in enumerate(self.resident):
+            if job.G - g <= k and i not in self.counting:
+                self.batch.count_columns(i, True)
+                self.counting.add(i)
         self.batch.run(k)
         self.batch.sync()
         self.resident = [(job, g + k) for job, g in self.resident]

@@ -327,6 +327,17 @@ int  clotho_pop_stats(clotho_ctx *ctx, uint32_t index, clotho_stats *out, uint32
 int  clotho_pop_margins(clotho_ctx *ctx, uint32_t index, uint32_t *col_counts, uint32_t *row_counts);
 int  clotho_pop_pairwise_difference(clotho_ctx *ctx, uint32_t index, const uint32_t *sample, uint32_t n,
                                     uint32_t *dist, clotho_pairwise *out);
+/* Column counts fused into the generation step.  With enable = 1 every later
+ * fused step of population `index` also counts, for each allele slot, the
+ * child rows that carry it (bit-sliced counters in the generation kernel's
+ * shared memory, added as each child word is finished), so that
+ * clotho_pop_stats / clotho_stats_compute read the counts instead of making a
+ * pass over the rows (the allele_frequency analysis,
+ * population_space_row_frequency_evaluator.hpp:37-62).  The counting build
+ * runs while a population asks for it and its rows are at most 712 words;
+ * otherwise the statistics count on demand as before.  enable = 0 stops it.
+ * Works on single-population contexts with index 0. */
+int  clotho_pop_count_columns(clotho_ctx *ctx, uint32_t index, int enable);
 /* One device-drawn generation of every population (N[i] offspring). */
 int  clotho_batch_generation_philox(clotho_ctx *ctx, const uint32_t *N);
 /* G such generations, replayed from one captured CUDA graph. */

@@ -205,3 +205,92 @@ def test_device_draws_match_neutral_theory():
     xi = np.mean(sfs, axis=0)                      # sites carried by 1, 2, 3 sequences
     assert np.all(np.abs(xi / xi_expect[:3] - 1.0) < 0.05), (xi, xi_expect[:3])
     b.close()
+
+
+def _columns(rows, A):
+    S = rows.shape[0]
+    return np.unpackbits(rows.view(np.uint8).reshape(S, -1), axis=1, bitorder="little")[:, :A].sum(axis=0)
+
+
+@pytest.mark.parametrize("cap", [8192, 1 << 14])
+def test_fused_column_counts_equal_the_rows(cap):
+    # populations that count their columns inside the generation step (bit-sliced counters in the kernel's
+    # shared memory): their statistics, read from those counts, equal numpy over their rows and the
+    # on-demand pass over the rows; counting changes no row, and the populations that do not count are
+    # untouched (8,192 slots: the narrow build; 16,384: the wide one)
+    G = 5
+    descs = [cg.make_desc(s["N"], cap, s["T"], p_neutral=0.3, **{k: v for k, v in s.items() if k not in ("N", "T")})
+             for s in SPECS]
+    a = cg.Batch(descs)
+    a.init()
+    b = cg.Batch(descs)
+    b.init()
+    for i in (0, 1, 3):
+        a.count_columns(i)
+    a.run(G)
+    b.run(G)
+    for i in range(len(SPECS)):
+        ra = a.rows(i)
+        assert np.array_equal(ra, b.rows(i)) and a.info(i)["device_error"] == 0
+        S, A = ra.shape[0], a.info(i)["A"]
+        col = _columns(ra, A)
+        sa, sb = a.stats(i, S + 1), b.stats(i, S + 1)
+        assert np.array_equal(sa["sfs"], np.bincount(col, minlength=S + 1)[:S + 1])
+        assert np.array_equal(sa["sfs"], sb["sfs"])
+        assert sa["segregating"] == int(((col > 0) & (col < S)).sum())
+        f = col / S
+        assert abs(sa["heterozygosity"] - np.sum(2 * f * (1 - f))) <= 1e-9 * max(1.0, sa["heterozygosity"])
+        assert sa["mean_fitness"] == sb["mean_fitness"]
+        mcol, _ = a.margins(i)   # the on-demand pass
+        assert np.array_equal(mcol, col)
+    a.close()
+    b.close()
+
+
+def test_fused_column_counts_of_one_population():
+    s = SPECS[1]
+    d = desc_of(s)
+    pop = cg.Population(s["N"], 1 << 14, s["T"], mu=s["mu"], rho=s["rho"], fitness=s["fitness"], p_neutral=0.3,
+                        seed=s["seed"], max_events=d.max_events, max_mutations=d.max_mutations)
+    pop.init(s["N"])
+    pop.count_columns()
+    pop.run_philox(s["N"], 6)
+    pop.check()
+    rows = pop.rows()
+    S, A = rows.shape[0], pop.info()["A"]
+    col = _columns(rows, A)
+    st = pop.stats(S + 1)
+    assert np.array_equal(st["sfs"], np.bincount(col, minlength=S + 1)[:S + 1])
+    assert abs(st["mean_fitness"] - pop.fitness().mean()) <= 1e-12 * pop.fitness().mean()
+    pop.count_columns(False)
+    pop.run_philox(s["N"], 1)
+    rows = pop.rows()
+    assert np.array_equal(pop.stats(S + 1)["sfs"], np.bincount(_columns(rows, pop.info()["A"]), minlength=S + 1)[:S + 1])
+
+
+def test_served_job_results_match_numpy_on_the_rows():
+    # every field of a served job's result -- the 64-bin spectrum (counted inside its last chunk of
+    # generations), segregating sites, mean fitness, generation, device error -- against numpy over the same
+    # job run alone
+    jobs = serving.synthetic_jobs(12, rate=500.0, seed=8, N_range=(200, 3000), G_range=(5, 30))
+    srv = serving.Server(budget_bytes=8 << 30, max_slots=5)
+    srv.run_open_loop(jobs)
+    assert len(srv.finished) == 12
+    for j in srv.finished:
+        d = j.desc()
+        pop = cg.Population(j.N, j.max_alleles(), j.T, mu=j.mu, rho=j.rho, fitness=j.fitness, fit_param=j.fit_param,
+                            p_neutral=j.p_neutral, seed=j.seed, max_events=d.max_events,
+                            max_mutations=d.max_mutations, max_fixed=d.max_fixed)
+        pop.init(j.N)
+        pop.run_philox(j.N, j.G)
+        rows = pop.rows()
+        S, A = rows.shape[0], pop.info()["A"]
+        col = _columns(rows, A)
+        sfs = np.bincount(np.minimum(col, 63), minlength=64)[:64]
+        fit = pop.fitness()
+        r = j.result
+        assert r["sfs"] == sfs.tolist(), j.id
+        assert r["segregating"] == int(((col > 0) & (col < S)).sum())
+        assert abs(r["mean_fitness"] - fit.mean()) <= 1e-12 * max(1.0, abs(fit.mean()))
+        assert r["generation"] == j.G and r["device_error"] == 0
+        pop.close()

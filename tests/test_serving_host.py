@@ -16,18 +16,23 @@ from clotho_gb300 import autotune, serving
 
 
 class FakeBatch:
-    """Resident populations as a list of [seed, generations run]; `run(k)`
-    advances all of them, `stats`/`info` report the population at an index."""
+    """Resident populations as a list of [seed, generations run, generation at which column counting was
+    switched on]; `run(k)` advances all of them, `stats`/`info` report the population at an index."""
 
     def __init__(self):
         self.pops = []
         self.runs = []
         self.peak = 0
+        self.counted = []      # (seed, generations run, counting since) of every population read by stats
 
     def add(self, desc, N0=None):
-        self.pops.append([desc.seed, 0])
+        self.pops.append([desc.seed, 0, None])
         self.peak = max(self.peak, len(self.pops))
         return len(self.pops) - 1
+
+    def count_columns(self, i, enable=True):
+        assert enable and self.pops[i][2] is None
+        self.pops[i][2] = self.pops[i][1]
 
     def remove(self, i):
         del self.pops[i]
@@ -41,7 +46,8 @@ class FakeBatch:
         pass
 
     def stats(self, i, sfs_len=0):
-        seed, gens = self.pops[i]
+        seed, gens, since = self.pops[i]
+        self.counted.append((seed, gens, since))
         d = {"segregating": seed % 1000, "mean_fitness": float(seed), "fixed_now": 0, "heterozygosity": 0.0}
         if sfs_len:
             d["sfs"] = np.full(sfs_len, seed % 7, np.uint32)
@@ -89,6 +95,11 @@ def test_every_job_runs_exactly_its_generations_and_gets_its_own_result(fake):
         assert j.result["sfs"] == [j.seed % 7] * 4
         assert j.admitted <= j.done
     assert all(1 <= k <= 8 for k, _ in b.runs)
+    # every job counted its columns during its last chunk of generations only (the chunk is at most 8)
+    by_seed = {j.seed: j for j in srv.finished}
+    assert len(b.counted) == 40
+    for seed, gens, since in b.counted:
+        assert since is not None and by_seed[seed].G - 8 <= since < gens == by_seed[seed].G
 
 
 def test_admission_keeps_the_budget(fake):
