@@ -122,6 +122,8 @@ struct clotho_ctx {
     std::vector<uint32_t> graph_key;
     bool in_step = false;
     uint32_t maxW = 0, maxS = 0, maxN = 0, maxNB = 0, maxA = 0;
+    // per classifier: populations of at most kSufMaxSlots slots (suffix table) and the others (intervals)
+    uint32_t n_suf = 0, n_iv = 0, maxW_suf = 0, maxW_iv = 0, maxA_suf = 0, maxA_iv = 0;
     cudaError_t launch_err = cudaSuccess;  // a launch set-up failure, reported by the next check_launch
     uint32_t ind_per_sm = 16;               // tuning (clotho_set_tuning)
     bool narrow_ok = true;
@@ -290,12 +292,23 @@ int sync_pop_arrays(clotho_ctx* ctx, uint32_t from = 0) {
                            ctx->stream));
     }
     ctx->maxW = ctx->maxS = ctx->maxN = ctx->maxNB = ctx->maxA = 0;
+    ctx->n_suf = ctx->n_iv = ctx->maxW_suf = ctx->maxW_iv = ctx->maxA_suf = ctx->maxA_iv = 0;
     for (PopHost* p : ctx->pops) {
-        ctx->maxW = std::max(ctx->maxW, p->dev[0].Wcap);
-        ctx->maxS = std::max(ctx->maxS, p->dev[0].Scap);
-        ctx->maxN = std::max(ctx->maxN, p->dev[0].Ncap);
-        ctx->maxNB = std::max(ctx->maxNB, p->dev[0].NB);
-        ctx->maxA = std::max(ctx->maxA, p->dev[0].Acap);
+        const PopDev& D = p->dev[0];
+        ctx->maxW = std::max(ctx->maxW, D.Wcap);
+        ctx->maxS = std::max(ctx->maxS, D.Scap);
+        ctx->maxN = std::max(ctx->maxN, D.Ncap);
+        ctx->maxNB = std::max(ctx->maxNB, D.NB);
+        ctx->maxA = std::max(ctx->maxA, D.Acap);
+        if (D.Acap <= kSufMaxSlots) {
+            ctx->n_suf += 1;
+            ctx->maxW_suf = std::max(ctx->maxW_suf, D.Wcap);
+            ctx->maxA_suf = std::max(ctx->maxA_suf, D.Acap);
+        } else {
+            ctx->n_iv += 1;
+            ctx->maxW_iv = std::max(ctx->maxW_iv, D.Wcap);
+            ctx->maxA_iv = std::max(ctx->maxA_iv, D.Acap);
+        }
     }
     if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
     CK(cudaStreamSynchronize(ctx->stream));
@@ -347,21 +360,30 @@ int prof_collect(clotho_ctx* ctx) {
 // The fused step's generation kernel counts columns (its counting build) when a population asked and the
 // counters fit in shared memory; k_fs_finalize of the same step zeroes those counts and marks them valid.
 bool count_on(clotho_ctx* ctx, uint32_t fuse) {
-    return ctx->counting > 0 && (fuse & kFuseFs) && !(ctx->profiling && ctx->phase_clocks) &&
-           generation_counts_fit(ctx->maxW, ctx->maxA);
+    return ctx->counting > 0 && ctx->n_suf > 0 && (fuse & kFuseFs) && !(ctx->profiling && ctx->phase_clocks) &&
+           generation_counts_fit(ctx->maxW_suf, ctx->maxA_suf);
 }
 
+// The generation kernel over every population: one launch when all populations use the same classifier;
+// in a batch that mixes them, one launch per classifier, each over its own populations (the suffix-table
+// pass first), so every population runs the classifier it runs alone.
 void launch_gen(clotho_ctx* ctx, const PopDev* pops, uint32_t npops, uint32_t fuse) {
-    if (ctx->maxA <= kSufMaxSlots) {  // per-row crossover plans of the suffix-table classifier
+    if (ctx->n_suf > 0) {  // per-row crossover plans of the suffix-table classifier (other populations skip it)
         launch_plan(cfg(ctx), pops, npops, ctx->maxS);
         ctx->launches += 6;  // order count, 3-kernel scan, order scatter, plan
     }
-    prof_begin(ctx);
-    const cudaError_t e = launch_generation(cfg(ctx), pops, npops, ctx->d_ctl, ctx->maxW, ctx->maxA, fuse,
-                                            ctx->profiling ? (ctx->phase_clocks ? 2 : 1) : 0, count_on(ctx, fuse));
-    if (e != cudaSuccess && ctx->launch_err == cudaSuccess) ctx->launch_err = e;
-    prof_end(ctx);
-    ctx->launches += 1;
+    const int prof = ctx->profiling ? (ctx->phase_clocks ? 2 : 1) : 0;
+    const bool mixed = ctx->n_suf > 0 && ctx->n_iv > 0;
+    const bool cnt = count_on(ctx, fuse);
+    for (int pass = 0; pass < (mixed ? 2 : 1); ++pass) {
+        const uint32_t W = mixed ? (pass == 0 ? ctx->maxW_suf : ctx->maxW_iv) : ctx->maxW;
+        const uint32_t A = mixed ? (pass == 0 ? ctx->maxA_suf : ctx->maxA_iv) : ctx->maxA;
+        prof_begin(ctx);
+        const cudaError_t e = launch_generation(cfg(ctx), pops, npops, ctx->d_ctl, W, A, fuse, prof, cnt, mixed);
+        if (e != cudaSuccess && ctx->launch_err == cudaSuccess) ctx->launch_err = e;
+        prof_end(ctx);
+        ctx->launches += 1;
+    }
 }
 
 template <class T>
@@ -425,7 +447,7 @@ void enqueue_fused_step(clotho_ctx* ctx, uint32_t set, bool philox) {
     launch_fs_finalize(L, pops, n, count_on(ctx, kFuseMut | kFusePheno | kFuseFs));
     if (!philox) launch_mut_csr_tape(L, pops, n, ctx->maxS);
     launch_mut_resolve(L, pops, n);
-    launch_ranks(L, pops, n, ctx->maxNB, ctx->maxW, ctx->maxA <= kSufMaxSlots);
+    launch_ranks(L, pops, n, ctx->maxNB, ctx->maxW_suf, ctx->n_suf > 0);
     if (philox) launch_select_philox(L, pops, n);
     launch_gen(ctx, pops, n, kFuseMut | kFusePheno | kFuseFs);
     launch_individuals(L, pops, n);
@@ -433,7 +455,7 @@ void enqueue_fused_step(clotho_ctx* ctx, uint32_t set, bool philox) {
     launch_end(L, pops, n);
     // begin, mutation counts or CSR (4 or 6), finalize, resolve, ranks (6, + suffix table), selection (device
     // draws), individuals, 3-kernel prefix sum, end; launch_gen and ensure_parent_acc count their own
-    ctx->launches += 19u + (philox ? 0u : 1u) + (ctx->maxA <= kSufMaxSlots ? 1u : 0u);
+    ctx->launches += 19u + (philox ? 0u : 1u) + (ctx->n_suf > 0 ? 1u : 0u);
     for (PopHost* p : ctx->pops) p->acc_valid = true;
 }
 

@@ -122,6 +122,7 @@ struct WorkCtl {
     uint32_t rows_per_item;         // scheduling granularity (set by the host)
     uint32_t wait_limit;            // try_wait rounds before a bulk copy is flagged late (0: default)
     uint32_t item_base[257];        // item prefix per population (<= 256 pops)
+    uint32_t gen_counter_iv;        // item counter of the interval-classifier pass of a mixed batch
     uint64_t rows_done;             // profiling: rows processed
     uint64_t words_done;            // profiling: words written
     uint64_t phase[16];             // profiling: k_generation phase cycles (kPh*)
@@ -288,8 +289,12 @@ void launch_mut_csr_tape(const LaunchCfg&, const PopDev* pops, uint32_t npops, u
 void launch_mut_counts_philox(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
 void launch_mut_resolve(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_select_philox(const LaunchCfg&, const PopDev* pops, uint32_t npops);
+// mixed: the batch holds populations of both classifiers (suffix table: capacity <= kSufMaxSlots; intervals:
+// above); this launch runs only the populations of its own classifier (maxW, maxA are theirs) and skips the
+// others' items, so each population keeps its classifier whatever it is batched with
 cudaError_t launch_generation(const LaunchCfg&, const PopDev* pops, uint32_t npops, WorkCtl* ctl,
-                              uint32_t maxW, uint32_t maxA, uint32_t fuse, int profile, bool count_on = false);
+                              uint32_t maxW, uint32_t maxA, uint32_t fuse, int profile, bool count_on = false,
+                              bool mixed = false);
 // whether the generation kernel's counting build fits this launch (suffix-table rows, counters in shared memory)
 bool generation_counts_fit(uint32_t maxW, uint32_t maxA);
 void launch_mut_scatter(const LaunchCfg&, const PopDev* pops, uint32_t npops);

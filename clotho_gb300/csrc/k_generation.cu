@@ -1259,7 +1259,7 @@ __device__ __forceinline__ void gen_row_iv(const PopDev& P, const DevStatus& st,
 template <bool SUF, bool PROF, bool NARROW, bool CNT = false>
 __global__ void __launch_bounds__(kGenThreads, 1)
 k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restrict__ ctl, uint32_t fuse,
-             int profile, uint32_t maxW, uint32_t gacc) {
+             int profile, uint32_t maxW, uint32_t gacc, uint32_t mixed) {
     const long long c_start = PROF ? clock64() : 0;
     PhaseClk pc;
     if (PROF)
@@ -1362,7 +1362,8 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     }
     for (; npops > 1;) {
         if (threadIdx.x == 0) {
-            s_item = atomicAdd(&ctl->gen_counter, 1u);
+            // a mixed batch runs one pass per classifier, each on its own counter over the same items
+            s_item = atomicAdd((SUF || !mixed) ? &ctl->gen_counter : &ctl->gen_counter_iv, 1u);
             s_next = 0;
         }
         __syncthreads();
@@ -1378,6 +1379,10 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             p = lo;
         }
         const PopDev& P = pops[p];
+        if (mixed && (SUF != (P.suf != nullptr))) {  // the other classifier's pass takes this item
+            __syncthreads();
+            continue;
+        }
         const DevStatus st = *P.st;
         if ((int)p != cur_pop && gacc) {
             cur_pop = (int)p;
@@ -1498,7 +1503,8 @@ bool generation_counts_fit(uint32_t maxW, uint32_t maxA) {
 }
 
 cudaError_t launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, WorkCtl* ctl, uint32_t maxW,
-                              uint32_t maxA, uint32_t fuse, int profile, bool count_on) {
+                              uint32_t maxA, uint32_t fuse, int profile, bool count_on, bool mixed) {
+    const uint32_t mx = mixed ? 1u : 0u;
     const bool suf = maxA <= kSufMaxSlots;
     // the interval classifier keeps 3.5 KB of static shared memory per warp
     const uint32_t gacc = (!suf && 3ull * maxW * sizeof(uint64_t) + kWarps * 3584u > 220u * 1024u) ? 1u : 0u;
@@ -1534,31 +1540,31 @@ cudaError_t launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t n
     switch (si) {
         case 6:
             k_generation<true, false, true, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse,
-                                                                                              profile, maxW, 0u);
+                                                                                              profile, maxW, 0u, mx);
             break;
         case 5:
             k_generation<true, false, false, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse,
-                                                                                               profile, maxW, 0u);
+                                                                                               profile, maxW, 0u, mx);
             break;
         case 4:
-            k_generation<true, true, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
-                                                                                      maxW, 0u);
+            k_generation<true, true, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse,
+                                                                                       profile, maxW, 0u, mx);
             break;
         case 3:
-            k_generation<true, false, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
-                                                                                       maxW, 0u);
+            k_generation<true, false, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse,
+                                                                                        profile, maxW, 0u, mx);
             break;
         case 2:
-            k_generation<true, true, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse, profile,
-                                                                                       maxW, 0u);
+            k_generation<true, true, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse,
+                                                                                        profile, maxW, 0u, mx);
             break;
         case 1:
             k_generation<true, false, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse,
-                                                                                        profile, maxW, 0u);
+                                                                                        profile, maxW, 0u, mx);
             break;
         default:
             k_generation<false, false, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse,
-                                                                                         profile, maxW, gacc);
+                                                                                         profile, maxW, gacc, mx);
     }
     return cudaSuccess;
 }

@@ -69,6 +69,7 @@ __global__ void k_begin(const PopDev* __restrict__ pops, uint32_t npops, const u
         ctl->item_base[npops] = acc;
         ctl->gen_items = acc;
         ctl->gen_counter = 0;
+        ctl->gen_counter_iv = 0;
     }
 }
 
@@ -116,6 +117,7 @@ __global__ void __launch_bounds__(1024) k_uscan_a(const PopDev* __restrict__ pop
     for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         const ScanSel Z = scan_sel(P, which);
+        if (!Z.cnt) continue;  // the ordering keys exist only with the suffix-table classifier
         const uint32_t L = Z.L;
         const uint32_t nch = (L + kScanChunk - 1) / kScanChunk;
         for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x) {
@@ -139,7 +141,9 @@ __global__ void k_uscan_b(const PopDev* __restrict__ pops, uint32_t npops, int w
     const uint32_t p = blockIdx.x;
     if (p >= npops || threadIdx.x != 0) return;
     const PopDev& P = pops[p];
-    const uint32_t L = scan_sel(P, which).L;
+    const ScanSel Z = scan_sel(P, which);
+    if (!Z.cnt) return;
+    const uint32_t L = Z.L;
     const uint32_t nch = (L + kScanChunk - 1) / kScanChunk;
     uint32_t acc = 0;
     for (uint32_t c = 0; c < nch; ++c) {
@@ -155,6 +159,7 @@ __global__ void __launch_bounds__(1024) k_uscan_c(const PopDev* __restrict__ pop
     for (uint32_t p = blockIdx.z; p < npops; p += gridDim.z) {
         const PopDev& P = pops[p];
         const ScanSel Z = scan_sel(P, which);
+        if (!Z.cnt) continue;
         const uint32_t S = Z.ncur, L = Z.L;
         const uint32_t nch = (L + kScanChunk - 1) / kScanChunk;
         for (uint32_t c = blockIdx.x; c < nch; c += gridDim.x) {

@@ -78,29 +78,37 @@ def test_narrow_and_wide_builds_agree():
     assert d.max_alleles <= 128 * 64 < desc_of(SPECS[1]).max_alleles
 
 
-def test_interval_and_suffix_classifiers_agree():
-    # a batch holding a population of more than 65,536 slots runs every population on the interval
-    # classifier; alone, a small population runs on the suffix table.  Same rows and spectrum; the carried
-    # phenotypes are summed in different FP32 orders by the two classifiers, so fitness agrees to rounding.
+def test_each_population_keeps_its_classifier_in_a_mixed_batch():
+    # a batch holding a population of more than 65,536 slots (interval classifier) and a small one (suffix
+    # table): the generation kernel runs one pass per classifier, so each population runs the classifier it
+    # runs alone and its rows, spectrum and fitness are bit-identical to its run alone
     G = 15
     small = dict(N=400, T=2, mu=0.02, rho=4.0, fitness="gaussian_vs", fit_param=20.0, seed=31)
-    kw = {k: v for k, v in small.items() if k not in ("N", "T")}
-    d_small = cg.make_desc(small["N"], 4096, small["T"], p_neutral=0.3, **kw)
-    d_big = cg.make_desc(300, 70_000, 1, mu=0.05, rho=2.0, p_neutral=0.3, fitness="constant", seed=32)
-    pop = cg.Population(small["N"], 4096, small["T"], mu=small["mu"], rho=small["rho"], fitness=small["fitness"],
-                        fit_param=small["fit_param"], p_neutral=0.3, seed=small["seed"], max_events=d_small.max_events,
-                        max_mutations=d_small.max_mutations, max_fixed=d_small.max_fixed)
-    pop.init(small["N"])
-    pop.run_philox(small["N"], G)
-    pop.check()
-    b = cg.Batch([d_small, d_big])
+    big = dict(N=300, T=1, mu=0.05, rho=2.0, fitness="constant", fit_param=1.0, seed=32)
+    caps = (4096, 70_000)
+    descs, alone = [], []
+    for s, cap in zip((small, big), caps):
+        kw = {k: v for k, v in s.items() if k not in ("N", "T")}
+        d = cg.make_desc(s["N"], cap, s["T"], p_neutral=0.3, **kw)
+        descs.append(d)
+        pop = cg.Population(s["N"], cap, s["T"], mu=s["mu"], rho=s["rho"], fitness=s["fitness"],
+                            fit_param=s["fit_param"], p_neutral=0.3, seed=s["seed"], max_events=d.max_events,
+                            max_mutations=d.max_mutations, max_fixed=d.max_fixed)
+        pop.init(s["N"])
+        pop.run_philox(s["N"], G)
+        pop.check()
+        alone.append(pop)
+    b = cg.Batch(descs)
     b.init()
     b.run(G)
-    assert b.info(0)["device_error"] == 0 and b.info(1)["device_error"] == 0
-    assert np.array_equal(b.rows(0), pop.rows())
-    bs, st = b.stats(0, 64), pop.stats(64)
-    assert np.array_equal(bs["sfs"], st["sfs"])
-    assert abs(bs["mean_fitness"] / st["mean_fitness"] - 1.0) < 1e-9
+    for i, pop in enumerate(alone):
+        assert b.info(i)["device_error"] == 0
+        assert np.array_equal(b.rows(i), pop.rows())
+        bs, st = b.stats(i, 64), pop.stats(64)
+        assert np.array_equal(bs["sfs"], st["sfs"])
+        assert bs["mean_fitness"] == st["mean_fitness"]
+        assert b.info(i)["mean_fitness"] == pop.info()["mean_fitness"]
+    b.close()
 
 
 @pytest.mark.parametrize("cap", [8192, 1 << 14])
