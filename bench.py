@@ -62,6 +62,8 @@ def parse():
                    help="print the generation kernel's per-phase cycle breakdown (profiling build) and exit")
     p.add_argument("--no-batched", action="store_true", help="skip the batched and serving measurements")
     p.add_argument("--batched-only", action="store_true", help="only the batched and serving measurements")
+    p.add_argument("--c4-waves", action="store_true",
+                   help="the batched configuration with mu U[0.01,0.05] through footprint-admitted waves (one-off)")
     return p.parse_args()
 
 
@@ -277,6 +279,34 @@ def compare_batched(cg, serving, autotune, N_range, G, n=256, seed=11):
         "tuning": tuned, "autotune_s": t_tune, "device_errors": errs, "footprint_gb": footprint / 1e9}
 
 
+def c4_waves(budget_gb: int = 200, G: int = 50):
+    """The batched configuration's N, rho and trait ranges with mu at the low end of its stated range
+    (U[0.01, 0.05]): ~390 GB of populations, more than the device holds, so they run through the serving
+    loop's footprint admission, all arriving at once (waves: a population is admitted when its bitsets fit
+    the budget, and leaves when it reaches G); against the same jobs one at a time."""
+    import clotho_gb300 as cg
+    from clotho_gb300 import serving
+    jobs = serving.synthetic_jobs(256, rate=1e9, seed=11, N_range=(1_000, 200_000), G_range=(G, G),
+                                  mu_range=(0.01, 0.05))
+    for j in jobs:
+        j.arrival = 0.0
+    total = sum(cg.footprint_of(j.desc()) for j in jobs)
+    big = sum(1 for j in jobs if j.max_alleles() > 65_536)
+    pjobs = [serving.Job(**{k: getattr(j, k) for k in ("id", "N", "mu", "rho", "T", "G", "seed", "arrival")})
+             for j in jobs]
+    srv = serving.Server(budget_bytes=budget_gb << 30, max_slots=256)
+    s_srv = srv.run_open_loop(jobs)
+    s_plain = serving.run_plain(pjobs)
+    same = sum(1 for j, p in zip(sorted(srv.finished, key=lambda x: x.id), pjobs)
+               if j.result["sfs"] == p.result["sfs"] and j.result["mean_fitness"] == p.result["mean_fitness"])
+    return {"c4_waves": {
+        "workload": (f"256 populations, N log-U[1e3,2e5], mu U[0.01,0.05], rho U[0.1,5], T 1-4, G={G}: "
+                     f"{total / 1e9:.0f} GB of populations ({big} above 65,536 allele slots), through a "
+                     f"{budget_gb} GB admission budget"),
+        "served": s_srv, "plain": s_plain, "speedup_jobs_per_s": s_srv["jobs_per_s"] / s_plain["jobs_per_s"],
+        "peak_resident": srv.peak_resident, "peak_used_gb": srv.peak_used / 1e9, "identical_results": same}}
+
+
 def batched_and_serving():
     """Batched populations and continuous-batching serving against the plain engine one job at a time, on
     synthetic job mixes shaped like the batched and serving configurations (named deviations in `workload`),
@@ -295,6 +325,7 @@ def batched_and_serving():
                          f"({small.pop('footprint_gb'):.0f} GB): small populations, where one-at-a-time runs are "
                          "bound by launches and set-up")
     batched["small_populations"] = small
+    batched["waves"] = c4_waves()["c4_waves"]
 
     # ---- serving: open-loop Poisson arrivals at 20 jobs/s, both arms on the same job list
     sjobs = serving.synthetic_jobs(200, rate=20.0, seed=21, N_range=(1_000, 10_000), G_range=(200, 2000))
@@ -453,6 +484,9 @@ def main():
 
     if args.batch_kernels:
         print(json.dumps(batch_kernels(cg, args.warmup, args.steps)))
+        return
+    if args.c4_waves:
+        print(json.dumps(c4_waves()))
         return
     if args.batched_only:
         batched, serve = batched_and_serving()

@@ -74,6 +74,8 @@ class Server:
         self.used = 0
         self.steps = 0
         self.counting: set[int] = set()   # resident indices whose population counts its columns
+        self.peak_used = 0                 # bytes, and populations resident at once, at their highest
+        self.peak_resident = 0
 
     def submit(self, job: Job):
         self.queue.append(job)
@@ -91,6 +93,8 @@ class Server:
             self.used += fp
             job.admitted = now
             self.resident.append((job, 0))
+            self.peak_used = max(self.peak_used, self.used)
+            self.peak_resident = max(self.peak_resident, len(self.resident))
 
     def _retire(self, now: float):
         keep = []
