@@ -351,6 +351,25 @@ def batched_and_serving():
     return batched, serve
 
 
+def drop_in_rate(N, w, gens=3):
+    """The C++ drop-in engine (clotho_gb300/cpp, EngineGB300 through the tape call) at this N: every generation's
+    draws made on the host in the reference's order with a serial generator (std::mt19937_64: parents from the
+    fitness, 2N breakpoint counts and their positions, swap bits, new alleles), then one tape call.  Starts from
+    an empty population (its rows stay narrow), so the time is the host draws' plus a small device share."""
+    from clotho_gb300 import builder
+    try:
+        out = subprocess.run([builder.DRIVER_PATH, str(N), str(gens), str(w.mu), str(w.rho), str(w.T), "0", "7"],
+                             capture_output=True, text=True, timeout=600, check=True).stdout
+        perf = json.loads(out.strip().splitlines()[-1])["performance"]["simulate"][1:]
+    except Exception as e:  # the driver is a convenience measurement; the line stands without it
+        return {"error": str(e)[:200]}
+    s = statistics.mean(perf)
+    return {"value": 2.0 * N / s, "unit": UNIT, "ms_per_step": 1e3 * s,
+            "note": "C++ drop-in (tape mode): the reference's draws on the host with one serial generator, then "
+                    "the tape call; the host draws bound it (generations after the first, whose uniform parents "
+                    "are cheaper to draw)"}
+
+
 def single_core_rate(w, warmup=1, steps=2, N=None):
     """The reference's default thread count is the master thread alone (T=0,
     thread_count_parameter.hpp:22): the oracle on one core over a bounded sample
@@ -594,6 +613,8 @@ def main():
                        "tape (the reference's serial RNG draws) is not in this number"}
         for ptr in keep:
             cg.capi.load().clotho_host_free(ptr)
+        if rank == 0 and world == 1:
+            e2e["drop_in_host_draws"] = drop_in_rate(N, w)
 
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
