@@ -12,7 +12,9 @@ numpy (oracle/device_draws.py), and these tests
     under strong selection;
   * rebuild the event tape of device-drawn generations from the restated draws
     and replay it through the oracle: genomes, free lists, allele and fixed
-    tables bit-exact, phenotypes within the FP32 bound of tests/test_gpu_parity.py;
+    tables bit-exact, phenotypes within the FP32 bound of tests/test_gpu_parity.py, at small sizes and
+    on the N=1e6 measurement workload itself (2e6 rows, two generations; about a minute and 60 GB of host
+    memory);
   * compare site-frequency spectra, segregating sites, heterozygosity and mean
     fitness of device-drawn runs with oracle runs of the same parameters that
     draw from the oracle's own generator (the large-population configuration's
@@ -35,7 +37,7 @@ if not gpu_available():  # collected on CPU machines, skipped there
 
 import clotho_gb300 as cg  # noqa: E402
 from clotho_gb300 import workloads  # noqa: E402
-from tests.test_gpu_parity import FITS, compare_state  # noqa: E402
+from tests.test_gpu_parity import FITS, compare_state, fitness_of  # noqa: E402
 
 
 def random_start(N, A, T, rng, density=0.3, scale=0.3):
@@ -164,7 +166,8 @@ def test_parent_counts_follow_fitness_under_strong_selection(capsys):
 # ---------------------------------------------------------------------------
 # whole device-drawn generations replayed through the oracle
 
-def replay_device_generations(orc, gpu, sizes, kind, fit_param, mu, rho, bias, q1, T, p_neutral, seed):
+def replay_device_generations(orc, gpu, sizes, kind, fit_param, mu, rho, bias, q1, T, p_neutral, seed,
+                              compare=compare_state):
     for g, N in enumerate(sizes):
         before = gpu.info()
         fit = gpu.fitness()
@@ -192,7 +195,7 @@ def replay_device_generations(orc, gpu, sizes, kind, fit_param, mu, rho, bias, q
         np.testing.assert_allclose(mut_eff, ref.astype(np.float32), rtol=1e-6, atol=1e-7)
         tape = oracle.Tape(N, M, pairs, swap, ev_off, ev_pos, mut_seq, mut_pos, mut_eff.reshape(-1))
         orc.step_tape(tape)
-        compare_state(orc, gpu, g, kind=kind, fit_param=fit_param, mu=mu)
+        compare(orc, gpu, g, kind=kind, fit_param=fit_param, mu=mu)
 
 
 def device_pair(N_cap, A_cap, T, fitness, fit_param, mu, rho, bias, q1, p_neutral, seed, threads=4):
@@ -217,6 +220,80 @@ def test_bench_shape_device_generations_bit_exact(mu):
     assert gpu.info()["W"] == orc.info()["B"] == 912  # 58,000 slots -> 912-word rows
     replay_device_generations(orc, gpu, [N] * 4, w.fitness, w.fit_param, mu, w.rho, 0.5, True, w.T, w.p_neutral,
                               seed)
+
+
+def compare_state_full_size(orc, gpu, g, kind="constant", fit_param=1.0, mu=0.0):
+    """compare_state for populations whose rows take many GB on the host: rows compared in slices, and the
+    phenotype bound taken from each individual's allele count n and the largest |effect| of each trait,
+    (g + 2) 2^-24 max_i (n_i + 1) n_i max|w| (looser than compare_state's, which unpacks every set bit to sum
+    the |w| of each individual).  Returns the largest phenotype error and the bound."""
+    oi, gi = orc.info(), gpu.info()
+    assert gi["device_error"] == 0, f"gen {g}: device error {gi['device_error']}"
+    for k in ("N", "A", "fixed_count", "lost_count", "free_count", "fixed_total", "generation"):
+        assert oi[k] == gi[k], f"gen {g}: {k} oracle={oi[k]} gpu={gi[k]}"
+    assert oi["B"] == gi["W"], f"gen {g}: width oracle={oi['B']} gpu={gi['W']}"
+    rg = gpu.rows()
+    ro = orc.rows()
+    assert ro.shape == rg.shape
+    step = 1 << 16
+    for r0 in range(0, rg.shape[0], step):
+        a, b = ro[r0:r0 + step], rg[r0:r0 + step]
+        if not np.array_equal(a, b):
+            r, w = np.argwhere(a != b)[0]
+            raise AssertionError(f"gen {g}: rows differ; first row {r0 + r} word {w}: "
+                                 f"oracle {int(a[r, w]):#x} gpu {int(b[r, w]):#x}")
+    del ro, rg
+    assert np.array_equal(orc.free_list(), gpu.free_list()), f"gen {g}: free list differs"
+    po, ao, eo = orc.alleles()
+    pg, ag, eg = gpu.alleles()
+    assert np.array_equal(po, pg) and np.array_equal(ao, ag), f"gen {g}: allele table differs"
+    assert np.array_equal(eo, eg.astype(np.float64)), f"gen {g}: trait table differs"
+    fpo, fao, feo = orc.fixed()
+    fpg, fag, feg = gpu.fixed()
+    assert np.array_equal(fpo, fpg) and np.array_equal(fao, fag) and np.array_equal(feo, feg.astype(np.float64))
+    zo, zg = orc.phenotypes(), gpu.phenotypes().astype(np.float64)
+    _, rowc = gpu.margins()
+    n = rowc[0::2].astype(np.float64) + rowc[1::2]
+    maxw = np.abs(eg.astype(np.float64)).max(axis=0)
+    bound = (g + 2.0) * 2.0 ** -24 * ((n + 1.0) * n).max() * maxw + 1e-30
+    err = np.abs(zo - zg)
+    assert np.all(err <= bound), f"gen {g}: phenotype error {err.max()} above {bound}"
+    np.testing.assert_allclose(gpu.fitness(), fitness_of(gpu.phenotypes(), kind, fit_param, gi["N"], mu),
+                               rtol=1e-12, atol=1e-300)
+    return float(err.max()), float(bound.max())
+
+
+def test_bench_configuration_at_full_size_bit_exact(capsys):
+    # the N=1e6 measurement itself: 2e6 rows of 912 words, 58,000 pre-seeded alleles, four traits, the
+    # reference gaussian metric, rho=5, mu=1e-3, device-drawn parents, breakpoints and mutations, with the
+    # measurement's seed and capacities; two generations replayed through the oracle on every host core
+    import os
+    w = workloads.LARGE_N
+    N, seed = w.N, 20261203
+    gpu = cg.Population(N, w.max_alleles, w.T, fitness=w.fitness, fit_param=w.fit_param, mu=w.mu, rho=w.rho,
+                        bias=w.bias, p_neutral=w.p_neutral, seed=seed, max_fixed=1 << 20,
+                        max_events=int(2 * N * w.rho * 1.05 + 4096), max_mutations=int(2 * N * w.mu * 1.5 + 4096))
+    orc = oracle.Oracle(T=w.T, fitness=FITS[w.fitness], fit_param=w.fit_param, mu=w.mu, rho=w.rho, bias=w.bias,
+                        p_neutral=w.p_neutral, q1=True, threads=os.cpu_count() or 4, seed=seed)
+    pos, eff, thr = workloads.seeded_start(w)
+    gpu.seed_population(N, pos, eff, thr, seed)
+    rows = gpu.rows()
+    assert rows.shape == (2 * N, 912)
+    orc.load_population(N, rows, pos, eff)
+    del rows
+    errs = []
+
+    def compare(orc_, gpu_, g, **kw):
+        errs.append(compare_state_full_size(orc_, gpu_, g, **kw))
+
+    replay_device_generations(orc, gpu, [N] * 2, w.fitness, w.fit_param, w.mu, w.rho, w.bias, True, w.T,
+                              w.p_neutral, seed, compare=compare)
+    with capsys.disabled():
+        print(f"\nN=1e6 measurement workload, 2 device-drawn generations: rows bit-exact; phenotype "
+              f"|FP32 carried - FP64| max {max(e for e, _ in errs):.3e} (bound {min(b for _, b in errs):.3e}), "
+              f"alleles {gpu.info()['A']}, row width {gpu.info()['W']} words")
+    orc.close()
+    gpu.close()
 
 
 @pytest.mark.parametrize("case", ["qtl_selection", "q1_off_quadratic", "interval_classifier", "size_changes"])
