@@ -263,10 +263,12 @@ def compare_state_full_size(orc, gpu, g, kind="constant", fit_param=1.0, mu=0.0)
     return float(err.max()), float(bound.max())
 
 
-def test_bench_configuration_at_full_size_bit_exact(capsys):
+@pytest.mark.parametrize("mode", ["device", "tape"])
+def test_bench_configuration_at_full_size_bit_exact(mode, capsys):
     # the N=1e6 measurement itself: 2e6 rows of 912 words, 58,000 pre-seeded alleles, four traits, the
-    # reference gaussian metric, rho=5, mu=1e-3, device-drawn parents, breakpoints and mutations, with the
-    # measurement's seed and capacities; two generations replayed through the oracle on every host core
+    # reference gaussian metric, rho=5, mu=1e-3, with the measurement's seed and capacities, two generations
+    # against the oracle on every host core: device-drawn parents, breakpoints and mutations replayed through
+    # the oracle ("device"), or the drop-in's event tape drawn by the oracle's recorder ("tape")
     import os
     w = workloads.LARGE_N
     N, seed = w.N, 20261203
@@ -286,10 +288,15 @@ def test_bench_configuration_at_full_size_bit_exact(capsys):
     def compare(orc_, gpu_, g, **kw):
         errs.append(compare_state_full_size(orc_, gpu_, g, **kw))
 
-    replay_device_generations(orc, gpu, [N] * 2, w.fitness, w.fit_param, w.mu, w.rho, w.bias, True, w.T,
-                              w.p_neutral, seed, compare=compare)
+    if mode == "device":
+        replay_device_generations(orc, gpu, [N] * 2, w.fitness, w.fit_param, w.mu, w.rho, w.bias, True, w.T,
+                                  w.p_neutral, seed, compare=compare)
+    else:
+        for g in range(2):
+            gpu.simulate(orc.step_record(N))
+            compare(orc, gpu, g, kind=w.fitness, fit_param=w.fit_param, mu=w.mu)
     with capsys.disabled():
-        print(f"\nN=1e6 measurement workload, 2 device-drawn generations: rows bit-exact; phenotype "
+        print(f"\nN=1e6 measurement workload, 2 {mode} generations: rows bit-exact; phenotype "
               f"|FP32 carried - FP64| max {max(e for e, _ in errs):.3e} (bound {min(b for _, b in errs):.3e}), "
               f"alleles {gpu.info()['A']}, row width {gpu.info()['W']} words")
     orc.close()
