@@ -16,6 +16,9 @@ generation (free space, selection, crossover, mutation, phenotype, fitness).
            over its CUDA-event duration, against MEASURED_PEAKS.json hbm_gbs.
   cpu_baseline  the CPU oracle (restatement of the reference's path) on the
            host cores, on a bounded sample of the same workload.
+  configs  the neutral (N=1e4, 1,000 generations) and QTL-with-selection
+           (N=1e5, 2,000 generations) configurations as stated, on the GPU and
+           the CPU restatement, with the FP32-vs-FP64 phenotype error.
 
 --impl reference times that CPU restatement alone, on this arm's configuration
 (N=1e6, all host threads), with the single-core rate beside it: the
@@ -61,6 +64,10 @@ def parse():
     p.add_argument("--phase-clocks", action="store_true",
                    help="print the generation kernel's per-phase cycle breakdown (profiling build) and exit")
     p.add_argument("--no-batched", action="store_true", help="skip the batched and serving measurements")
+    p.add_argument("--no-configs", action="store_true",
+                   help="skip the neutral and QTL-with-selection configurations (GPU and CPU)")
+    p.add_argument("--configs-only", action="store_true",
+                   help="only the neutral and QTL-with-selection configurations")
     p.add_argument("--batched-only", action="store_true", help="only the batched and serving measurements")
     p.add_argument("--c4-waves", action="store_true",
                    help="the batched configuration with mu U[0.01,0.05] through footprint-admitted waves (one-off)")
@@ -370,6 +377,79 @@ def drop_in_rate(N, w, gens=3):
                     "are cheaper to draw)"}
 
 
+def stated_configs(cg, threads):
+    """The neutral (N=1e4, G=1,000) and QTL-with-selection (N=1e5, G=2,000) configurations as stated, from an
+    empty start with device draws, in one graph-replayed call each; then the rate and the generation kernel's
+    bandwidth at the final load, and the CPU restatement on the same final state (all host threads and one),
+    with the FP32-carried phenotypes of the QTL run against the FP64 sums of its rows."""
+    import numpy as np
+    import oracle
+    from clotho_gb300.workloads import NEUTRAL_WF, QTL_SELECTION
+    fits = {"constant": oracle.FIT_CONSTANT, "gaussian_vs": oracle.FIT_GAUSSIAN_VS}
+    peak, peak_kind = measured_peak()
+    out = {}
+    for key, w, cpu_gens in (("neutral_wf", NEUTRAL_WF, 1000), ("qtl_selection", QTL_SELECTION, 2)):
+        pop = cg.Population(w.N, w.max_alleles, w.T, fitness=w.fitness, fit_param=w.fit_param, mu=w.mu, rho=w.rho,
+                            bias=w.bias, p_neutral=w.p_neutral, seed=20261203, max_fixed=1 << 20)
+        pop.init(w.N)
+        pop.sync()
+        pop.timer_begin()
+        pop.run_philox(w.N, w.generations)
+        ms = pop.timer_end()
+        pop.sync()
+        pop.check()
+        whole = 2.0 * w.N * w.generations / (ms / 1e3)
+        pop.timer_begin()
+        pop.run_philox(w.N, 20)
+        ms_f = pop.timer_end()
+        pop.profile(True)
+        for _ in range(4):
+            pop.simulate_philox(w.N)
+        kms, nl, rows_done, words_done = pop.kernel_time()
+        pop.profile(False)
+        pop.check()
+        info = pop.info()
+        kern_ms = kms / max(nl, 1)
+        gbs = 16.0 * words_done / max(nl, 1) / (kern_ms / 1e3) / 1e9
+        gpu = {"seq_gen_per_s": whole, "generations": w.generations, "s": ms / 1e3,
+               "final": {"generation": info["generation"], "A": info["A"], "W": info["W"],
+                         "seq_gen_per_s": 2.0 * w.N * 20 / (ms_f / 1e3), "ms_per_generation": ms_f / 20,
+                         "kernel_ms": kern_ms, "achieved_gbs": gbs, "frac": gbs / peak,
+                         "peak_kind": f"of {peak_kind}"}}
+        rows = pop.rows()
+        pos, _, eff = pop.alleles()
+        z_gpu = pop.phenotypes().astype(np.float64)
+        pop.close()
+        cpu = {}
+        for name, thr in (("all_cores", threads), ("single_core", 1)):
+            orc = oracle.Oracle(T=w.T, fitness=fits[w.fitness], fit_param=w.fit_param, mu=w.mu, rho=w.rho,
+                                bias=w.bias, p_neutral=w.p_neutral, q1=True, threads=thr, seed=7)
+            orc.load_population(w.N, rows, pos, eff.reshape(-1))
+            if name == "all_cores" and w.p_neutral < 1.0:
+                err = np.abs(orc.phenotypes() - z_gpu)
+                gpu["phenotype_error"] = {"max": float(err.max()), "mean": float(err.mean()),
+                                          "max_abs_z": float(np.abs(z_gpu).max()),
+                                          "note": "FP32-carried phenotypes after the whole run against the "
+                                                  "FP64 sums of the same rows (the oracle's order)"}
+            n = cpu_gens if thr > 1 else max(1, cpu_gens // 2)
+            t0 = time.perf_counter()
+            stages = {}
+            for _ in range(n):
+                orc.step_record(w.N)
+                for k, v in orc.times().items():
+                    stages[k] = stages.get(k, 0.0) + v
+            dt = time.perf_counter() - t0
+            orc.close()
+            cpu[name] = {"seq_gen_per_s": 2.0 * w.N * n / dt, "cores": thr, "generations": n, "s": dt,
+                         "stage_seconds": stages}
+        del rows
+        out[key] = {"workload": w.name, "gpu": gpu, "cpu": cpu,
+                    "cpu_sample": "oracle/clotho_oracle.cpp from the GPU run's final state (same rows, allele "
+                                  "and effect tables), its own draws"}
+    out["neutral_wf"]["note"] = "about 10 MB of rows: L2-resident, bound by launch and dependent latency, not HBM"
+    return out
+
+
 def single_core_rate(w, warmup=1, steps=2, N=None):
     """The reference's default thread count is the master thread alone (T=0,
     thread_count_parameter.hpp:22): the oracle on one core over a bounded sample
@@ -507,6 +587,9 @@ def main():
     if args.c4_waves:
         print(json.dumps(c4_waves()))
         return
+    if args.configs_only:
+        print(json.dumps({"configs": stated_configs(cg, os.cpu_count() or 1)}))
+        return
     if args.batched_only:
         batched, serve = batched_and_serving()
         print(json.dumps({"batched": batched, "serving": serve}))
@@ -632,6 +715,11 @@ def main():
         pop.close()
         batched, serve = batched_and_serving()
 
+    configs = None
+    if rank == 0 and world == 1 and not args.no_configs:
+        pop.close()
+        configs = stated_configs(cg, os.cpu_count() or 1)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -641,7 +729,7 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single",
                            "l2": "inputs larger than L2 (rows 16 GB per population)"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-                "batched": batched, "serving": serve}
+                "batched": batched, "serving": serve, "configs": configs}
         print(json.dumps(line), flush=True)
 
 
