@@ -69,6 +69,9 @@ def parse():
     p.add_argument("--configs-only", action="store_true",
                    help="only the neutral and QTL-with-selection configurations")
     p.add_argument("--batched-only", action="store_true", help="only the batched and serving measurements")
+    p.add_argument("--qtl-kernel", type=int, default=0, metavar="G",
+                   help="the QTL-with-selection configuration from an empty start for G + warmup + steps eager "
+                        "generations (ncu runs of the interval-classifier kernel)")
     p.add_argument("--c4-waves", action="store_true",
                    help="the batched configuration with mu U[0.01,0.05] through footprint-admitted waves (one-off)")
     return p.parse_args()
@@ -586,6 +589,17 @@ def main():
         return
     if args.c4_waves:
         print(json.dumps(c4_waves()))
+        return
+    if args.qtl_kernel:
+        from clotho_gb300.workloads import QTL_SELECTION as q
+        pop = cg.Population(q.N, q.max_alleles, q.T, fitness=q.fitness, fit_param=q.fit_param, mu=q.mu, rho=q.rho,
+                            bias=q.bias, p_neutral=q.p_neutral, seed=20261203, max_fixed=1 << 20)
+        pop.init(q.N)
+        for _ in range(args.qtl_kernel + args.warmup + args.steps):
+            pop.simulate_philox(q.N)
+        pop.sync()
+        pop.check()
+        print(json.dumps({"qtl_kernel": True, "info": pop.info()}))
         return
     if args.configs_only:
         print(json.dumps({"configs": stated_configs(cg, os.cpu_count() or 1)}))

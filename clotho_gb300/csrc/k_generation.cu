@@ -45,6 +45,7 @@
 // items of rows, which its warps claim one at a time.
 #include "engine.cuh"
 
+#include <algorithm>
 #include <mutex>
 
 namespace clotho {
@@ -1247,10 +1248,12 @@ __device__ __forceinline__ void gen_row_iv(const PopDev& P, const DevStatus& st,
 
 }  // namespace
 
-// Dynamic shared memory: [AND acc: maxW][OR acc: maxW][fixed mask: maxW] u64,
-// then (SUF) the warps' mask bitmaps and one WarpSmem per warp.  With gacc set (rows
-// too wide for that layout) the AND/OR fold goes to the population's global
-// accumulators and the fixed mask is read from global memory.
+// Dynamic shared memory: [AND acc: aw][OR acc: aw][fixed mask: aw] u64 (aw = maxW in the
+// suffix-table builds, acc_words in the interval-classifier build), then (SUF) the warps' mask
+// bitmaps and one WarpSmem per warp.  A population whose current rows are wider than acc_words
+// (interval classifier) folds into its global AND/OR accumulators and reads its fixed mask from
+// global memory; the choice is made per population from its widths on the device, so a graph
+// captured for a large capacity keeps the shared accumulators while the rows are narrow.
 // PROF (suffix-table build only): per-phase cycle counters into ctl->phase.
 // NARROW (suffix-table build only): every row is at most 128 words.
 // CNT (suffix-table builds, shared accumulators): per-column counts of the child rows of the populations
@@ -1259,7 +1262,7 @@ __device__ __forceinline__ void gen_row_iv(const PopDev& P, const DevStatus& st,
 template <bool SUF, bool PROF, bool NARROW, bool CNT = false>
 __global__ void __launch_bounds__(kGenThreads, 1)
 k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restrict__ ctl, uint32_t fuse,
-             int profile, uint32_t maxW, uint32_t gacc, uint32_t mixed) {
+             int profile, uint32_t maxW, uint32_t acc_words, uint32_t mixed) {
     const long long c_start = PROF ? clock64() : 0;
     PhaseClk pc;
     if (PROF)
@@ -1272,9 +1275,13 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     __shared__ uint32_t s_sm[kIvWarps][128];
     __shared__ uint32_t s_item, s_next;
     __shared__ uint32_t s_crows;   // CNT, one population: rows the block has counted
-    uint64_t* sF = s_dyn;
-    uint64_t* sV = s_dyn + maxW;
-    uint64_t* sfix = s_dyn + 2u * maxW;
+    const uint32_t aw = SUF ? maxW : acc_words;
+    uint64_t* const sF0 = s_dyn;
+    uint64_t* const sV0 = s_dyn + aw;
+    uint64_t* const sfix0 = s_dyn + 2u * aw;
+    uint64_t* sF = sF0;
+    uint64_t* sV = sV0;
+    uint64_t* sfix = sfix0;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     // SUF: per-warp mask bitmaps [kWarps][maxW] u64, then one WarpSmem per warp
     uint64_t* mask = s_dyn + (3u + (SUF ? warp : 0u)) * maxW;
@@ -1299,6 +1306,7 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     int cur_pop = -1;
     uint32_t cur_W = 0, cur_A = 0;
     bool cur_cnt = false;      // CNT: the block's current population counts columns
+    bool cur_g = false;        // the block's current population folds into its global accumulators
     uint32_t crows = 0;        // CNT, batches: rows the block has counted since its last flush (block-uniform)
     uint64_t rows_done = 0, words_done = 0;
 
@@ -1310,7 +1318,8 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
         const DevStatus st = *P.st;
         cur_pop = 0;
         cur_W = st.W;
-        if (gacc) {
+        cur_g = !SUF && max(st.W, st.pW) > acc_words;
+        if (cur_g) {
             sF = P.accF;
             sV = P.accV;
             sfix = P.fixmask;
@@ -1324,7 +1333,7 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
         const uint32_t S = 2u * st.N;
         const uint32_t Se = (S + 1u) >> 1;
         cur_A = st.A;
-        cur_cnt = CNT && do_fs && !gacc && st.count_cols != 0u;
+        cur_cnt = CNT && do_fs && !cur_g && st.count_cols != 0u;
         Fold fo{sF, sV, cur_cnt ? cplanes : nullptr, maxW};
         // the next claim is taken before the current rows run, so its
         // round trip to the counter is hidden behind them
@@ -1384,13 +1393,8 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             continue;
         }
         const DevStatus st = *P.st;
-        if ((int)p != cur_pop && gacc) {
-            cur_pop = (int)p;
-            sF = P.accF;
-            sV = P.accV;
-            sfix = P.fixmask;
-        } else if ((int)p != cur_pop) {
-            if (cur_pop >= 0 && do_fs) {
+        if ((int)p != cur_pop) {
+            if (cur_pop >= 0 && do_fs && !cur_g) {
                 const PopDev& Q = pops[cur_pop];
                 for (uint32_t w = threadIdx.x; w < cur_W; w += blockDim.x) {
                     atomicAnd((unsigned long long*)&Q.accF[w], (unsigned long long)sF[w]);
@@ -1402,11 +1406,21 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             cur_pop = (int)p;
             cur_W = st.W;
             cur_A = st.A;
-            cur_cnt = CNT && do_fs && st.count_cols != 0u;
+            cur_g = !SUF && max(st.W, st.pW) > acc_words;
+            cur_cnt = CNT && do_fs && !cur_g && st.count_cols != 0u;
             crows = 0;
-            if (do_fs)
-                for (uint32_t w = threadIdx.x; w < cur_W; w += blockDim.x) { sF[w] = ~0ull; sV[w] = 0ull; }
-            for (uint32_t w = threadIdx.x; w < st.pW; w += blockDim.x) sfix[w] = P.fixmask[w];
+            if (cur_g) {
+                sF = P.accF;
+                sV = P.accV;
+                sfix = P.fixmask;
+            } else {
+                sF = sF0;
+                sV = sV0;
+                sfix = sfix0;
+                if (do_fs)
+                    for (uint32_t w = threadIdx.x; w < cur_W; w += blockDim.x) { sF[w] = ~0ull; sV[w] = 0ull; }
+                for (uint32_t w = threadIdx.x; w < st.pW; w += blockDim.x) sfix[w] = P.fixmask[w];
+            }
             __syncthreads();
         }
         // all effects zero: the gathered sums are exactly zero, skip them
@@ -1416,7 +1430,7 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
         const uint32_t r0 = (item - ctl->item_base[p]) * rpi;
         const uint32_t r1 = min(S, r0 + rpi);
         const uint32_t Se = (S + 1u) >> 1;
-        if (CNT && cur_cnt && !gacc) {  // block-uniform: flush before the counters could overflow
+        if (CNT && cur_cnt) {  // block-uniform: flush before the counters could overflow
             if (crows + (r1 - r0) > kCountMax) {
                 count_flush(cplanes, maxW, cur_W, cur_A, P.colcnt);
                 __syncthreads();
@@ -1424,7 +1438,7 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             }
             crows += r1 - r0;
         }
-        const Fold fo{sF, sV, (CNT && cur_cnt && !gacc) ? cplanes : nullptr, maxW};
+        const Fold fo{sF, sV, (CNT && cur_cnt) ? cplanes : nullptr, maxW};
         // narrow build: each warp claims its next row one ahead and fetches that row's plan entries into L1
         // behind the current row (narrow rows are bound by their chains of dependent loads)
         uint32_t kc = 0;
@@ -1468,7 +1482,7 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
         __syncthreads();
     }
     __syncthreads();
-    if (cur_pop >= 0 && do_fs && !gacc) {
+    if (cur_pop >= 0 && do_fs && !cur_g) {
         const PopDev& Q = pops[cur_pop];
         for (uint32_t w = threadIdx.x; w < cur_W; w += blockDim.x) {
             atomicAnd((unsigned long long*)&Q.accF[w], (unsigned long long)sF[w]);
@@ -1506,11 +1520,15 @@ cudaError_t launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t n
                               uint32_t maxA, uint32_t fuse, int profile, bool count_on, bool mixed) {
     const uint32_t mx = mixed ? 1u : 0u;
     const bool suf = maxA <= kSufMaxSlots;
-    // the interval classifier keeps 3.5 KB of static shared memory per warp
-    const uint32_t gacc = (!suf && 3ull * maxW * sizeof(uint64_t) + kWarps * 3584u > 220u * 1024u) ? 1u : 0u;
     // the counting build: column counters in shared memory (the phase-clock builds do not count)
     const bool cnt = count_on && profile != 2 && generation_counts_fit(maxW, maxA);
-    const size_t smem = gacc ? 0 : suf ? suf_smem(maxW, cnt) : 3ull * maxW * sizeof(uint64_t);
+    // the interval classifier keeps 3.5 KB of static shared memory per warp; its AND/OR accumulators and
+    // fixed mask take what is left of 220 KB, rows of up to acc_words words (wider rows fold into the
+    // global accumulators).  acc_words is a multiple of kWordAlign, so the second and third regions start
+    // on 16-byte boundaries: the lanes access them as 16-byte word pairs.
+    const size_t acc_fit = (220u * 1024u - kWarps * 3584u) / (3u * sizeof(uint64_t)) / kWordAlign * kWordAlign;
+    const uint32_t acc_words = suf ? maxW : (uint32_t)std::min<size_t>(maxW, acc_fit);
+    const size_t smem = suf ? suf_smem(maxW, cnt) : 3ull * acc_words * sizeof(uint64_t);
     // profile 2: the suffix-table kernel's build with phase clocks; rows of at most
     // 128 words: its narrow build (copy rows by direct loads)
     const bool narrow = L.narrow_ok && maxW <= 64u * kDirectCopyChunks;
@@ -1564,7 +1582,7 @@ cudaError_t launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t n
             break;
         default:
             k_generation<false, false, false><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse,
-                                                                                         profile, maxW, gacc, mx);
+                                                                                         profile, maxW, acc_words, mx);
     }
     return cudaSuccess;
 }

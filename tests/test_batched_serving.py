@@ -111,6 +111,41 @@ def test_each_population_keeps_its_classifier_in_a_mixed_batch():
     b.close()
 
 
+def test_shared_and_global_accumulators_in_one_batch():
+    # an interval-classifier population whose rows pass 6,976 words in its first generation (480,000 new
+    # alleles: 40 individuals, mu = 6,000 per sequence) folds into its global AND/OR accumulators, batched
+    # with a narrow interval-classifier population and a suffix-table population that keep theirs in shared
+    # memory; the kernel's blocks move between the two kinds of population, and each population's rows,
+    # spectrum and fitness equal its run alone
+    G = 3
+    specs = [(dict(N=40, T=1, mu=6000.0, rho=2.0, fitness="gaussian_vs", fit_param=50.0, seed=41), 1_200_000),
+             (dict(N=300, T=1, mu=0.05, rho=2.0, fitness="constant", fit_param=1.0, seed=42), 70_000),
+             (dict(N=400, T=2, mu=0.02, rho=4.0, fitness="gaussian_vs", fit_param=20.0, seed=43), 4096)]
+    descs, alone = [], []
+    for s, cap in specs:
+        kw = {k: v for k, v in s.items() if k not in ("N", "T")}
+        d = cg.make_desc(s["N"], cap, s["T"], p_neutral=0.3, **kw)
+        descs.append(d)
+        pop = cg.Population(s["N"], cap, s["T"], mu=s["mu"], rho=s["rho"], fitness=s["fitness"],
+                            fit_param=s["fit_param"], p_neutral=0.3, seed=s["seed"], max_events=d.max_events,
+                            max_mutations=d.max_mutations, max_fixed=d.max_fixed)
+        pop.init(s["N"])
+        pop.run_philox(s["N"], G)
+        pop.check()
+        alone.append(pop)
+    assert alone[0].info()["W"] > 6976
+    b = cg.Batch(descs)
+    b.init()
+    b.run(G)
+    for i, pop in enumerate(alone):
+        assert b.info(i)["device_error"] == 0
+        assert np.array_equal(b.rows(i), pop.rows()), i
+        bs, st = b.stats(i, 64), pop.stats(64)
+        assert np.array_equal(bs["sfs"], st["sfs"])
+        assert bs["mean_fitness"] == st["mean_fitness"]
+    b.close()
+
+
 @pytest.mark.parametrize("cap", [8192, 1 << 14])
 def test_launch_shapes_do_not_change_results(cap):
     # every tuning knob (rows per item, the narrow build where rows are at most 128 words, blocks per SM of

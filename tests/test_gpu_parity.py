@@ -204,6 +204,28 @@ def test_seeded_population_parity():
         compare_state(orc, gpu, g, kind="gaussian_vs", fit_param=50.0)
 
 
+def test_rows_wider_than_the_shared_accumulators():
+    # 460,000 seeded allele slots (7,192-word rows): wider than the interval-classifier kernel's shared-memory
+    # AND/OR accumulators hold (6,976 words), so its fold goes to the population's global accumulators and it
+    # reads the fixed mask from global memory; carrier fractions U[0, 1) give fixed and lost columns, and
+    # 4,000 new alleles a generation reuse their slots
+    rng = np.random.default_rng(17)
+    N, A, T = 40, 460_000, 1
+    pos = rng.random(A)
+    eff = (rng.standard_normal(A * T) * 0.02).astype(np.float32)
+    thr = (rng.random(A) * 2 ** 32).astype(np.uint64).clip(0, 2 ** 32 - 1).astype(np.uint32)
+    orc, gpu = make_pair(N, 480_000, T=T, fitness="gaussian_vs", fit_param=500.0, mu=50.0, rho=3.0,
+                         p_neutral=0.3)
+    orc.seed_population(N, pos, eff, thr, 7)
+    gpu.seed_population(N, pos, eff, thr, 7)
+    assert gpu.info()["W"] == 7192
+    compare_state(orc, gpu, -1, kind="gaussian_vs", fit_param=500.0)
+    for g in range(4):
+        gpu.simulate(orc.step_record(N))
+        compare_state(orc, gpu, g, kind="gaussian_vs", fit_param=500.0, mu=50.0)
+    assert gpu.info()["fixed_total"] > 0 and gpu.info()["W"] > 6976
+
+
 def test_edge_tie_breakpoint_equals_position():
     # A breakpoint exactly at an allele's position counts as <= (upper_bound,
     # classifiers/region_classifier.hpp:73): that allele comes from the bottom strand.
