@@ -63,16 +63,16 @@ std::vector<size_t> sizes_of(const Geometry& g) {
         (S + 1) * 4 * 2ull,              // row_cnt, row_off
         S * 4, g.Mcap * 4ull, g.Mcap * 4ull,  // row_cur, row_mut, mut_slot
         (g.NB + 1ull) * 4 * 2, g.NB * 4ull, A * 8, A * 4, A * 4,  // bcnt+boff, bcur, bpos, bslot, rank
-        A <= kSufMaxSlots ? A * 4 : 0,                            // inv
-        A <= kSufMaxSlots ? (A / 64 + 1) * W * 8 : 0,             // suf
-        A <= kSufMaxSlots ? S * 16 : 0,                           // plan_row
-        A <= kSufMaxSlots ? (S + 1) * 4 * 2 : 0,                  // ord_cnt + ord_off
-        A <= kSufMaxSlots ? S * 4 : 0,                            // ord_cur
-        A <= kSufMaxSlots ? S * 4 : 0,                            // ord_pos
-        A <= kSufMaxSlots ? g.EVcap * 4ull : 0,                   // plan_go
-        A <= kSufMaxSlots ? g.EVcap * 4ull : 0,                   // plan_cr
-        A <= kSufMaxSlots ? S * 8 : 0,                            // plan_mut
-        A <= kSufMaxSlots ? S * 32 : 0,                           // plan_z
+        A <= kTableMaxSlots ? A * 4 : 0,                            // inv
+        A <= kTableMaxSlots ? (A / 64 + 1) * W * 8 : 0,             // suf
+        A <= kTableMaxSlots ? S * 16 : 0,                           // plan_row
+        A <= kTableMaxSlots ? (S + 1) * 4 * 2 : 0,                  // ord_cnt + ord_off
+        A <= kTableMaxSlots ? S * 4 : 0,                            // ord_cur
+        A <= kTableMaxSlots ? S * 4 : 0,                            // ord_pos
+        A <= kTableMaxSlots ? g.EVcap * 4ull : 0,                   // plan_go
+        A <= kTableMaxSlots ? g.EVcap * 4ull : 0,                   // plan_cr
+        A <= kTableMaxSlots ? S * 8 : 0,                            // plan_mut
+        A <= kTableMaxSlots ? S * 32 : 0,                           // plan_z
         A * 4,                                                    // colcnt
         sizeof(DevStatus),
         // two tape sets: pairs, swap, ev_off, ev_pos, mut_seq, mut_pos, mut_eff
@@ -122,7 +122,7 @@ struct clotho_ctx {
     std::vector<uint32_t> graph_key;
     bool in_step = false;
     uint32_t maxW = 0, maxS = 0, maxN = 0, maxNB = 0, maxA = 0;
-    // per classifier: populations of at most kSufMaxSlots slots (suffix table) and the others (intervals)
+    // per classifier: populations of at most kTableMaxSlots slots (suffix table) and the others (intervals)
     uint32_t n_suf = 0, n_iv = 0, maxW_suf = 0, maxW_iv = 0, maxA_suf = 0, maxA_iv = 0;
     cudaError_t launch_err = cudaSuccess;  // a launch set-up failure, reported by the next check_launch
     uint32_t ind_per_sm = 16;               // tuning (clotho_set_tuning)
@@ -300,7 +300,7 @@ int sync_pop_arrays(clotho_ctx* ctx, uint32_t from = 0) {
         ctx->maxN = std::max(ctx->maxN, D.Ncap);
         ctx->maxNB = std::max(ctx->maxNB, D.NB);
         ctx->maxA = std::max(ctx->maxA, D.Acap);
-        if (D.Acap <= kSufMaxSlots) {
+        if (D.Acap <= kTableMaxSlots) {
             ctx->n_suf += 1;
             ctx->maxW_suf = std::max(ctx->maxW_suf, D.Wcap);
             ctx->maxA_suf = std::max(ctx->maxA_suf, D.Acap);
@@ -929,8 +929,8 @@ int clotho_crossover(clotho_ctx* ctx, const uint8_t* swap, const uint32_t* ev_of
     if ((rc = h2d(ctx, D.ev_off, ev_off, 2ull * N + 1, ctx->stream))) return rc;
     if ((rc = h2d(ctx, D.ev_pos, ev_pos, (size_t)ev_total, ctx->stream))) return rc;
     // item prefix is already set by begin; ranks over the current positions
-    launch_ranks(cfg(ctx), ctx->d_pops[0], 1, ctx->maxNB, ctx->maxW, ctx->maxA <= kSufMaxSlots);
-    ctx->launches += 6u + (ctx->maxA <= kSufMaxSlots ? 1u : 0u);
+    launch_ranks(cfg(ctx), ctx->d_pops[0], 1, ctx->maxNB, ctx->maxW, ctx->maxA <= kTableMaxSlots);
+    ctx->launches += 6u + (ctx->maxA <= kTableMaxSlots ? 1u : 0u);
     launch_gen(ctx, ctx->d_pops[0], 1, 0u);
     if ((rc = check_launch(ctx, "crossover"))) return rc;
     CK(cudaStreamSynchronize(ctx->stream));

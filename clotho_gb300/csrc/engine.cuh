@@ -21,7 +21,9 @@ constexpr uint32_t kMaxEvReg = 16;         // events held in registers
 constexpr uint32_t kMaxEvDevice = 128;     // device-drawn events per gamete
 constexpr uint32_t kMaxMutReg = 32;        // mutations per row held in registers
 constexpr uint32_t kWordAlign = 64;        // row stride granularity (words)
-constexpr uint32_t kSufMaxSlots = 65536;   // allele capacity up to which the suffix-table classifier runs
+constexpr uint32_t kSufMaxSlots = 65536;   // allele capacity up to which suffix-table masks are built in per-warp bitmaps
+constexpr uint32_t kTableMaxSlots = 1u << 19;  // allele capacity up to which a population has a suffix table
+                                               // (above kSufMaxSlots its masks are XORed chunk by chunk)
 
 // sticky device error bits (CLOTHO_DEVERR_* in clotho_gpu.h)
 constexpr uint32_t kErrAlleles = 1u, kErrFixed = 2u, kErrEvents = 4u, kErrParent = 8u,
@@ -91,8 +93,8 @@ struct PopDev {
     double*   bpos;        // [Acap] positions grouped by bucket
     uint32_t* bslot;       // [Acap] slot of each bpos entry
     uint32_t* rank;        // [Acap] rank of each slot (position, then slot index) among the A slots
-    uint32_t* inv;         // [Acap] slot of each rank (Acap <= kSufMaxSlots, else null)
-    uint64_t* suf;         // [(Acap/64 + 1) * Wcap] suffix table of the crossover classifier (or null)
+    uint32_t* inv;         // [Acap] slot of each rank (Acap <= kTableMaxSlots, else null)
+    uint64_t* suf;         // [(Acap/64 + 1) * Wcap] suffix table of the crossover classifier (Acap <= kTableMaxSlots, else null)
     uint4*    plan_row;    // [Scap] crossover plans in processing order: row, top strand, event base, events | flags << 30
     uint32_t* ord_cnt;     // [Scap + 1] rows per ordering key (zero between steps)
     uint32_t* ord_off;     // [Scap + 1] exclusive prefix of ord_cnt
@@ -289,9 +291,11 @@ void launch_mut_csr_tape(const LaunchCfg&, const PopDev* pops, uint32_t npops, u
 void launch_mut_counts_philox(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
 void launch_mut_resolve(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_select_philox(const LaunchCfg&, const PopDev* pops, uint32_t npops);
-// mixed: the batch holds populations of both classifiers (suffix table: capacity <= kSufMaxSlots; intervals:
+// mixed: the batch holds populations of both classifiers (suffix table: capacity <= kTableMaxSlots; intervals:
 // above); this launch runs only the populations of its own classifier (maxW, maxA are theirs) and skips the
-// others' items, so each population keeps its classifier whatever it is batched with
+// others' items, so each population keeps its classifier whatever it is batched with.  The suffix-table
+// launch builds its masks in per-warp bitmaps when every one of its populations has at most kSufMaxSlots
+// slots, else chunk by chunk from the table (the same masks)
 cudaError_t launch_generation(const LaunchCfg&, const PopDev* pops, uint32_t npops, WorkCtl* ctl,
                               uint32_t maxW, uint32_t maxA, uint32_t fuse, int profile, bool count_on = false,
                               bool mixed = false);

@@ -26,13 +26,16 @@
 //              FreeSpaceAnalyzerMT input (free_space_task_population_space_row_interlaced.hpp:51-72).
 //
 // Two crossover classifiers:
-//   suffix table (A <= 65,536 slots): the switch mask of a gamete with rank
+//   suffix table (A <= 524,288 slots): the switch mask of a gamete with rank
 //              thresholds r_1..r_E is XOR_k G(r_k), G(r) = {slots with rank >= r}.
 //              G at every multiple of 64 is a per-generation table in L2
 //              (suf[g * Wcap + w], built by k_suf_build); G(r) differs from the
 //              nearest table row by at most 32 slots, which the warp toggles in
 //              its own correction bitmap in shared memory.  Per word: E table
-//              loads and XORs, no per-bit work.
+//              loads and XORs, no per-bit work.  Rows too wide for a bitmap per
+//              warp (A > 65,536) take each chunk's mask words straight from the
+//              table and toggle the correction slots that fall in the chunk
+//              (chunk-mask build); their copy rows stream through registers.
 //   intervals  (wider allele spaces): sorted thresholds pair into half-open rank
 //              intervals; every heterozygous bit is classified by its rank.
 //
@@ -491,6 +494,9 @@ constexpr uint32_t kRound = 32u * kRoundLane;
 constexpr uint32_t kTableInflight = CLOTHO_TABLE_INFLIGHT;
 constexpr uint32_t kFlatLoads = 4;   // table loads per lane when a narrow row's whole mask is built at once
 constexpr uint32_t kDirectCopyChunks = 2;   // copy rows up to 128 words load their strand directly
+constexpr uint32_t kCmMaxEv = 16;           // chunk-mask build: breakpoints a row takes through the table
+constexpr uint32_t kCmCorr = 32u * kCmMaxEv;   // chunk-mask build: correction slots a warp holds
+constexpr uint32_t kCmAccWords = 3072;      // chunk-mask build: widest rows folded in shared memory
 #ifndef CLOTHO_WARP_CHUNK
 #define CLOTHO_WARP_CHUNK 1
 #endif
@@ -614,10 +620,9 @@ __device__ __forceinline__ void row_mutations(const PopDev& P, uint32_t M, const
     }
 }
 
-#if !CLOTHO_COPY_BULK
 // Copy rows (no breakpoint): the top strand with the fixed columns cleared and
-// the new alleles added; the bottom-strand registers of the crossover loop
-// hold more of the top strand here, six chunks ahead.
+// the new alleles added, streamed through registers six chunks ahead (the
+// chunk-mask build, whose warps have no bitmap for a bulk copy to land in).
 __device__ __forceinline__ void row_body_copy(const PopDev& P, uint32_t M, const RowArgs& R, const uint64_t* sfix,
                                               bool do_mut, bool do_fs, const Fold& fo) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -646,8 +651,6 @@ __device__ __forceinline__ void row_body_copy(const PopDev& P, uint32_t M, const
         }
     }
 }
-
-#endif
 
 // Narrow copy rows (the narrow build of the kernel, every row <= 128 words):
 // one 16-byte load a lane per chunk, all issued at once, cost less than arming
@@ -735,13 +738,17 @@ __device__ __forceinline__ bool row_body_copy_bulk(const PopDev& P, uint32_t M, 
 }
 
 // Crossover rows.  MODE 0: switch mask from the warp's mask bitmap; MODE 1:
-// direct event compares (tape rows with more than kMaxEvDevice events).
+// direct event compares (tape rows with more than kMaxEvDevice events);
+// MODE 2 (chunk-mask build): each chunk's mask words XORed from the table rows
+// of the breakpoints (lane k < E holds row k's offset in my_go) and toggled at
+// the row's correction slots (cs[32 k + lane], 0xffffffff for none).
 // PROF: clock the effect gather into *gcyc (profiling build).
 template <int MODE, bool PROF = false>
 __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const RowArgs& R, const uint64_t* sfix,
                                              uint64_t* mask, uint32_t* Q, bool inv, bool do_mut, bool gather,
                                              bool do_fs, const Fold& fo, float (&d)[kMaxTraits],
-                                             unsigned long long* gcyc = nullptr) {
+                                             unsigned long long* gcyc = nullptr, const uint32_t* cs = nullptr,
+                                             uint32_t my_go = 0u) {
     const uint32_t lane = threadIdx.x & 31u;
     constexpr bool xo = true;
     const float4* eff4 = reinterpret_cast<const float4*>(P.eff);
@@ -774,6 +781,33 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
                     *mw = make_ulonglong2(0, 0);  // the bitmap starts every row at zero
                     m0 = m.x;
                     m1 = m.y;
+                }
+            } else if (MODE == 2) {
+                // table rows (L2-resident) of the row's breakpoints; words past the parent's width take no
+                // switch.  The next chunk's words are prefetched into L1 behind this chunk's work.
+                for (uint32_t k = 0; k < R.E; ++k) {
+                    const uint64_t* tk = P.suf + __shfl_sync(0xffffffffu, my_go, k);
+                    if (w + 64u < R.Wp) asm volatile("prefetch.global.L1 [%0];" ::"l"(tk + w + 64u));
+                    if (live && w < R.Wp) {
+                        const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(tk + w));
+                        m0 ^= v.x;
+                        m1 ^= v.y;
+                    }
+                }
+                // correction slots that fall in this chunk: each is toggled by the lane that owns its word
+                for (uint32_t k = 0; k < R.E; ++k) {
+                    const uint32_t rel = cs[32u * k + lane] - w0 * 64u;
+                    uint32_t hits = __ballot_sync(0xffffffffu, rel < 4096u);
+                    while (hits) {
+                        const uint32_t l = (uint32_t)(__ffs(hits) - 1);
+                        hits &= hits - 1u;
+                        const uint32_t r = __shfl_sync(0xffffffffu, rel, l);
+                        if ((r >> 7) == lane) {
+                            const uint32_t bit = r & 127u;
+                            if (bit < 64u) m0 ^= 1ull << bit;
+                            else m1 ^= 1ull << (bit - 64u);
+                        }
+                    }
                 }
             } else {
                 m0 = sw_mask_events(h0, w * 64u, P.pos, R.evg, R.E);
@@ -809,10 +843,12 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
     }
 }
 
+// inv: gather the unswitched heterozygous set (the plan chose the bottom strand's carried value as the base).
 __device__ CLOTHO_COLD float4 row_body_events(const PopDev& P, uint32_t M, const RowArgs R, const uint64_t* sfix,
-                                               uint32_t* Q, bool do_mut, bool gather, bool do_fs, const Fold& fo) {
+                                               uint32_t* Q, bool do_mut, bool gather, bool do_fs, const Fold& fo,
+                                               bool inv = false) {
     float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
-    row_body_suf<1>(P, M, R, sfix, nullptr, Q, false, do_mut, gather, do_fs, fo, d);
+    row_body_suf<1>(P, M, R, sfix, nullptr, Q, inv, do_mut, gather, do_fs, fo, d);
     return make_float4(d[0], d[1], d[2], d[3]);
 }
 
@@ -835,11 +871,11 @@ struct PhaseClk {
 // at processing position v (k_row_plan): row, top strand, breakpoints, table
 // rows and correction ranks.  PROF: clock the row's phases into pc.
 // Returns false when the row's bulk copy was abandoned (the warp then stops working on rows).
-template <bool PROF, bool NARROW>
+template <bool PROF, bool NARROW, bool CM = false>
 __device__ __forceinline__ bool gen_row_suf(const PopDev& P, const DevStatus& st, uint32_t v, const uint64_t* sfix,
                                             uint64_t* mask, WarpSmem& ws, uint32_t& phase,
                                             const uint32_t* wait_limit, bool do_mut, bool do_ph, bool gather, bool do_fs,
-                                            const Fold& fo, PhaseClk& pc) {
+                                            const Fold& fo, PhaseClk& pc, uint32_t* cs = nullptr) {
     const uint32_t lane = threadIdx.x & 31u;
     const long long c0 = PROF ? clock64() : 0;
     long long c1 = 0, c2 = 0, c3 = 0;
@@ -860,15 +896,32 @@ __device__ __forceinline__ bool gen_row_suf(const PopDev& P, const DevStatus& st
     R.E = E;
     R.philox = P.mode == kModePhilox;
     R.evg = P.ev_pos + base;
-    if (E > 0 || !CLOTHO_COPY_BULK) prefetch_l2(R.top, R.Wp * 8u);
+    if (E > 0 || CM || !CLOTHO_COPY_BULK) prefetch_l2(R.top, R.Wp * 8u);
     if (E > 0) prefetch_l2(R.bot, R.Wp * 8u);
     R.zbase = pz;  // z(inv ? bottom : top) - sum(fixed), from the plan
     float d[kMaxTraits] = {0.f, 0.f, 0.f, 0.f};
     row_mutation_setup(P, st, pm.x, pm.y, do_mut, gather, R, d);
     bool landed = true;
     if (PROF) c1 = clock64();
-    if (flags & kPlanLong) {
-        add4(d, row_body_events(P, st.M, R, sfix, ws.q, do_mut, gather, do_fs, fo));
+    if ((flags & kPlanLong) || (CM && E > kCmMaxEv)) {
+        add4(d, row_body_events(P, st.M, R, sfix, ws.q, do_mut, gather, do_fs, fo, inv));
+    } else if (CM && E == 0) {
+        row_body_copy(P, st.M, R, sfix, do_mut, do_fs, fo);
+    } else if (CM) {
+        // chunk masks: the breakpoints' table-row offsets in lanes 0..E-1, their correction slots in cs
+        const uint32_t my_go = lane < E ? __ldg(P.plan_go + base + lane) : 0u;
+        const uint32_t my_cr = lane < E ? __ldg(P.plan_cr + base + lane) : 0u;
+        for (uint32_t k = 0; k < E; ++k) {  // the first chunk's table words, behind the corrections' set-up
+            const uint64_t* tk = P.suf + __shfl_sync(0xffffffffu, my_go, k);  // every lane takes part
+            if (2u * lane < R.Wp) asm volatile("prefetch.global.L1 [%0];" ::"l"(tk + 2u * lane));
+        }
+        __syncwarp();  // the previous row's reads of cs are done
+        for (uint32_t k = 0; k < E; ++k) {
+            const uint32_t pcr = __shfl_sync(0xffffffffu, my_cr, k);
+            cs[32u * k + lane] = lane < (pcr >> 20) ? __ldg(P.inv + (pcr & 0xfffffu) + lane) : 0xffffffffu;
+        }
+        __syncwarp();
+        row_body_suf<2>(P, st.M, R, sfix, nullptr, ws.q, inv, do_mut, gather, do_fs, fo, d, nullptr, cs, my_go);
     } else if (E == 0) {
 #if CLOTHO_COPY_BULK
         if (NARROW)
@@ -1259,7 +1312,7 @@ __device__ __forceinline__ void gen_row_iv(const PopDev& P, const DevStatus& st,
 // CNT (suffix-table builds, shared accumulators): per-column counts of the child rows of the populations
 // that asked (DevStatus::count_cols), in kCountPlanes bit-sliced planes after the WarpSmem array, flushed to
 // PopDev::colcnt when the block moves to another population and at the kernel's end.
-template <bool SUF, bool PROF, bool NARROW, bool CNT = false>
+template <bool SUF, bool PROF, bool NARROW, bool CNT = false, bool CM = false>
 __global__ void __launch_bounds__(kGenThreads, 1)
 k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restrict__ ctl, uint32_t fuse,
              int profile, uint32_t maxW, uint32_t acc_words, uint32_t mixed) {
@@ -1275,7 +1328,9 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     __shared__ uint32_t s_sm[kIvWarps][128];
     __shared__ uint32_t s_item, s_next;
     __shared__ uint32_t s_crows;   // CNT, one population: rows the block has counted
-    const uint32_t aw = SUF ? maxW : acc_words;
+    // the suffix-table builds keep their accumulators maxW words wide; the chunk-mask and interval builds
+    // hold rows of up to acc_words words in shared memory
+    const uint32_t aw = (SUF && !CM) ? maxW : acc_words;
     uint64_t* const sF0 = s_dyn;
     uint64_t* const sV0 = s_dyn + aw;
     uint64_t* const sfix0 = s_dyn + 2u * aw;
@@ -1283,13 +1338,17 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     uint64_t* sV = sV0;
     uint64_t* sfix = sfix0;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    // SUF: per-warp mask bitmaps [kWarps][maxW] u64, then one WarpSmem per warp
-    uint64_t* mask = s_dyn + (3u + (SUF ? warp : 0u)) * maxW;
-    WarpSmem& ws = reinterpret_cast<WarpSmem*>(s_dyn + (3u + kWarps) * maxW)[SUF ? warp : 0u];
+    // SUF: per-warp mask bitmaps [kWarps][maxW] u64, then one WarpSmem per warp; CM: no bitmaps, one WarpSmem
+    // per warp, then kCmCorr correction slots per warp
+    uint64_t* mask = s_dyn + (3u + ((SUF && !CM) ? warp : 0u)) * maxW;
+    WarpSmem* const wsa = reinterpret_cast<WarpSmem*>(s_dyn + (CM ? 3u * aw : (3u + kWarps) * maxW));
+    WarpSmem& ws = wsa[SUF ? warp : 0u];
+    uint32_t* const cs = CM ? reinterpret_cast<uint32_t*>(wsa + kWarps) + warp * kCmCorr : nullptr;
     uint32_t bphase = 0;  // parity of the warp's bulk-copy barrier
     const uint32_t* wait_limit = &ctl->wait_limit;  // read only when a copy is late
     if (SUF) {
-        for (uint32_t w = lane; w < maxW; w += 32u) mask[w] = 0ull;
+        if (!CM)
+            for (uint32_t w = lane; w < maxW; w += 32u) mask[w] = 0ull;
         if (lane == 0) {
             mbar_init(&ws.mbar);
             ws.dead = 0u;
@@ -1318,7 +1377,7 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
         const DevStatus st = *P.st;
         cur_pop = 0;
         cur_W = st.W;
-        cur_g = !SUF && max(st.W, st.pW) > acc_words;
+        cur_g = (!SUF || CM) && max(st.W, st.pW) > acc_words;
         if (cur_g) {
             sF = P.accF;
             sV = P.accV;
@@ -1356,8 +1415,8 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
                     }
                 }
                 if (SUF) {
-                    if (!gen_row_suf<PROF, NARROW>(P, st, v, sfix, mask, ws, bphase, wait_limit, do_mut, do_ph,
-                                                   gather, do_fs, fo, pc)) {
+                    if (!gen_row_suf<PROF, NARROW, CM>(P, st, v, sfix, mask, ws, bphase, wait_limit, do_mut, do_ph,
+                                                       gather, do_fs, fo, pc, cs)) {
                         ws.dead = 1u;
                         break;
                     }
@@ -1406,7 +1465,7 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             cur_pop = (int)p;
             cur_W = st.W;
             cur_A = st.A;
-            cur_g = !SUF && max(st.W, st.pW) > acc_words;
+            cur_g = (!SUF || CM) && max(st.W, st.pW) > acc_words;
             cur_cnt = CNT && do_fs && !cur_g && st.count_cols != 0u;
             crows = 0;
             if (cur_g) {
@@ -1471,8 +1530,8 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
                 // a warp whose copy never landed keeps taking its rows (leaving them undone) and the
                 // block's barriers
                 if (ws.dead) continue;
-                if (!gen_row_suf<PROF, NARROW>(P, st, v, sfix, mask, ws, bphase, wait_limit, do_mut, do_ph, gather,
-                                               do_fs, fo, pc))
+                if (!gen_row_suf<PROF, NARROW, CM>(P, st, v, sfix, mask, ws, bphase, wait_limit, do_mut, do_ph, gather,
+                                                   do_fs, fo, pc, cs))
                     ws.dead = 1u;
             } else
                 gen_row_iv(P, st, g, sfix, s_iv[warp], s_thr[warp], s_q[warp], s_sm[warp], do_mut, do_ph, gather,
@@ -1502,8 +1561,9 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     }
 }
 
-// The suffix-table classifier runs when every population has a table
-// (capacity <= kSufMaxSlots slots, so maxW <= 1,024 words).  Returns the error of
+// The suffix-table classifier runs when every population has a table (capacity <= kTableMaxSlots slots);
+// with every capacity <= kSufMaxSlots (maxW <= 1,024 words) in its per-warp bitmap builds, else in the
+// chunk-mask build.  Returns the error of
 // the shared-memory opt-in (the kernel is not launched then), else cudaSuccess.
 namespace {
 constexpr size_t kSmemLimit = 227u * 1024u;   // dynamic shared memory a block may opt into
@@ -1519,30 +1579,43 @@ bool generation_counts_fit(uint32_t maxW, uint32_t maxA) {
 cudaError_t launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, WorkCtl* ctl, uint32_t maxW,
                               uint32_t maxA, uint32_t fuse, int profile, bool count_on, bool mixed) {
     const uint32_t mx = mixed ? 1u : 0u;
-    const bool suf = maxA <= kSufMaxSlots;
+    // every population has a suffix table up to kTableMaxSlots slots; up to kSufMaxSlots its masks are built
+    // in per-warp bitmaps, above that (rows too wide for a bitmap per warp) chunk by chunk from the table
+    const bool suf = maxA <= kTableMaxSlots;
+    const bool cm = suf && maxA > kSufMaxSlots;
     // the counting build: column counters in shared memory (the phase-clock builds do not count)
     const bool cnt = count_on && profile != 2 && generation_counts_fit(maxW, maxA);
-    // the interval classifier keeps 3.5 KB of static shared memory per warp; its AND/OR accumulators and
+    // the interval classifier keeps 3.5 KB of static shared memory per warp, the chunk-mask build a
+    // WarpSmem and kCmCorr correction slots per warp in dynamic shared memory; their AND/OR accumulators and
     // fixed mask take what is left of 220 KB, rows of up to acc_words words (wider rows fold into the
-    // global accumulators).  acc_words is a multiple of kWordAlign, so the second and third regions start
-    // on 16-byte boundaries: the lanes access them as 16-byte word pairs.
-    const size_t acc_fit = (220u * 1024u - kWarps * 3584u) / (3u * sizeof(uint64_t)) / kWordAlign * kWordAlign;
-    const uint32_t acc_words = suf ? maxW : (uint32_t)std::min<size_t>(maxW, acc_fit);
-    const size_t smem = suf ? suf_smem(maxW, cnt) : 3ull * acc_words * sizeof(uint64_t);
+    // global accumulators).  acc_words is a multiple of kWordAlign, so every region starts on a 16-byte
+    // boundary: the lanes access them as 16-byte word pairs.
+    const size_t per_warp = cm ? sizeof(WarpSmem) + kCmCorr * sizeof(uint32_t) : 3584u;
+    const size_t acc_fit =
+        (220u * 1024u - 4096u - kWarps * per_warp) / (3u * sizeof(uint64_t)) / kWordAlign * kWordAlign;
+    // (the chunk-mask build keeps its accumulators to kCmAccWords words, so that L1 keeps room for the
+    // table words it prefetches a chunk ahead)
+    const uint32_t acc_words = (suf && !cm) ? maxW
+                               : cm         ? (uint32_t)std::min<size_t>(maxW, std::min<size_t>(acc_fit, kCmAccWords))
+                                            : (uint32_t)std::min<size_t>(maxW, acc_fit);
+    const size_t smem = cm    ? 3ull * acc_words * sizeof(uint64_t) + kWarps * per_warp
+                        : suf ? suf_smem(maxW, cnt)
+                              : 3ull * acc_words * sizeof(uint64_t);
     // profile 2: the suffix-table kernel's build with phase clocks; rows of at most
     // 128 words: its narrow build (copy rows by direct loads)
     const bool narrow = L.narrow_ok && maxW <= 64u * kDirectCopyChunks;
-    const int si = suf ? (profile == 2 ? (narrow ? 4 : 2) : cnt ? (narrow ? 6 : 5) : narrow ? 3 : 1) : 0;
-    const void* fns[7] = {(const void*)k_generation<false, false, false>, (const void*)k_generation<true, false, false>,
+    const int si = cm ? 7 : suf ? (profile == 2 ? (narrow ? 4 : 2) : cnt ? (narrow ? 6 : 5) : narrow ? 3 : 1) : 0;
+    const void* fns[8] = {(const void*)k_generation<false, false, false>, (const void*)k_generation<true, false, false>,
                           (const void*)k_generation<true, true, false>, (const void*)k_generation<true, false, true>,
                           (const void*)k_generation<true, true, true>,
                           (const void*)k_generation<true, false, false, true>,
-                          (const void*)k_generation<true, false, true, true>};
+                          (const void*)k_generation<true, false, true, true>,
+                          (const void*)k_generation<true, false, false, false, true>};
     // static shared memory is above 48 KB on its own, so the opt-in attribute is always needed; it is a
     // property of the function on each device, so it is kept per device (host threads share the table)
     {
         static std::mutex mu;
-        static size_t configured[kMaxGenDevices][7] = {};
+        static size_t configured[kMaxGenDevices][8] = {};
         int dev = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e != cudaSuccess) return e;
@@ -1556,6 +1629,10 @@ cudaError_t launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t n
         }
     }
     switch (si) {
+        case 7:
+            k_generation<true, false, false, false, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(
+                pops, npops, ctl, fuse, profile, maxW, acc_words, mx);
+            break;
         case 6:
             k_generation<true, false, true, true><<<L.num_sms, kGenThreads, smem, L.stream>>>(pops, npops, ctl, fuse,
                                                                                               profile, maxW, 0u, mx);
@@ -1733,12 +1810,20 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
                 flags = kPlanLong;  // tape rows with very long event lists: direct compares
             } else if (E > 0) {
                 uint32_t* cr = E <= kPlanSmemEv ? s_cr[threadIdx.x] : P.plan_cr + base;
+                // the chunk-mask build (which a batch may run for any of its suffix-table populations)
+                // classifies rows of more than kCmMaxEv breakpoints by direct compares against their
+                // positions, which device-drawn rows keep in the event list for it (rare: E > 16)
+                const bool keep_pos = philox && E > kCmMaxEv;
                 for (uint32_t k = 0; k < E; k += 2u) {
                     double e0, e1 = 0.0;
                     if (philox) {
                         const U4 a = philox4x32(g, 1u + (k >> 1), st.gen, kStreamGamete, P.seed);
                         e0 = u01(a.x, a.y);
                         e1 = u01(a.z, a.w);
+                        if (keep_pos) {
+                            P.ev_pos[base + k] = e0;
+                            if (k + 1u < E) P.ev_pos[base + k + 1u] = e1;
+                        }
                     } else {
                         e0 = __ldg(P.ev_pos + base + k);
                         if (k + 1u < E) e1 = __ldg(P.ev_pos + base + k + 1u);
@@ -1842,7 +1927,10 @@ __global__ void k_rank_final(const PopDev* __restrict__ pops, uint32_t npops) {
 }
 
 // suf[g * Wcap + w] = bits of word w whose slot has rank >= 64 g, for
-// g = 0 .. ceil(A/64) (the last row is empty).  A block covers 32 words.
+// g = 0 .. ceil(A/64) (the last row is empty).  A unit of work is 32 words and
+// every kSufSlices-th table row; the units are spread over the whole grid from
+// the current width, so the blocks are busy however wide the capacity is.
+constexpr uint32_t kSufSlices = 16;
 __global__ void __launch_bounds__(256) k_suf_build(const PopDev* __restrict__ pops, uint32_t npops) {
     __shared__ uint32_t s_grp[32][65];  // (rank >> 6) + 1 per slot, 0 beyond A
     const uint32_t tx = threadIdx.x & 31u, ty = threadIdx.x >> 5;
@@ -1851,7 +1939,9 @@ __global__ void __launch_bounds__(256) k_suf_build(const PopDev* __restrict__ po
         if (!P.suf) continue;
         const uint32_t A = P.st->A, W = P.st->W;
         const uint32_t Gt = (A + 63u) >> 6;
-        for (uint32_t wb = blockIdx.x * 32u; wb < W; wb += gridDim.x * 32u) {
+        const uint32_t wblocks = (W + 31u) / 32u;
+        for (uint32_t u = blockIdx.x; u < wblocks * kSufSlices; u += gridDim.x) {
+            const uint32_t wb = (u % wblocks) * 32u, slice = u / wblocks;
             __syncthreads();
             for (uint32_t i = threadIdx.x; i < 2048u; i += blockDim.x) {
                 const uint32_t s = wb * 64u + i;
@@ -1860,7 +1950,7 @@ __global__ void __launch_bounds__(256) k_suf_build(const PopDev* __restrict__ po
             __syncthreads();
             const uint32_t w = wb + tx;
             if (w >= W) continue;
-            for (uint32_t g = blockIdx.y * 8u + ty; g <= Gt; g += gridDim.y * 8u) {
+            for (uint32_t g = slice * 8u + ty; g <= Gt; g += kSufSlices * 8u) {
                 uint64_t m = 0;
 #pragma unroll 16
                 for (uint32_t b = 0; b < 64u; ++b) m |= (uint64_t)(s_grp[tx][b] > g) << b;
@@ -1878,9 +1968,8 @@ void launch_ranks(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32
     k_rank_scatter<<<g, 256, 0, L.stream>>>(pops, npops);
     k_rank_final<<<g, 256, 0, L.stream>>>(pops, npops);
     if (suf) {
-        const dim3 pg = pop_grid(npops, 0x7fffffffu, L.num_sms, 4);
-        const uint32_t gx = (maxW + 31u) / 32u;
-        k_suf_build<<<dim3(gx, max(1u, min(8u, pg.x / max(1u, gx))), pg.z), 256, 0, L.stream>>>(pops, npops);
+        const uint32_t units = (maxW + 31u) / 32u * kSufSlices;
+        k_suf_build<<<pop_grid(npops, units, L.num_sms, 4), 256, 0, L.stream>>>(pops, npops);
     }
 }
 

@@ -79,13 +79,13 @@ def test_narrow_and_wide_builds_agree():
 
 
 def test_each_population_keeps_its_classifier_in_a_mixed_batch():
-    # a batch holding a population of more than 65,536 slots (interval classifier) and a small one (suffix
+    # a batch holding a population of more than 524,288 slots (interval classifier) and a small one (suffix
     # table): the generation kernel runs one pass per classifier, so each population runs the classifier it
     # runs alone and its rows, spectrum and fitness are bit-identical to its run alone
     G = 15
     small = dict(N=400, T=2, mu=0.02, rho=4.0, fitness="gaussian_vs", fit_param=20.0, seed=31)
     big = dict(N=300, T=1, mu=0.05, rho=2.0, fitness="constant", fit_param=1.0, seed=32)
-    caps = (4096, 70_000)
+    caps = (4096, 600_000)
     descs, alone = [], []
     for s, cap in zip((small, big), caps):
         kw = {k: v for k, v in s.items() if k not in ("N", "T")}
@@ -112,11 +112,11 @@ def test_each_population_keeps_its_classifier_in_a_mixed_batch():
 
 
 def test_shared_and_global_accumulators_in_one_batch():
-    # an interval-classifier population whose rows pass 6,976 words in its first generation (480,000 new
-    # alleles: 40 individuals, mu = 6,000 per sequence) folds into its global AND/OR accumulators, batched
-    # with a narrow interval-classifier population and a suffix-table population that keep theirs in shared
-    # memory; the kernel's blocks move between the two kinds of population, and each population's rows,
-    # spectrum and fitness equal its run alone
+    # an interval-classifier population (1.2e6 slots) whose rows pass 6,976 words in its first generation
+    # (480,000 new alleles: 40 individuals, mu = 6,000 per sequence) folds into its global AND/OR
+    # accumulators, batched with a 73,728-slot population (chunk-mask build) and a 4,096-slot one, which alone
+    # runs the bitmap build and here the chunk-mask build of the batch's suffix-table pass; each population's
+    # rows, spectrum and fitness equal its run alone
     G = 3
     specs = [(dict(N=40, T=1, mu=6000.0, rho=2.0, fitness="gaussian_vs", fit_param=50.0, seed=41), 1_200_000),
              (dict(N=300, T=1, mu=0.05, rho=2.0, fitness="constant", fit_param=1.0, seed=42), 70_000),

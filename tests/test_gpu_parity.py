@@ -158,11 +158,18 @@ def test_many_events_beyond_register_set():
     run_parity(8, 100, 4096, mu=0.3, rho=24.0, p_neutral=1.0, q1=False)
 
 
-@pytest.mark.parametrize("A_cap", [70_000, 500_000])
-def test_wide_allele_space_interval_classifier(A_cap):
-    # capacities above 65,536 slots run the interval classifier over global
-    # ranks; at 500,000 the free-space fold also goes to global accumulators
+@pytest.mark.parametrize("A_cap", [70_000, 500_000, 600_000])
+def test_wide_allele_space_classifiers(A_cap):
+    # capacities above 65,536 slots: up to 524,288 slots the suffix table's masks are built chunk by chunk
+    # (chunk-mask build); above that the interval classifier tests every heterozygous bit by its rank
     run_parity(6, 60, A_cap, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.5, rho=3.0, p_neutral=0.5)
+
+
+def test_chunk_masks_with_many_breakpoints():
+    # the chunk-mask build (70,000 slots) with rho = 20 and Q1 off: rows of up to 16 breakpoints take their
+    # masks from the table, longer ones compare every heterozygous bit with the breakpoint positions
+    run_parity(8, 80, 70_000, T=2, fitness="gaussian_vs", fit_param=4.0, mu=2.0, rho=20.0, p_neutral=0.5,
+               q1=False)
 
 
 def test_suffix_table_boundaries():
@@ -205,10 +212,10 @@ def test_seeded_population_parity():
 
 
 def test_rows_wider_than_the_shared_accumulators():
-    # 460,000 seeded allele slots (7,192-word rows): wider than the interval-classifier kernel's shared-memory
-    # AND/OR accumulators hold (6,976 words), so its fold goes to the population's global accumulators and it
-    # reads the fixed mask from global memory; carrier fractions U[0, 1) give fixed and lost columns, and
-    # 4,000 new alleles a generation reuse their slots
+    # 460,000 seeded allele slots (7,192-word rows, the chunk-mask build): wider than its shared-memory AND/OR
+    # accumulators hold (6,464 words), so its fold goes to the population's global accumulators and it reads
+    # the fixed mask from global memory; carrier fractions U[0, 1) give fixed and lost columns, and 4,000 new
+    # alleles a generation reuse their slots
     rng = np.random.default_rng(17)
     N, A, T = 40, 460_000, 1
     pos = rng.random(A)
@@ -223,7 +230,7 @@ def test_rows_wider_than_the_shared_accumulators():
     for g in range(4):
         gpu.simulate(orc.step_record(N))
         compare_state(orc, gpu, g, kind="gaussian_vs", fit_param=500.0, mu=50.0)
-    assert gpu.info()["fixed_total"] > 0 and gpu.info()["W"] > 6976
+    assert gpu.info()["fixed_total"] > 0 and gpu.info()["W"] > 6464
 
 
 def test_edge_tie_breakpoint_equals_position():
@@ -588,7 +595,7 @@ def test_c2_qtl_selection_at_its_stated_population_size(capsys):
     # the QTL-with-selection configuration at its stated size: N = 1e5 (2e5 rows), mu = 0.1 per sequence
     # (2e4 new alleles a generation), rho = 1, one trait with N(0,1) effects, exp(-z^2/2), parents from the
     # FP64 prefix sum over 1e5 fitness values (25 scan chunks), parent-major ordering over 1e5 parents; the
-    # allele count passes 65,536 slots, so the interval classifier runs.  12 generations (the oracle's
+    # allele count passes 65,536 slots, so the chunk-mask build runs.  12 generations (the oracle's
     # cost grows with the rows' width); state compared every fourth generation and at the end.
     import os
     from clotho_gb300 import workloads
