@@ -30,7 +30,14 @@ struct PopHost {
 
 struct Geometry {
     uint32_t Ncap, Scap, Wcap, Aslots, Mcap, EVcap, FXcap, T, NB;
+    bool table;  // the population has a suffix table (its crossover classifier)
 };
+
+// Suffix tables above kSufMaxSlots slots (masks chunk by chunk) pay for themselves at low recombination: on
+// GB300 at 2,352-word rows and rho = 1 the chunk-mask kernel took 2.65 against the interval classifier's
+// 3.20 ms, while at 472-word rows it took 0.44 / 0.59 / 0.82 ms a generation against 0.45 / 0.51 / 0.60 ms at
+// rho = 0.5 / 2 / 5 (each row's breakpoints cost a table load per chunk).
+constexpr double kChunkMaxRho = 1.0;
 
 Geometry geometry(const clotho_desc& d) {
     Geometry g{};
@@ -45,6 +52,7 @@ Geometry geometry(const clotho_desc& d) {
     g.T = d.traits;
     g.NB = 1024;
     while (g.NB < g.Aslots) g.NB <<= 1;
+    g.table = g.Aslots <= kSufMaxSlots || (g.Aslots <= kTableMaxSlots && d.rho <= kChunkMaxRho);
     return g;
 }
 
@@ -63,16 +71,16 @@ std::vector<size_t> sizes_of(const Geometry& g) {
         (S + 1) * 4 * 2ull,              // row_cnt, row_off
         S * 4, g.Mcap * 4ull, g.Mcap * 4ull,  // row_cur, row_mut, mut_slot
         (g.NB + 1ull) * 4 * 2, g.NB * 4ull, A * 8, A * 4, A * 4,  // bcnt+boff, bcur, bpos, bslot, rank
-        A <= kTableMaxSlots ? A * 4 : 0,                            // inv
-        A <= kTableMaxSlots ? (A / 64 + 1) * W * 8 : 0,             // suf
-        A <= kTableMaxSlots ? S * 16 : 0,                           // plan_row
-        A <= kTableMaxSlots ? (S + 1) * 4 * 2 : 0,                  // ord_cnt + ord_off
-        A <= kTableMaxSlots ? S * 4 : 0,                            // ord_cur
-        A <= kTableMaxSlots ? S * 4 : 0,                            // ord_pos
-        A <= kTableMaxSlots ? g.EVcap * 4ull : 0,                   // plan_go
-        A <= kTableMaxSlots ? g.EVcap * 4ull : 0,                   // plan_cr
-        A <= kTableMaxSlots ? S * 8 : 0,                            // plan_mut
-        A <= kTableMaxSlots ? S * 32 : 0,                           // plan_z
+        g.table ? A * 4 : 0,                            // inv
+        g.table ? (A / 64 + 1) * W * 8 : 0,             // suf
+        g.table ? S * 16 : 0,                           // plan_row
+        g.table ? (S + 1) * 4 * 2 : 0,                  // ord_cnt + ord_off
+        g.table ? S * 4 : 0,                            // ord_cur
+        g.table ? S * 4 : 0,                            // ord_pos
+        g.table ? g.EVcap * 4ull : 0,                   // plan_go
+        g.table ? g.EVcap * 4ull : 0,                   // plan_cr
+        g.table ? S * 8 : 0,                            // plan_mut
+        g.table ? S * 32 : 0,                           // plan_z
         A * 4,                                                    // colcnt
         sizeof(DevStatus),
         // two tape sets: pairs, swap, ev_off, ev_pos, mut_seq, mut_pos, mut_eff
@@ -122,8 +130,10 @@ struct clotho_ctx {
     std::vector<uint32_t> graph_key;
     bool in_step = false;
     uint32_t maxW = 0, maxS = 0, maxN = 0, maxNB = 0, maxA = 0;
-    // per classifier: populations of at most kTableMaxSlots slots (suffix table) and the others (intervals)
+    // per generation-kernel build: suffix-table masks in bitmaps (bm, at most kSufMaxSlots slots) or chunk by
+    // chunk (cm, the other populations with a table), interval classifier (iv, no table); suf = bm + cm
     uint32_t n_suf = 0, n_iv = 0, maxW_suf = 0, maxW_iv = 0, maxA_suf = 0, maxA_iv = 0;
+    uint32_t n_bm = 0, n_cm = 0, maxW_bm = 0, maxW_cm = 0, maxA_bm = 0, maxA_cm = 0;
     cudaError_t launch_err = cudaSuccess;  // a launch set-up failure, reported by the next check_launch
     uint32_t ind_per_sm = 16;               // tuning (clotho_set_tuning)
     bool narrow_ok = true;
@@ -293,6 +303,7 @@ int sync_pop_arrays(clotho_ctx* ctx, uint32_t from = 0) {
     }
     ctx->maxW = ctx->maxS = ctx->maxN = ctx->maxNB = ctx->maxA = 0;
     ctx->n_suf = ctx->n_iv = ctx->maxW_suf = ctx->maxW_iv = ctx->maxA_suf = ctx->maxA_iv = 0;
+    ctx->n_bm = ctx->n_cm = ctx->maxW_bm = ctx->maxW_cm = ctx->maxA_bm = ctx->maxA_cm = 0;
     for (PopHost* p : ctx->pops) {
         const PopDev& D = p->dev[0];
         ctx->maxW = std::max(ctx->maxW, D.Wcap);
@@ -300,10 +311,19 @@ int sync_pop_arrays(clotho_ctx* ctx, uint32_t from = 0) {
         ctx->maxN = std::max(ctx->maxN, D.Ncap);
         ctx->maxNB = std::max(ctx->maxNB, D.NB);
         ctx->maxA = std::max(ctx->maxA, D.Acap);
-        if (D.Acap <= kTableMaxSlots) {
+        if (D.suf != nullptr) {
             ctx->n_suf += 1;
             ctx->maxW_suf = std::max(ctx->maxW_suf, D.Wcap);
             ctx->maxA_suf = std::max(ctx->maxA_suf, D.Acap);
+            if (D.Acap <= kSufMaxSlots) {
+                ctx->n_bm += 1;
+                ctx->maxW_bm = std::max(ctx->maxW_bm, D.Wcap);
+                ctx->maxA_bm = std::max(ctx->maxA_bm, D.Acap);
+            } else {
+                ctx->n_cm += 1;
+                ctx->maxW_cm = std::max(ctx->maxW_cm, D.Wcap);
+                ctx->maxA_cm = std::max(ctx->maxA_cm, D.Acap);
+            }
         } else {
             ctx->n_iv += 1;
             ctx->maxW_iv = std::max(ctx->maxW_iv, D.Wcap);
@@ -360,26 +380,33 @@ int prof_collect(clotho_ctx* ctx) {
 // The fused step's generation kernel counts columns (its counting build) when a population asked and the
 // counters fit in shared memory; k_fs_finalize of the same step zeroes those counts and marks them valid.
 bool count_on(clotho_ctx* ctx, uint32_t fuse) {
-    return ctx->counting > 0 && ctx->n_suf > 0 && (fuse & kFuseFs) && !(ctx->profiling && ctx->phase_clocks) &&
-           generation_counts_fit(ctx->maxW_suf, ctx->maxA_suf);
+    return ctx->counting > 0 && ctx->n_bm > 0 && (fuse & kFuseFs) && !(ctx->profiling && ctx->phase_clocks) &&
+           generation_counts_fit(ctx->maxW_bm, ctx->maxA_bm);
 }
 
-// The generation kernel over every population: one launch when all populations use the same classifier;
-// in a batch that mixes them, one launch per classifier, each over its own populations (the suffix-table
-// pass first), so every population runs the classifier it runs alone.
+// The generation kernel over every population: one launch when all populations use the same build; in a
+// batch that mixes them, one launch per build (bitmap, chunk-mask, interval), each over its own populations,
+// so every population runs the build it runs alone.
 void launch_gen(clotho_ctx* ctx, const PopDev* pops, uint32_t npops, uint32_t fuse) {
     if (ctx->n_suf > 0) {  // per-row crossover plans of the suffix-table classifier (other populations skip it)
         launch_plan(cfg(ctx), pops, npops, ctx->maxS);
         ctx->launches += 6;  // order count, 3-kernel scan, order scatter, plan
     }
     const int prof = ctx->profiling ? (ctx->phase_clocks ? 2 : 1) : 0;
-    const bool mixed = ctx->n_suf > 0 && ctx->n_iv > 0;
+    const uint32_t kinds = (ctx->n_bm > 0) + (ctx->n_cm > 0) + (ctx->n_iv > 0);
+    const bool mixed = kinds > 1;
     const bool cnt = count_on(ctx, fuse);
-    for (int pass = 0; pass < (mixed ? 2 : 1); ++pass) {
-        const uint32_t W = mixed ? (pass == 0 ? ctx->maxW_suf : ctx->maxW_iv) : ctx->maxW;
-        const uint32_t A = mixed ? (pass == 0 ? ctx->maxA_suf : ctx->maxA_iv) : ctx->maxA;
+    const uint32_t pn[3] = {ctx->n_bm, ctx->n_cm, ctx->n_iv};
+    const uint32_t pW[3] = {ctx->maxW_bm, ctx->maxW_cm, ctx->maxW_iv};
+    const uint32_t pA[3] = {ctx->maxA_bm, ctx->maxA_cm, ctx->maxA_iv};
+    const GenBuild builds[3] = {kBuildBitmap, kBuildChunk, kBuildInterval};
+    for (int pass = 0; pass < 3; ++pass) {
+        if (pn[pass] == 0) continue;
+        const uint32_t W = mixed ? pW[pass] : ctx->maxW;
+        const uint32_t A = mixed ? pA[pass] : ctx->maxA;
         prof_begin(ctx);
-        const cudaError_t e = launch_generation(cfg(ctx), pops, npops, ctx->d_ctl, W, A, fuse, prof, cnt, mixed);
+        const cudaError_t e =
+            launch_generation(cfg(ctx), pops, npops, ctx->d_ctl, W, A, fuse, prof, builds[pass], cnt, mixed);
         if (e != cudaSuccess && ctx->launch_err == cudaSuccess) ctx->launch_err = e;
         prof_end(ctx);
         ctx->launches += 1;
@@ -929,8 +956,8 @@ int clotho_crossover(clotho_ctx* ctx, const uint8_t* swap, const uint32_t* ev_of
     if ((rc = h2d(ctx, D.ev_off, ev_off, 2ull * N + 1, ctx->stream))) return rc;
     if ((rc = h2d(ctx, D.ev_pos, ev_pos, (size_t)ev_total, ctx->stream))) return rc;
     // item prefix is already set by begin; ranks over the current positions
-    launch_ranks(cfg(ctx), ctx->d_pops[0], 1, ctx->maxNB, ctx->maxW, ctx->maxA <= kTableMaxSlots);
-    ctx->launches += 6u + (ctx->maxA <= kTableMaxSlots ? 1u : 0u);
+    launch_ranks(cfg(ctx), ctx->d_pops[0], 1, ctx->maxNB, ctx->maxW, ctx->n_suf > 0);
+    ctx->launches += 6u + (ctx->n_suf > 0 ? 1u : 0u);
     launch_gen(ctx, ctx->d_pops[0], 1, 0u);
     if ((rc = check_launch(ctx, "crossover"))) return rc;
     CK(cudaStreamSynchronize(ctx->stream));

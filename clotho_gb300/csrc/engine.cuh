@@ -22,8 +22,12 @@ constexpr uint32_t kMaxEvDevice = 128;     // device-drawn events per gamete
 constexpr uint32_t kMaxMutReg = 32;        // mutations per row held in registers
 constexpr uint32_t kWordAlign = 64;        // row stride granularity (words)
 constexpr uint32_t kSufMaxSlots = 65536;   // allele capacity up to which suffix-table masks are built in per-warp bitmaps
-constexpr uint32_t kTableMaxSlots = 1u << 19;  // allele capacity up to which a population has a suffix table
-                                               // (above kSufMaxSlots its masks are XORed chunk by chunk)
+#ifndef CLOTHO_TABLE_MAX_SLOTS
+#define CLOTHO_TABLE_MAX_SLOTS (1u << 19)
+#endif
+// allele capacity up to which a population has a suffix table (above kSufMaxSlots its masks are XORed chunk
+// by chunk); at least kSufMaxSlots
+constexpr uint32_t kTableMaxSlots = CLOTHO_TABLE_MAX_SLOTS;
 
 // sticky device error bits (CLOTHO_DEVERR_* in clotho_gpu.h)
 constexpr uint32_t kErrAlleles = 1u, kErrFixed = 2u, kErrEvents = 4u, kErrParent = 8u,
@@ -125,6 +129,7 @@ struct WorkCtl {
     uint32_t wait_limit;            // try_wait rounds before a bulk copy is flagged late (0: default)
     uint32_t item_base[257];        // item prefix per population (<= 256 pops)
     uint32_t gen_counter_iv;        // item counter of the interval-classifier pass of a mixed batch
+    uint32_t gen_counter_cm;        // item counter of the chunk-mask pass of a mixed batch
     uint64_t rows_done;             // profiling: rows processed
     uint64_t words_done;            // profiling: words written
     uint64_t phase[16];             // profiling: k_generation phase cycles (kPh*)
@@ -291,14 +296,15 @@ void launch_mut_csr_tape(const LaunchCfg&, const PopDev* pops, uint32_t npops, u
 void launch_mut_counts_philox(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
 void launch_mut_resolve(const LaunchCfg&, const PopDev* pops, uint32_t npops);
 void launch_select_philox(const LaunchCfg&, const PopDev* pops, uint32_t npops);
-// mixed: the batch holds populations of both classifiers (suffix table: capacity <= kTableMaxSlots; intervals:
-// above); this launch runs only the populations of its own classifier (maxW, maxA are theirs) and skips the
-// others' items, so each population keeps its classifier whatever it is batched with.  The suffix-table
-// launch builds its masks in per-warp bitmaps when every one of its populations has at most kSufMaxSlots
-// slots, else chunk by chunk from the table (the same masks)
+// Generation-kernel builds: suffix-table masks in per-warp bitmaps (capacity <= kSufMaxSlots), chunk by
+// chunk from the table (populations with a table above that), interval classifier (populations without a
+// table).  mixed: the batch holds populations of more than one kind; this launch runs only the populations
+// of its own kind (build; maxW, maxA are theirs) and skips the others' items, so each population keeps the
+// build it runs alone whatever it is batched with
+enum GenBuild : int { kBuildInterval = 0, kBuildBitmap = 1, kBuildChunk = 2 };
 cudaError_t launch_generation(const LaunchCfg&, const PopDev* pops, uint32_t npops, WorkCtl* ctl,
-                              uint32_t maxW, uint32_t maxA, uint32_t fuse, int profile, bool count_on = false,
-                              bool mixed = false);
+                              uint32_t maxW, uint32_t maxA, uint32_t fuse, int profile, GenBuild build,
+                              bool count_on = false, bool mixed = false);
 // whether the generation kernel's counting build fits this launch (suffix-table rows, counters in shared memory)
 bool generation_counts_fit(uint32_t maxW, uint32_t maxA);
 void launch_mut_scatter(const LaunchCfg&, const PopDev* pops, uint32_t npops);

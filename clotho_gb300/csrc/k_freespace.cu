@@ -107,7 +107,8 @@ __global__ void __launch_bounds__(1024) k_fs_finalize(const PopDev* __restrict__
     DevStatus* st = P.st;
     // column counts of this step's child rows, for the populations that asked: zeroed here, added by the
     // generation kernel's counting build
-    const bool counting = count_on && st->count_cols != 0u && P.suf != nullptr;  // the suffix-table builds count
+    // the bitmap builds of the suffix-table classifier count (capacity <= kSufMaxSlots)
+    const bool counting = count_on && st->count_cols != 0u && P.suf != nullptr && P.Acap <= kSufMaxSlots;
     if (counting)
         for (uint32_t a = threadIdx.x; a < P.Acap; a += 1024u) P.colcnt[a] = 0u;
     __shared__ uint32_t s_warp[32];

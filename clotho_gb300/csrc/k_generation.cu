@@ -783,15 +783,24 @@ __device__ __forceinline__ void row_body_suf(const PopDev& P, uint32_t M, const 
                     m1 = m.y;
                 }
             } else if (MODE == 2) {
-                // table rows (L2-resident) of the row's breakpoints; words past the parent's width take no
-                // switch.  The next chunk's words are prefetched into L1 behind this chunk's work.
-                for (uint32_t k = 0; k < R.E; ++k) {
-                    const uint64_t* tk = P.suf + __shfl_sync(0xffffffffu, my_go, k);
-                    if (w + 64u < R.Wp) asm volatile("prefetch.global.L1 [%0];" ::"l"(tk + w + 64u));
-                    if (live && w < R.Wp) {
-                        const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(tk + w));
-                        m0 ^= v.x;
-                        m1 ^= v.y;
+                // table rows (L2-resident) of the row's breakpoints, four loads in flight; words past the
+                // parent's width take no switch.  The next chunk's words are prefetched into L1 behind this
+                // chunk's work.
+                for (uint32_t k0 = 0; k0 < R.E; k0 += 4u) {
+                    ulonglong2 v[4];
+#pragma unroll
+                    for (uint32_t j = 0; j < 4u; ++j) {
+                        const uint32_t k = k0 + j;
+                        const uint64_t* tk = P.suf + __shfl_sync(0xffffffffu, my_go, k & 31u);
+                        const bool on = k < R.E;
+                        if (on && w + 64u < R.Wp) asm volatile("prefetch.global.L1 [%0];" ::"l"(tk + w + 64u));
+                        v[j] = (on && live && w < R.Wp) ? __ldg(reinterpret_cast<const ulonglong2*>(tk + w))
+                                                        : make_ulonglong2(0, 0);
+                    }
+#pragma unroll
+                    for (uint32_t j = 0; j < 4u; ++j) {
+                        m0 ^= v[j].x;
+                        m1 ^= v[j].y;
                     }
                 }
                 // correction slots that fall in this chunk: each is toggled by the lane that owns its word
@@ -1431,7 +1440,10 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     for (; npops > 1;) {
         if (threadIdx.x == 0) {
             // a mixed batch runs one pass per classifier, each on its own counter over the same items
-            s_item = atomicAdd((SUF || !mixed) ? &ctl->gen_counter : &ctl->gen_counter_iv, 1u);
+            s_item = atomicAdd(!mixed || (SUF && !CM) ? &ctl->gen_counter
+                               : CM                   ? &ctl->gen_counter_cm
+                                                      : &ctl->gen_counter_iv,
+                               1u);
             s_next = 0;
         }
         __syncthreads();
@@ -1447,7 +1459,9 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
             p = lo;
         }
         const PopDev& P = pops[p];
-        if (mixed && (SUF != (P.suf != nullptr))) {  // the other classifier's pass takes this item
+        // the build of this population (by its capacity) against this launch's build
+        const uint32_t kind = P.suf == nullptr ? 0u : P.Acap > kSufMaxSlots ? 2u : 1u;
+        if (mixed && kind != (SUF ? (CM ? 2u : 1u) : 0u)) {  // another pass takes this item
             __syncthreads();
             continue;
         }
@@ -1577,14 +1591,14 @@ bool generation_counts_fit(uint32_t maxW, uint32_t maxA) {
 }
 
 cudaError_t launch_generation(const LaunchCfg& L, const PopDev* pops, uint32_t npops, WorkCtl* ctl, uint32_t maxW,
-                              uint32_t maxA, uint32_t fuse, int profile, bool count_on, bool mixed) {
+                              uint32_t maxA, uint32_t fuse, int profile, GenBuild build, bool count_on, bool mixed) {
     const uint32_t mx = mixed ? 1u : 0u;
-    // every population has a suffix table up to kTableMaxSlots slots; up to kSufMaxSlots its masks are built
-    // in per-warp bitmaps, above that (rows too wide for a bitmap per warp) chunk by chunk from the table
-    const bool suf = maxA <= kTableMaxSlots;
-    const bool cm = suf && maxA > kSufMaxSlots;
+    // suffix-table populations up to kSufMaxSlots slots build their masks in per-warp bitmaps; wider ones
+    // (rows too wide for a bitmap per warp) chunk by chunk from the table
+    const bool suf = build != kBuildInterval;
+    const bool cm = build == kBuildChunk;
     // the counting build: column counters in shared memory (the phase-clock builds do not count)
-    const bool cnt = count_on && profile != 2 && generation_counts_fit(maxW, maxA);
+    const bool cnt = count_on && profile != 2 && build == kBuildBitmap && generation_counts_fit(maxW, maxA);
     // the interval classifier keeps 3.5 KB of static shared memory per warp, the chunk-mask build a
     // WarpSmem and kCmCorr correction slots per warp in dynamic shared memory; their AND/OR accumulators and
     // fixed mask take what is left of 220 KB, rows of up to acc_words words (wider rows fold into the

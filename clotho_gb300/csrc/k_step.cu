@@ -70,6 +70,7 @@ __global__ void k_begin(const PopDev* __restrict__ pops, uint32_t npops, const u
         ctl->gen_items = acc;
         ctl->gen_counter = 0;
         ctl->gen_counter_iv = 0;
+        ctl->gen_counter_cm = 0;
     }
 }
 

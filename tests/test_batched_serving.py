@@ -114,12 +114,12 @@ def test_each_population_keeps_its_classifier_in_a_mixed_batch():
 def test_shared_and_global_accumulators_in_one_batch():
     # an interval-classifier population (1.2e6 slots) whose rows pass 6,976 words in its first generation
     # (480,000 new alleles: 40 individuals, mu = 6,000 per sequence) folds into its global AND/OR
-    # accumulators, batched with a 73,728-slot population (chunk-mask build) and a 4,096-slot one, which alone
-    # runs the bitmap build and here the chunk-mask build of the batch's suffix-table pass; each population's
-    # rows, spectrum and fitness equal its run alone
+    # accumulators, batched with a 73,728-slot population (chunk-mask build) and a 4,096-slot one (bitmap
+    # build): three passes of the generation kernel over the same items, and each population's rows,
+    # spectrum and fitness equal its run alone
     G = 3
     specs = [(dict(N=40, T=1, mu=6000.0, rho=2.0, fitness="gaussian_vs", fit_param=50.0, seed=41), 1_200_000),
-             (dict(N=300, T=1, mu=0.05, rho=2.0, fitness="constant", fit_param=1.0, seed=42), 70_000),
+             (dict(N=300, T=1, mu=0.05, rho=1.0, fitness="constant", fit_param=1.0, seed=42), 70_000),
              (dict(N=400, T=2, mu=0.02, rho=4.0, fitness="gaussian_vs", fit_param=20.0, seed=43), 4096)]
     descs, alone = [], []
     for s, cap in specs:

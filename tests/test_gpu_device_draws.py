@@ -303,7 +303,7 @@ def test_bench_configuration_at_full_size_bit_exact(mode, capsys):
     gpu.close()
 
 
-@pytest.mark.parametrize("case", ["qtl_selection", "q1_off_quadratic", "chunk_masks", "chunk_masks_long_rows",
+@pytest.mark.parametrize("case", ["qtl_selection", "q1_off_quadratic", "chunk_masks", "many_breakpoints",
                                   "interval_classifier", "size_changes"])
 def test_device_generations_bit_exact(case):
     if case == "qtl_selection":      # C2-shaped: one trait, N(0,1) effects, exp(-z^2/2)
@@ -312,10 +312,10 @@ def test_device_generations_bit_exact(case):
     elif case == "q1_off_quadratic":
         kw = dict(T=3, fitness="quadratic", fit_param=3.0, mu=0.2, rho=3.0, bias=0.3, q1=False, p_neutral=0.5)
         sizes, A_cap = [200] * 15, 8192
-    elif case == "chunk_masks":           # capacity above 65,536 slots: masks chunk by chunk from the table
-        kw = dict(T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.5, rho=3.0, bias=0.5, q1=True, p_neutral=0.5)
+    elif case == "chunk_masks":           # capacity above 65,536 slots, rho <= 1: masks chunk by chunk
+        kw = dict(T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.5, rho=1.0, bias=0.5, q1=False, p_neutral=0.5)
         sizes, A_cap = [100] * 8, 70_000
-    elif case == "chunk_masks_long_rows":  # rho = 20: most rows have more than 16 breakpoints
+    elif case == "many_breakpoints":      # rho = 20 (interval classifier): most rows have > 16 breakpoints
         kw = dict(T=1, fitness="gaussian_vs", fit_param=4.0, mu=0.5, rho=20.0, bias=0.5, q1=False, p_neutral=0.5)
         sizes, A_cap = [80] * 6, 70_000
     elif case == "interval_classifier":   # capacity above 524,288 slots

@@ -158,18 +158,31 @@ def test_many_events_beyond_register_set():
     run_parity(8, 100, 4096, mu=0.3, rho=24.0, p_neutral=1.0, q1=False)
 
 
-@pytest.mark.parametrize("A_cap", [70_000, 500_000, 600_000])
-def test_wide_allele_space_classifiers(A_cap):
-    # capacities above 65,536 slots: up to 524,288 slots the suffix table's masks are built chunk by chunk
-    # (chunk-mask build); above that the interval classifier tests every heterozygous bit by its rank
-    run_parity(6, 60, A_cap, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.5, rho=3.0, p_neutral=0.5)
+@pytest.mark.parametrize("A_cap,rho", [(70_000, 1.0), (500_000, 0.8), (70_000, 3.0), (600_000, 1.0)])
+def test_wide_allele_space_classifiers(A_cap, rho):
+    # capacities above 65,536 slots: up to 524,288 slots and rho <= 1 the suffix table's masks are built
+    # chunk by chunk (chunk-mask build); otherwise the interval classifier tests every heterozygous bit by
+    # its rank
+    run_parity(6, 60, A_cap, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.5, rho=rho, p_neutral=0.5)
 
 
 def test_chunk_masks_with_many_breakpoints():
-    # the chunk-mask build (70,000 slots) with rho = 20 and Q1 off: rows of up to 16 breakpoints take their
-    # masks from the table, longer ones compare every heterozygous bit with the breakpoint positions
-    run_parity(8, 80, 70_000, T=2, fitness="gaussian_vs", fit_param=4.0, mu=2.0, rho=20.0, p_neutral=0.5,
-               q1=False)
+    # the chunk-mask build (70,000 slots; the population's rho of 1 selects it) on tapes drawn with rho = 20
+    # and Q1 off: rows of up to 16 breakpoints take their masks from the table, longer ones compare every
+    # heterozygous bit with the breakpoint positions
+    N, G = 80, 8
+    orc = oracle.Oracle(T=2, fitness=FITS["gaussian_vs"], fit_param=4.0, mu=2.0, rho=20.0, p_neutral=0.5,
+                        q1=False, threads=2, seed=11)
+    gpu = cg.Population(N, 70_000, 2, fitness="gaussian_vs", fit_param=4.0, mu=2.0, rho=1.0, p_neutral=0.5,
+                        q1=False, seed=11, max_events=int(4 * N * 20.0 + 4096), max_mutations=int(4 * N * 2.0 + 4096),
+                        max_fixed=1 << 16)
+    orc.init(N)
+    gpu.init(N)
+    for g in range(G):
+        tape = orc.step_record(N)
+        assert np.diff(tape.ev_off).max() > 16
+        gpu.simulate(tape)
+        compare_state(orc, gpu, g, kind="gaussian_vs", fit_param=4.0, mu=2.0)
 
 
 def test_suffix_table_boundaries():
@@ -211,17 +224,18 @@ def test_seeded_population_parity():
         compare_state(orc, gpu, g, kind="gaussian_vs", fit_param=50.0)
 
 
-def test_rows_wider_than_the_shared_accumulators():
-    # 460,000 seeded allele slots (7,192-word rows, the chunk-mask build): wider than its shared-memory AND/OR
-    # accumulators hold (6,464 words), so its fold goes to the population's global accumulators and it reads
-    # the fixed mask from global memory; carrier fractions U[0, 1) give fixed and lost columns, and 4,000 new
-    # alleles a generation reuse their slots
+@pytest.mark.parametrize("rho", [1.0, 3.0])
+def test_rows_wider_than_the_shared_accumulators(rho):
+    # 460,000 seeded allele slots (7,192-word rows): wider than the shared-memory AND/OR accumulators of the
+    # chunk-mask build (rho = 1: 3,072 words) and of the interval classifier (rho = 3: 6,976 words) hold, so
+    # the fold goes to the population's global accumulators and the fixed mask is read from global memory;
+    # carrier fractions U[0, 1) give fixed and lost columns, and 4,000 new alleles a generation reuse slots
     rng = np.random.default_rng(17)
     N, A, T = 40, 460_000, 1
     pos = rng.random(A)
     eff = (rng.standard_normal(A * T) * 0.02).astype(np.float32)
     thr = (rng.random(A) * 2 ** 32).astype(np.uint64).clip(0, 2 ** 32 - 1).astype(np.uint32)
-    orc, gpu = make_pair(N, 480_000, T=T, fitness="gaussian_vs", fit_param=500.0, mu=50.0, rho=3.0,
+    orc, gpu = make_pair(N, 480_000, T=T, fitness="gaussian_vs", fit_param=500.0, mu=50.0, rho=rho,
                          p_neutral=0.3)
     orc.seed_population(N, pos, eff, thr, 7)
     gpu.seed_population(N, pos, eff, thr, 7)
@@ -230,7 +244,7 @@ def test_rows_wider_than_the_shared_accumulators():
     for g in range(4):
         gpu.simulate(orc.step_record(N))
         compare_state(orc, gpu, g, kind="gaussian_vs", fit_param=500.0, mu=50.0)
-    assert gpu.info()["fixed_total"] > 0 and gpu.info()["W"] > 6464
+    assert gpu.info()["fixed_total"] > 0 and gpu.info()["W"] > 6976
 
 
 def test_edge_tie_breakpoint_equals_position():
