@@ -191,9 +191,12 @@ def test_suffix_table_boundaries():
     run_parity(12, 120, 8192, mu=2.0, rho=12.0, p_neutral=1.0, q1=False)
 
 
-def test_staged_policies_equal_fused():
-    orc, gpu = make_pair(180, 4096, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.2, rho=1.5, p_neutral=0.4)
-    gpu2 = cg.Population(180, 4096, 2, fitness="gaussian_vs", fit_param=4.0, mu=0.2, rho=1.5, p_neutral=0.4,
+@pytest.mark.parametrize("A_cap,rho", [(4096, 1.5), (70_000, 1.0), (70_000, 1.5)])
+def test_staged_policies_equal_fused(A_cap, rho):
+    # the staged stage-by-stage calls against the fused step, for each generation-kernel build: bitmap
+    # masks, chunk masks (70,000 slots at rho <= 1), interval classifier
+    orc, gpu = make_pair(180, A_cap, T=2, fitness="gaussian_vs", fit_param=4.0, mu=0.2, rho=rho, p_neutral=0.4)
+    gpu2 = cg.Population(180, A_cap, 2, fitness="gaussian_vs", fit_param=4.0, mu=0.2, rho=rho, p_neutral=0.4,
                          max_events=8192, max_mutations=8192, max_fixed=1 << 16)
     orc.init(180)
     gpu.init(180)
