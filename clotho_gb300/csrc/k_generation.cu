@@ -400,8 +400,8 @@ struct WarpSmem {
     uint32_t pad;
 };
 
-// Copy rows: 1 = one bulk copy of the parent strand into the warp's bitmap,
-// 0 = register streaming six chunks deep (kept for comparison)
+// Copy rows of the bitmap builds: 1 = one bulk copy of the parent strand into the warp's bitmap,
+// 0 = register streaming six chunks deep (what the chunk-mask build, which has no bitmaps, always does)
 #ifndef CLOTHO_COPY_BULK
 #define CLOTHO_COPY_BULK 1
 #endif
