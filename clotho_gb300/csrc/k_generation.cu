@@ -1310,12 +1310,13 @@ __device__ __forceinline__ void gen_row_iv(const PopDev& P, const DevStatus& st,
 
 }  // namespace
 
-// Dynamic shared memory: [AND acc: aw][OR acc: aw][fixed mask: aw] u64 (aw = maxW in the
-// suffix-table builds, acc_words in the interval-classifier build), then (SUF) the warps' mask
-// bitmaps and one WarpSmem per warp.  A population whose current rows are wider than acc_words
-// (interval classifier) folds into its global AND/OR accumulators and reads its fixed mask from
-// global memory; the choice is made per population from its widths on the device, so a graph
-// captured for a large capacity keeps the shared accumulators while the rows are narrow.
+// Dynamic shared memory: [AND acc: aw][OR acc: aw][fixed mask: aw] u64 (aw = maxW in the bitmap
+// builds, acc_words in the chunk-mask and interval-classifier builds), then, in the bitmap builds,
+// the warps' mask bitmaps and one WarpSmem per warp, in the chunk-mask build one WarpSmem and
+// kCmCorr correction slots per warp.  A population whose current rows are wider than acc_words
+// (chunk-mask and interval builds) folds into its global AND/OR accumulators and reads its fixed
+// mask from global memory; the choice is made per population from its widths on the device, so a
+// graph captured for a large capacity keeps the shared accumulators while the rows are narrow.
 // PROF (suffix-table build only): per-phase cycle counters into ctl->phase.
 // NARROW (suffix-table build only): every row is at most 128 words.
 // CNT (suffix-table builds, shared accumulators): per-column counts of the child rows of the populations
@@ -1575,9 +1576,10 @@ k_generation(const PopDev* __restrict__ pops, uint32_t npops, WorkCtl* __restric
     }
 }
 
-// The suffix-table classifier runs when every population has a table (capacity <= kTableMaxSlots slots);
-// with every capacity <= kSufMaxSlots (maxW <= 1,024 words) in its per-warp bitmap builds, else in the
-// chunk-mask build.  Returns the error of
+// One launch of the generation kernel in the given build over the populations of that build (every
+// population in a launch of one kind; in a mixed batch the others' items are skipped): per-warp bitmap
+// masks (capacities <= kSufMaxSlots, maxW <= 1,024 words), chunk masks (other populations with a
+// suffix table) or the interval classifier.  Returns the error of
 // the shared-memory opt-in (the kernel is not launched then), else cudaSuccess.
 namespace {
 constexpr size_t kSmemLimit = 227u * 1024u;   // dynamic shared memory a block may opt into
