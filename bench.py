@@ -391,7 +391,7 @@ def stated_configs(cg, threads):
     fits = {"constant": oracle.FIT_CONSTANT, "gaussian_vs": oracle.FIT_GAUSSIAN_VS}
     peak, peak_kind = measured_peak()
     out = {}
-    for key, w, cpu_gens in (("neutral_wf", NEUTRAL_WF, 1000), ("qtl_selection", QTL_SELECTION, 2)):
+    for key, w, cpu_gens in (("neutral_wf", NEUTRAL_WF, 1000), ("qtl_selection", QTL_SELECTION, 6)):
         pop = cg.Population(w.N, w.max_alleles, w.T, fitness=w.fitness, fit_param=w.fit_param, mu=w.mu, rho=w.rho,
                             bias=w.bias, p_neutral=w.p_neutral, seed=20261203, max_fixed=1 << 20)
         pop.init(w.N)
