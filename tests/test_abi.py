@@ -49,6 +49,27 @@ def test_footprint_query_needs_no_gpu():
     assert b >= 2 * 2000 * 64 * 8
 
 
+def test_suffix_tables_by_capacity_and_crossover_rate():
+    # a population gets a suffix table (and its crossover plans) up to 65,536 allele slots, and up to 524,288
+    # slots when its rho is at most 1 (chunk masks); otherwise the interval classifier, without them.  The
+    # table alone is (A/64 + 1) x W words, so the footprints of rho 1 and rho 3 differ by at least that much
+    # above 65,536 slots, and not at all up to 65,536 or above 524,288
+    from clotho_gb300 import capi
+    L = capi.load()
+
+    def fp(A, rho):
+        d = capi.Desc(1000, A, 1, 4096, 4096, 4096, 0, 1, 1.0, 0.01, rho, 0.5, 0.5, 0.0, 1.0, 1)
+        return L.clotho_footprint_for(ctypes.byref(d))
+
+    for A in (4096, 65_536, 600_000):
+        assert fp(A, 1.0) == fp(A, 3.0), A
+    for A in (70_000, 200_000, 524_288):
+        W = (A + 511) // 512 * 8
+        W = (W + 63) // 64 * 64
+        slots = W * 64
+        assert fp(A, 1.0) - fp(A, 3.0) >= (slots // 64 + 1) * W * 8, A
+
+
 def test_oracle_exports_its_header():
     import oracle
     lib = ctypes.CDLL(oracle.build())
