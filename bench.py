@@ -443,8 +443,9 @@ def stated_configs(cg, threads):
                     stages[k] = stages.get(k, 0.0) + v
             dt = time.perf_counter() - t0
             orc.close()
-            cpu[name] = {"seq_gen_per_s": 2.0 * w.N * n / dt, "cores": thr, "generations": n, "s": dt,
-                         "stage_seconds": stages}
+            rate = 2.0 * w.N * n / dt
+            cpu[name] = {"seq_gen_per_s": rate, "cores": thr, "generations": n, "s": dt, "stage_seconds": stages,
+                         "derived_gbs": rate * 16.0 * info["W"] / 1e9}
         del rows
         out[key] = {"workload": w.name, "gpu": gpu, "cpu": cpu,
                     "cpu_sample": "oracle/clotho_oracle.cpp from the GPU run's final state (same rows, allele "
@@ -460,7 +461,7 @@ def single_core_rate(w, warmup=1, steps=2, N=None):
     width; the per-row cost does not depend on N)."""
     N = N or CPU_SAMPLE_N
     v, dt, info, _ = run_cpu_oracle(w, N, steps, warmup, 1)
-    return {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+    return {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "derived_gbs": v * 16.0 * info["B"] / 1e9,
             "sample": (f"oracle/clotho_oracle.cpp on 1 thread (the reference's default T=0), N={N} "
                        f"individuals, same allele load (A={info['A']}, W={info['B']} words/row), {steps} "
                        f"generations after {warmup} warm-up, {dt:.1f} s")}
@@ -488,7 +489,8 @@ def reference_arm(args, rank):
             "config": {"workload": w.name, "N": N, "T": w.T, "A": info["A"], "W_live": info["B"], "rho": w.rho,
                        "mu": w.mu, "fitness": w.fitness, "threads": threads, "same_config": N == w.N},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
-                             "stage_seconds": stages, "setup_seconds": t_setup},
+                             "stage_seconds": stages, "setup_seconds": t_setup,
+                             "derived_gbs": v * 16.0 * info["B"] / 1e9},
             "single_core": single_core_rate(w, N=min(CPU_SAMPLE_N, N)),
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -722,7 +724,9 @@ def main():
                "sample": (f"oracle/clotho_oracle.cpp on {threads} host threads, N={CPU_LEG_N} individuals, same "
                           f"allele load (A={oinfo['A']}, W={oinfo['B']}), 4 generations after 1 warm-up, "
                           f"{dt:.1f} s"),
-               "stage_seconds": stages, "single_core": single_core_rate(w)}
+               "stage_seconds": stages, "single_core": single_core_rate(w),
+               "derived_gbs": v * 16.0 * oinfo["B"] / 1e9,
+               "derived_gbs_note": "seq-gen/s x 16 B x the row width: the GPU roofline's algorithmic basis"}
 
     batched = serve = None
     if rank == 0 and world == 1 and not args.no_batched:

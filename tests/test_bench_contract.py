@@ -39,6 +39,10 @@ def test_reference_arm_line(monkeypatch):
     assert "N=300" in cb["sample"] and d["config"]["N"] == 300
     sc = d["single_core"]
     assert sc["cores"] == 1 and sc["value"] > 0 and "N=200" in sc["sample"]
+    # derived bandwidth on the GPU roofline's basis: seq-gen/s x 16 B x the row width in words
+    W = d["config"]["W_live"]
+    assert abs(cb["derived_gbs"] - d["value"] * 16.0 * W / 1e9) <= 1e-9 * cb["derived_gbs"]
+    assert sc["derived_gbs"] > 0
     e = d["e2e"]
     assert e == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["workload"].startswith("large_n")
