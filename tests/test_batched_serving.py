@@ -146,11 +146,12 @@ def test_shared_and_global_accumulators_in_one_batch():
     b.close()
 
 
-@pytest.mark.parametrize("cap", [8192, 1 << 14])
+@pytest.mark.parametrize("cap", [8192, 1 << 14, 70_000])
 def test_launch_shapes_do_not_change_results(cap):
     # every tuning knob (rows per item, the narrow build where rows are at most 128 words, blocks per SM of
     # the per-individual kernels) gives bit-identical rows, statistics and mean fitness; at 8,192 slots
-    # the narrow build runs unless switched off
+    # the narrow build runs unless switched off; at 70,000 slots the populations of rho <= 1 run the
+    # chunk-mask build and the other one the interval classifier
     G = 6
     outs = []
     for rpi, narrow, blocks in ((64, 1, 16), (1024, 0, 4), (256, 1, 24), (512, 0, 8)):
