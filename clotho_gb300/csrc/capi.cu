@@ -67,7 +67,7 @@ std::vector<size_t> sizes_of(const Geometry& g) {
         A * 4, A * 8, A * 4, A * 16,     // free_list, pos, age, eff (traits padded to 4)
         g.FXcap * 8ull, g.FXcap * 4ull, g.FXcap * T * 4ull,
         S * 32, S * 32, N * 32, N * 8, N * 8,    // zg[0], zg[1], zi, fit, cdf
-        (N / 1024 + 8) * 8, ((S > g.NB ? S : g.NB) / 1024 + 8) * 4ull,
+        (N / 1024 + 8) * 8, ((S > g.NB ? S : g.NB) / 1024 + 8) * 4ull, ((S > g.NB ? S : g.NB) / 1024 + 8) * 4ull,
         (S + 1) * 4 * 2ull,              // row_cnt, row_off
         S * 4, g.Mcap * 4ull, g.Mcap * 4ull,  // row_cur, row_mut, mut_slot
         (g.NB + 1ull) * 4 * 2, g.NB * 4ull, A * 8, A * 4, A * 4,  // bcnt+boff, bcur, bpos, bslot, rank
@@ -96,6 +96,11 @@ struct clotho_ctx {
     int num_sms = 152;
     cudaStream_t stream = nullptr, copy_stream = nullptr;
     cudaStream_t own_stream = nullptr;  // the context's own compute stream (stream may be the caller's)
+    // a step's parent selection and row ordering run on side_stream beside the allele-space work (mutation
+    // counts, free space, new alleles, ranks, suffix tables), forked after the step's header and joined
+    // before the row plans; a captured step keeps the two branches as parallel graph branches
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     // populations' device tables come from the context's own stream-ordered pool, which keeps freed
     // blocks for the next population (a serving loop adds and removes populations every few steps)
     cudaMemPool_t pool = nullptr;
@@ -249,7 +254,7 @@ int alloc_pop(clotho_ctx* ctx, const clotho_desc& d, PopHost** out) {
     b.fx_pos = (double*)ptr[k++]; b.fx_age = (uint32_t*)ptr[k++]; b.fx_eff = (float*)ptr[k++];
     b.zg[0] = (double*)ptr[k++]; b.zg[1] = (double*)ptr[k++];
     b.zi = (double*)ptr[k++]; b.fit = (double*)ptr[k++]; b.cdf = (double*)ptr[k++];
-    b.scan_part = (double*)ptr[k++]; b.scan_upart = (uint32_t*)ptr[k++];
+    b.scan_part = (double*)ptr[k++]; b.scan_upart = (uint32_t*)ptr[k++]; b.scan_opart = (uint32_t*)ptr[k++];
     b.row_cnt = (uint32_t*)ptr[k++];
     b.row_off = b.row_cnt + (g.Scap + 1);
     b.row_cur = (uint32_t*)ptr[k++]; b.row_mut = (uint32_t*)ptr[k++]; b.mut_slot = (uint32_t*)ptr[k++];
@@ -387,10 +392,15 @@ bool count_on(clotho_ctx* ctx, uint32_t fuse) {
 // The generation kernel over every population: one launch when all populations use the same build; in a
 // batch that mixes them, one launch per build (bitmap, chunk-mask, interval), each over its own populations,
 // so every population runs the build it runs alone.
-void launch_gen(clotho_ctx* ctx, const PopDev* pops, uint32_t npops, uint32_t fuse) {
+// ordered: the rows' processing order is already enqueued (the fused step's side branch).
+void launch_gen(clotho_ctx* ctx, const PopDev* pops, uint32_t npops, uint32_t fuse, bool ordered = false) {
     if (ctx->n_suf > 0) {  // per-row crossover plans of the suffix-table classifier (other populations skip it)
-        launch_plan(cfg(ctx), pops, npops, ctx->maxS);
-        ctx->launches += 6;  // order count, 3-kernel scan, order scatter, plan
+        if (!ordered) {
+            launch_order(cfg(ctx), pops, npops, ctx->maxS);
+            ctx->launches += 5;  // order count, 3-kernel scan, order scatter
+        }
+        launch_row_plan(cfg(ctx), pops, npops, ctx->maxS);
+        ctx->launches += 1;
     }
     const int prof = ctx->profiling ? (ctx->phase_clocks ? 2 : 1) : 0;
     const uint32_t kinds = (ctx->n_bm > 0) + (ctx->n_cm > 0) + (ctx->n_iv > 0);
@@ -470,13 +480,30 @@ void enqueue_fused_step(clotho_ctx* ctx, uint32_t set, bool philox) {
     ctx->pairs_set = set == 1u ? 1u : 0u;  // the device-drawn set (2) shares set 0's buffers
     launch_begin(L, pops, n, ctx->d_hdr[set], ctx->d_ctl);
     ensure_parent_acc(ctx, pops, n);
+    // side branch: parents (from the parent generation's fitness) and the rows' processing order (from the
+    // parents) read only the step header and the pairs, and write only the pairs, the ordering arrays and
+    // their own scan partials, none of which the main branch touches before the join
+    auto note = [ctx](cudaError_t e) {
+        if (e != cudaSuccess && ctx->launch_err == cudaSuccess) ctx->launch_err = e;
+    };
+    LaunchCfg Ls = L;
+    Ls.stream = ctx->side_stream;
+    note(cudaEventRecord(ctx->fork_ev, L.stream));
+    note(cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev, 0));
+    if (philox) launch_select_philox(Ls, pops, n);
+    if (ctx->n_suf > 0) {
+        launch_order(Ls, pops, n, ctx->maxS);
+        ctx->launches += 5;  // order count, 3-kernel scan, order scatter
+    }
+    note(cudaEventRecord(ctx->join_ev, ctx->side_stream));
+    // main branch: the child's allele space
     if (philox) launch_mut_counts_philox(L, pops, n, ctx->maxS);
     launch_fs_finalize(L, pops, n, count_on(ctx, kFuseMut | kFusePheno | kFuseFs));
     if (!philox) launch_mut_csr_tape(L, pops, n, ctx->maxS);
     launch_mut_resolve(L, pops, n);
     launch_ranks(L, pops, n, ctx->maxNB, ctx->maxW_suf, ctx->n_suf > 0);
-    if (philox) launch_select_philox(L, pops, n);
-    launch_gen(ctx, pops, n, kFuseMut | kFusePheno | kFuseFs);
+    note(cudaStreamWaitEvent(L.stream, ctx->join_ev, 0));
+    launch_gen(ctx, pops, n, kFuseMut | kFusePheno | kFuseFs, true);
     launch_individuals(L, pops, n);
     launch_cdf(L, pops, n, ctx->maxN);
     launch_end(L, pops, n);
@@ -548,7 +575,10 @@ int clotho_create(const clotho_desc* desc, clotho_ctx** out) {
         return CLOTHO_E_CUDA;
     }
     if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
         clotho_destroy(ctx);  // releases whichever stream was made
         return CLOTHO_E_CUDA;
@@ -622,6 +652,7 @@ int clotho_destroy(clotho_ctx* ctx) {
     if (!ctx) return CLOTHO_E_ARG;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    if (ctx->side_stream) cudaStreamSynchronize(ctx->side_stream);
     for (PopHost* p : ctx->pops) free_pop(ctx, p);
     ctx->pops.clear();
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
@@ -647,6 +678,9 @@ int clotho_destroy(clotho_ctx* ctx) {
     if (ctx->t1) cudaEventDestroy(ctx->t1);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
+    if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+    if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
     delete ctx;
     return 0;
 }

@@ -79,6 +79,7 @@ struct PopDev {
     double*   cdf;         // [Ncap]
     double*   scan_part;   // [Ncap / 1024 + 2]
     uint32_t* scan_upart;  // [Scap / 1024 + 2]
+    uint32_t* scan_opart;  // [Scap / 1024 + 2] the row-ordering scan's own partials (it runs beside the others)
     uint32_t* pairs;       // [2 * Ncap]
     uint8_t*  swap;        // [Scap]
     uint32_t* ev_off;      // [Scap + 1]
@@ -328,6 +329,10 @@ void launch_uscan_buckets(const LaunchCfg&, const PopDev* pops, uint32_t npops, 
 void launch_uscan_order(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
 
 void launch_plan(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
+// the two halves of launch_plan: the rows' processing order (by parent; needs only the pairs and the step
+// header) and the per-row plans (needs the ranks, the suffix tables and the new alleles as well)
+void launch_order(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
+void launch_row_plan(const LaunchCfg&, const PopDev* pops, uint32_t npops, uint32_t maxS);
 int init_recip_step();  // k_step.cu's copy of the reciprocal table
 int init_recip_gen();   // k_generation.cu's copy
 

@@ -1888,12 +1888,20 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
 
 int init_recip_gen() { return fill_recip_table(); }
 
-void launch_plan(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
+void launch_order(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
     const dim3 g = pop_grid(npops, blocks_for(maxS, 256), L.num_sms, 8);
     k_ord_count<<<g, 256, 0, L.stream>>>(pops, npops);
     launch_uscan_order(L, pops, npops, maxS);
     k_ord_scatter<<<g, 256, 0, L.stream>>>(pops, npops);
-    k_row_plan<<<g, 256, 0, L.stream>>>(pops, npops);
+}
+
+void launch_row_plan(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
+    k_row_plan<<<pop_grid(npops, blocks_for(maxS, 256), L.num_sms, 8), 256, 0, L.stream>>>(pops, npops);
+}
+
+void launch_plan(const LaunchCfg& L, const PopDev* pops, uint32_t npops, uint32_t maxS) {
+    launch_order(L, pops, npops, maxS);
+    launch_row_plan(L, pops, npops, maxS);
 }
 
 // ---------------------------------------------------------------------------

@@ -100,17 +100,18 @@ struct ScanSel {
     uint32_t* cur;
     uint32_t L;      // elements (counts) to scan; off gets L entries
     uint32_t ncur;   // cursors to zero
+    uint32_t* part;  // chunk partials (the ordering scan has its own: it runs beside the other two)
 };
 // which == 0: per-row mutation counts; 1: position buckets; 2: rows per ordering key.  The ordering keys
 // are parent individuals (below pN, which exceeds 2N when the population shrinks more than twofold) or, in
 // the measurement orders, below 2N or N + pN: the scan covers max(2N, N + pN) keys, at most 2 * Ncap.
 __device__ inline ScanSel scan_sel(const PopDev& P, int which) {
-    if (which == 0) return ScanSel{P.row_cnt, P.row_off, P.row_cur, 2u * P.st->N + 1u, 2u * P.st->N};
+    if (which == 0) return ScanSel{P.row_cnt, P.row_off, P.row_cur, 2u * P.st->N + 1u, 2u * P.st->N, P.scan_upart};
     if (which == 2) {
         const uint32_t keys = max(2u * P.st->N, P.st->N + P.st->pN);
-        return ScanSel{P.ord_cnt, P.ord_off, P.ord_cur, keys + 1u, keys};
+        return ScanSel{P.ord_cnt, P.ord_off, P.ord_cur, keys + 1u, keys, P.scan_opart};
     }
-    return ScanSel{P.bcnt, P.boff, P.bcur, P.NB + 1u, P.NB};
+    return ScanSel{P.bcnt, P.boff, P.bcur, P.NB + 1u, P.NB, P.scan_upart};
 }
 
 __global__ void __launch_bounds__(1024) k_uscan_a(const PopDev* __restrict__ pops, uint32_t npops, int which) {
@@ -131,7 +132,7 @@ __global__ void __launch_bounds__(1024) k_uscan_a(const PopDev* __restrict__ pop
             if (threadIdx.x == 0) {
                 uint32_t t = 0;
                 for (int i = 0; i < 32; ++i) t += s_w[i];
-                P.scan_upart[c] = t;
+                Z.part[c] = t;
             }
             __syncthreads();
         }
@@ -148,8 +149,8 @@ __global__ void k_uscan_b(const PopDev* __restrict__ pops, uint32_t npops, int w
     const uint32_t nch = (L + kScanChunk - 1) / kScanChunk;
     uint32_t acc = 0;
     for (uint32_t c = 0; c < nch; ++c) {
-        uint32_t t = P.scan_upart[c];
-        P.scan_upart[c] = acc;
+        uint32_t t = Z.part[c];
+        Z.part[c] = acc;
         acc += t;
     }
 }
@@ -175,7 +176,7 @@ __global__ void __launch_bounds__(1024) k_uscan_c(const PopDev* __restrict__ pop
             __syncthreads();
             uint32_t woff = 0;
             for (uint32_t i = 0; i < (threadIdx.x >> 5); ++i) woff += s_w[i];
-            uint32_t run = P.scan_upart[c] + woff + incl - s;
+            uint32_t run = Z.part[c] + woff + incl - s;
             for (uint32_t k = 0; k < 4; ++k) {
                 if (b + k < L) {
                     Z.off[b + k] = run;
