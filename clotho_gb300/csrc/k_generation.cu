@@ -1822,13 +1822,20 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
                 }
             }
             if (!live) continue;
+            // what the plan entry needs besides the breakpoints, fetched before the breakpoint work so that
+            // their round trips overlap it: the processing position, the new alleles' CSR range, and the
+            // carried phenotypes of both parent strands (one 64-byte line; the gather direction picks one)
+            const uint32_t at = P.ord_pos[g];
+            const uint32_t mo = P.row_off[g], mend = P.row_off[g + 1u];
+            const uint32_t topr = 2u * pind + (swap ? 1u : 0u);
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(P.zg[st.cur ^ 1u] + (size_t)(topr & ~1u) * 4u));
             if (E > kMaxEvDevice) {
                 flags = kPlanLong;  // tape rows with very long event lists: direct compares
             } else if (E > 0) {
                 uint32_t* cr = E <= kPlanSmemEv ? s_cr[threadIdx.x] : P.plan_cr + base;
-                // the chunk-mask build (which a batch may run for any of its suffix-table populations)
-                // classifies rows of more than kCmMaxEv breakpoints by direct compares against their
-                // positions, which device-drawn rows keep in the event list for it (rare: E > 16)
+                // the chunk-mask build classifies rows of more than kCmMaxEv breakpoints by direct compares
+                // against their positions, which device-drawn rows keep in the event list for it (every
+                // population's, to keep the plan kernel uniform; rare: E > 16)
                 const bool keep_pos = philox && E > kCmMaxEv;
                 for (uint32_t k = 0; k < E; k += 2u) {
                     double e0, e1 = 0.0;
@@ -1871,13 +1878,10 @@ __global__ void __launch_bounds__(256) k_row_plan(const PopDev* __restrict__ pop
                 E = 0;
                 flags = 0;
             }
-            const uint32_t at = P.ord_pos[g];
-            const uint32_t topr = 2u * pind + (swap ? 1u : 0u);
             P.plan_row[at] = make_uint4(g, topr, base, E | (flags << kPlanFlagShift));
             // what the row's set-up would otherwise fetch after its plan: the new alleles' CSR
             // range and the carried phenotype's base strand value less the fixed effects
-            const uint32_t mo = P.row_off[g];
-            P.plan_mut[at] = make_uint2(mo, P.row_off[g + 1u] - mo);
+            P.plan_mut[at] = make_uint2(mo, mend - mo);
             const uint32_t zs = ((flags & kPlanInv) && st.nz_eff != 0) ? topr ^ 1u : topr;
             const double* zp = P.zg[st.cur ^ 1u] + (size_t)zs * 4u;
 #pragma unroll
